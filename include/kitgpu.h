@@ -1,0 +1,170 @@
+/*
+ * kitgpu.h -- C ABI of the GB300 (sm_103a) discrete-velocity-method time step.
+ *
+ * This library replaces the Julia CPU hot path of KitBase.jl (v0.9.31) for the
+ * reduced-distribution forms 1D2F1V and 2D2F2V:
+ *   reconstruct!  src/Solver/solver_reconstruction.jl:101-153 (1D), :475-620 (2D)
+ *   evolve!       src/Solver/solver_evolution.jl:64-89 (1D), :608-679 (2D)
+ *                 + evolve_boundary! src/Solver/evolve_boundary.jl:4-178
+ *   update!       src/Solver/solver_update.jl:61-93 (1D), :193-246 (2D)
+ *                 + update_boundary! src/Solver/update_boundary.jl:6-61, :172-306
+ *   step!         src/Solver/step_2f.jl:6-64 (1D2F1V), :179-249 (2D2F2V)
+ * with the kinetic fluxes flux_kfvs!, flux_kcu!, flux_ugks! and
+ * flux_boundary_maxwell! (src/Flux/flux_*.jl files) and BGK / Shakhov relaxation.
+ *
+ * Conventions
+ *  - Every function returns an int status: KB_OK (0) or a negative KB_ERR_*.
+ *    kb_last_error() returns a thread-local message for the last failure.
+ *  - Plain pointers and sizes only.  All pointers named host_* or documented as
+ *    host arrays point to host memory; the library copies them.
+ *  - Cell order: x fastest, ghost layers included:
+ *        cell = (j + ngy) * (nx + 2*ngx) + (i + ngx),  i in [-ngx, nx+ngx), j likewise
+ *    (0-based; the reference's 1-based ctr[i, j] is cell (i-1, j-1)).
+ *    This is the column-major order of the reference's OffsetArray{ControlVolume2F}.
+ *  - Velocity order: iu fastest, v = iu + nu * iv (column-major order of the
+ *    reference's u[i, j] matrices, src/Phase/phase_velocity.jl:128-258).
+ *  - Per-cell vectors: w and prim have dim + 2 entries (3 in 1D, 4 in 2D).
+ *  - A handle owns one CUDA stream.  A handle is not thread-safe; separate
+ *    handles may be driven from separate host threads.
+ */
+#ifndef KITGPU_H
+#define KITGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KB_OK 0
+#define KB_ERR_ARG (-1)       /* bad argument (null pointer, out-of-range value) */
+#define KB_ERR_CONFIG (-2)    /* unsupported or inconsistent configuration */
+#define KB_ERR_CUDA (-3)      /* CUDA runtime failure (message in kb_last_error) */
+#define KB_ERR_NUMERIC (-4)   /* non-finite or non-positive rho / lambda after a step */
+#define KB_ERR_TIMEOUT (-5)   /* a bounded device wait gave up */
+#define KB_ERR_NOMEM (-6)     /* device allocation failed */
+#define KB_ERR_STATE (-7)     /* call order violated (e.g. update before evolve) */
+
+/* flux solver: KS.set.flux, dispatched at src/Solver/solver_evolution.jl:80 */
+enum { KB_FLUX_KFVS = 0, KB_FLUX_KCU = 1, KB_FLUX_UGKS = 2 };
+/* collision model: KS.set.collision, tested at src/Solver/step_2f.jl:34 */
+enum { KB_COLL_BGK = 0, KB_COLL_SHAKHOV = 1 };
+/* boundary condition per side: KS.set.boundary (src/Solver/update_boundary.jl) */
+enum { KB_BC_FIX = 0, KB_BC_EXTRA = 1, KB_BC_PERIOD = 2, KB_BC_MAXWELL = 3 };
+/* storage / arithmetic form of the distributions */
+enum {
+  KB_PREC_FP64 = 0,  /* plain form: everything in FP64 */
+  KB_PREC_FP32 = 1   /* h, b and pointwise fluxes in FP32; moments, w, prim, q in FP64 */
+};
+
+/* Solver configuration: the fields of Setup / PSpace / Gas that the DVM step reads
+ * (src/Struct/struct_setup.jl:106-119, src/Geometry/geo_struct.jl:10-186,
+ *  src/Struct/struct_property.jl:51-64). */
+typedef struct kb_config {
+  int32_t dim;           /* 1 (1D2F1V) or 2 (2D2F2V) */
+  int32_t nx, ny;        /* physical cells; ny = 1 in 1D */
+  int32_t ngx, ngy;      /* ghost layers (nxg, nyg); ngy = 0 in 1D */
+  int32_t nu, nv;        /* velocity points per axis; nv = 1 in 1D */
+  int32_t flux;          /* KB_FLUX_* */
+  int32_t collision;     /* KB_COLL_* */
+  int32_t bc[4];         /* x-left, x-right, y-down, y-up (1D uses bc[0], bc[1]) */
+  int32_t interp_order;  /* 1: no reconstruction, 2: van Leer slopes */
+  int32_t precision;     /* KB_PREC_* */
+  double x0, x1, y0, y1; /* physical domain; cells are uniform */
+  double umax, vmax;     /* vs.u1 / vs.v1, used by the CFL time step */
+  double K;              /* internal degrees of freedom (inK) */
+  double gamma;          /* heat capacity ratio */
+  double mu_ref;         /* reference viscosity (ref_vhs_vis) */
+  double omega;          /* VHS viscosity index (gas.omega) */
+  double Pr;             /* Prandtl number */
+} kb_config_t;
+
+typedef struct kb_handle kb_handle_t;
+
+/* Library version string. */
+const char* kb_version(void);
+
+/* Message describing the last failing call on this host thread. */
+const char* kb_last_error(void);
+
+/* Build a solver on the current CUDA device.  u, v, weights are host arrays of
+ * nu*nv velocity abscissae and quadrature weights (VSpace1D / VSpace2D fields);
+ * v may be NULL in 1D.  Replaces SolverSet construction + init_fvm storage
+ * (src/Solver/solver_set.jl:73-117, src/Solver/solver_init.jl:119-141, :285-325). */
+int kb_create(const kb_config_t* cfg, const double* u, const double* v,
+              const double* weights, kb_handle_t** out);
+
+/* Release every device allocation of the handle. */
+int kb_destroy(kb_handle_t* h);
+
+/* Maxwell wall primitive states for one side, in the global frame, one per
+ * boundary face: side 0/1 (x-left/right) take ny faces, side 2/3 (y-down/up)
+ * take nx faces; each face has dim+2 values [rho, U, (V,) lambda] (rho unused).
+ * These are the values KS.ib.bc(xc, yc, p) returns at the face midpoints
+ * (src/Solver/evolve_boundary.jl:4-178). */
+int kb_set_wall(kb_handle_t* h, int side, const double* host_prim);
+
+/* Copy the whole cell state (all cells incl. ghosts) host -> device.
+ * w, prim: [ncell][dim+2]; h, b: [ncell][nu*nv].  FP32 handles round h, b
+ * on the device.  Replaces the deep copies in ControlVolume(W, PRIM, H, B, ND)
+ * (src/Struct/struct_ctr.jl:207-241). */
+int kb_upload_state(kb_handle_t* h, const double* w, const double* prim,
+                    const double* hdist, const double* bdist);
+
+/* Copy the whole cell state device -> host (same layout as kb_upload_state).
+ * Any pointer may be NULL to skip that field.  Feeds write_jld / extract_sol. */
+int kb_download_state(kb_handle_t* h, double* w, double* prim, double* hdist,
+                      double* bdist);
+
+/* CFL time step of the current state: timestep(KS, ctr, simTime)
+ * (src/Solver/solver_main.jl:240-288 1D, :290-342 2D). */
+int kb_timestep(kb_handle_t* h, double cfl, double sim_time, double max_time,
+                double* dt_out);
+
+/* reconstruct!: van Leer slopes of w for every cell.  The slopes of h and b
+ * are formed on the fly inside kb_evolve / kb_update, so this stage only
+ * refreshes the w slopes that KCU / UGKS read. */
+int kb_reconstruct(kb_handle_t* h);
+
+/* evolve!: interface fluxes fw of every face (flux chosen by cfg.flux) plus
+ * Maxwell wall fluxes.  Requires kb_reconstruct first when interp_order = 2. */
+int kb_evolve(kb_handle_t* h, double dt);
+
+/* update!: finite-volume update of w, BGK / Shakhov relaxation of h and b,
+ * boundary cells and ghost fill.  residual (host, dim+2 doubles, may be NULL)
+ * receives the residual of this step (src/Solver/solver_update.jl:86-88). */
+int kb_update(kb_handle_t* h, double dt, double* residual);
+
+/* nsteps fused time steps reconstruct! -> evolve! -> update! with a fixed dt.
+ * residual (host, dim+2 doubles, may be NULL) receives the last step's residual.
+ * Replaces the body of the solve! loop (src/Solver/solver_main.jl:32-72). */
+int kb_step(kb_handle_t* h, double dt, int32_t nsteps, double* residual);
+
+/* Face fluxes of the last kb_evolve, materialised for inspection: fw in the
+ * global frame [nface][dim+2], fh, fb [nface][nu*nv].  x faces first
+ * ((nx+1)*ny, i fastest), then y faces (nx*(ny+1)).  Faces that the
+ * reference never computes for this configuration are returned as zero.
+ * Any pointer may be NULL.  (face.fw / face.fh / face.fb of Interface2F,
+ * src/Struct/struct_face.jl:56-65.) */
+int kb_download_faces(kb_handle_t* h, double dt, double* fw, double* fh, double* fb);
+
+/* Slopes sw [ncell][dim][dim+2], sh, sb [ncell][dim][nu*nv] as reconstruct!
+ * would store them (ctr.sw / ctr.sh / ctr.sb; 2D slopes use the last index
+ * for the direction, src/Data/data_array.jl:15-50).  Any pointer may be NULL. */
+int kb_download_slopes(kb_handle_t* h, double* sw, double* sh, double* sb);
+
+/* Status word of the handle: KB_OK, or KB_ERR_NUMERIC once a step produced a
+ * non-finite or non-positive density / lambda. */
+int kb_status(kb_handle_t* h);
+
+/* Device bytes held by the handle. */
+int kb_device_bytes(kb_handle_t* h, int64_t* bytes);
+
+/* Number of kernel launches issued by this handle since creation. */
+int kb_launch_count(kb_handle_t* h, int64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KITGPU_H */

@@ -1,0 +1,66 @@
+// kb_kernels.cuh -- launch interface between the C ABI (kb_abi.cu) and the
+// DVM kernels (kb_kernels.cu).
+#pragma once
+
+#include "kb_device.cuh"
+
+namespace kb {
+
+// Device buffers of one solve (owned by kb_handle, see kb_abi.cu).
+struct DevState {
+  Geo g;
+  int prec;   // 0: FP64, 1: FP32 split
+  int flux, coll;
+  const double* u;  // velocity tables [vstride]
+  const double* v;
+  const double* wt;
+  const float* uf;
+  const float* vf;
+  const float* wtf;
+  void* h[2];       // [ncell][vstride] (double or float)
+  void* b[2];
+  int cur;          // index of the current state in h / b
+  double* w;        // [ncell][4]
+  double* prim;     // [ncell][4]
+  double* sw;       // [ncell][2][4]
+  FaceParam* fp;    // [nface]
+  FaceParamF* fpf;  // [nface]
+  double* fw;       // [nface][4] global frame
+  double* wall;     // [nface][4] wall prim, global frame (only wall faces read)
+  double* rhow;     // [nface] Maxwell wall density
+  signed char* kind;  // [nface] 0 none, 1 interior, 2 wall
+  double* q;        // [ncell][2]
+  CellParam* cp;    // [ncell]
+  CellParamF* cpf;  // [ncell]
+  double* blockres; // [nblocks][16] residual partials
+  double* residual; // [4]
+  int* status;      // [1]
+  int nface_x, nface_y;
+  int ncell;
+  int res_blocks;   // number of blocks of k_cell_param
+};
+
+// Face classification for the current configuration (host computes, uploads).
+void face_kinds_host(const Geo& g, signed char* kind);
+
+// One time step (reconstruct! -> evolve! -> update!) on `stream`.
+// Returns the number of kernel launches.
+int launch_reconstruct(DevState& s, cudaStream_t st);
+int launch_evolve(DevState& s, double dt, cudaStream_t st);
+int launch_update(DevState& s, double dt, cudaStream_t st);
+
+// Materialise face fluxes fh / fb (double) of the current state, and slopes.
+int launch_faces_dump(DevState& s, double dt, double* fh, double* fb, cudaStream_t st);
+int launch_slopes_dump(DevState& s, double* sh, double* sb, cudaStream_t st);
+
+// Conversion kernels for upload / download of distributions.
+int launch_convert_in(void* dst, int prec, const double* src, long ncell, int nvel, int vstride,
+                      cudaStream_t st);
+int launch_convert_out(double* dst, int prec, const void* src, long ncell, int nvel,
+                       int vstride, cudaStream_t st);
+int launch_pack_w(double* dst4, const double* src, long ncell, int nw, cudaStream_t st);
+
+// CFL time step (timestep, src/Solver/solver_main.jl:240-342): tmax into out.
+int launch_timestep(const DevState& s, double umax, double vmax, double* out, cudaStream_t st);
+
+}  // namespace kb
