@@ -218,6 +218,8 @@ int kb_create(const kb_config_t* cfg, const double* u, const double* v, const do
   ALLOC(h->s.q, double, h->ncell * 2);
   ALLOC(h->s.cp, kb::CellParam, h->ncell);
   ALLOC(h->s.cpf, kb::CellParamF, h->ncell);
+  ALLOC(h->s.fc, kb::FaceCoef32, h->nface);
+  ALLOC(h->s.cc, kb::CellCoef32, h->ncell);
   ALLOC(h->s.blockres, double, (size_t)h->s.res_blocks * 16);
   ALLOC(h->s.residual, double, 4);
   ALLOC(h->s.status, int, 1);
@@ -234,6 +236,9 @@ int kb_create(const kb_config_t* cfg, const double* u, const double* v, const do
   cudaMemset(h->s.wall, 0, sizeof(double) * h->nface * 4);
   cudaMemset(h->s.rhow, 0, sizeof(double) * h->nface);
   cudaMemset(h->s.status, 0, sizeof(int));
+  cudaMemset(h->s.fc, 0, sizeof(kb::FaceCoef32) * h->nface);
+  cudaMemset(h->s.cc, 0, sizeof(kb::CellCoef32) * h->ncell);
+  cudaMemset(h->s.fp, 0, sizeof(kb::FaceParam) * h->nface);
   cudaMemset(h->s.residual, 0, sizeof(double) * 4);
 
   // velocity tables (padded entries have zero weight)
@@ -338,6 +343,11 @@ int kb_upload_state(kb_handle_t* h, const double* w, const double* prim, const d
   h->s.cur = 0;
   KB_TRY(dist_in(h, h->s.h[0], hdist));
   KB_TRY(dist_in(h, h->s.b[0], bdist));
+  // both ping-pong buffers start equal: ghost cells of fix / Maxwell solves are
+  // never rewritten, so the second buffer must hold them too
+  size_t dist = (size_t)h->ncell * h->vstride * (h->s.prec == KB_PREC_FP64 ? 8 : 4);
+  KB_CUDA(cudaMemcpyAsync(h->s.h[1], h->s.h[0], dist, cudaMemcpyDeviceToDevice, h->stream));
+  KB_CUDA(cudaMemcpyAsync(h->s.b[1], h->s.b[0], dist, cudaMemcpyDeviceToDevice, h->stream));
   KB_TRY(sync(h));
   h->evolved = false;
   return KB_OK;

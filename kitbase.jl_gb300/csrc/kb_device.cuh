@@ -45,7 +45,7 @@ struct FaceParam {
   double mult;      // factor applied to the discrete moments (len or 1)
   double len;       // face length (1 in 1D)
   double Mxi2;      // <xi^4> moment of the interface Maxwellian
-  double pad;
+  double tr[2];     // transport coefficients incl. len: Th = tr0 un h_face - tr1 un^2 sh
 };
 
 // FP32 copy of the per-v coefficients of FaceParam, read by the FP32 kernels.
@@ -77,6 +77,42 @@ struct CellParamF {
   float rho_n, U, V, lam, cB, dtau, inv;
   float o_rho_n, oU, oV, olam, ocB, sf0, sf1;  // sf0/1 = sfac * q0/1
   int upd, coll;
+};
+
+// FP32 coefficient block of one face for the velocity-owning kernels.  With
+// face-frame velocity (un, ut), c2 = un^2 + ut^2 and the monomials
+// m = (un, un^2, un^3, un^2 ut, un^2 c2, un ut, un c2):
+//   H  = 2^(E.x + E.y un + E.z ut + E.w c2)            (interface Maxwellian)
+//   fh = H (C1 m1 + ... + C7 m7) + T.x un h_f - T.y un^2 dh
+//   fb = H (D1 m1 + ... + D7 m7) + T.x un b_f - T.y un^2 db
+// where h_f is the upwind face value and dh the unscaled van Leer slope
+// (slope * dx), T.y already divided by dx; len is folded in.  C2..C5 and
+// D2..D5 depend on the upwind side (aL for un >= 0, aR otherwise).
+// For a Maxwell wall face: E is the wall Maxwellian, T.x = len dt,
+// T.z = K / (2 lambda_w), T.w = rot.
+struct __align__(16) FaceCoef32 {
+  float4 E;
+  float4 T;   // T3, T4 / dx, C1, D1
+  float4 G;   // C6, C7, D6, D7
+  float4 Cp;  // C2..C5 for un >= 0
+  float4 Dp;  // D2..D5 for un >= 0
+  float4 Cm;  // C2..C5 for un < 0
+  float4 Dm;  // D2..D5 for un < 0
+};
+
+// FP32 coefficients of the pointwise cell update (velocity (u, v), c2):
+//   M   = 2^(EM.x + EM.y u + EM.z v + EM.w c2),  MB = M A.x
+//   OH  = 2^(EO.x + EO.y u + EO.z v + EO.w c2)   (old Maxwellian, Shakhov)
+//   cq  = Q.x + Q.y u + Q.z v,  tl = TL.x + TL.y u + TL.z v + TL.w c2
+//   MH += cq (tl - 5) OH,  MB += cq (tl - 3) OH Q.w
+//   h   = (h + div * A.w + A.y MH) * A.z
+// Cells left unchanged carry A = (0, 0, 1, 0), Q = 0 and EM.x = -200.
+struct __align__(16) CellCoef32 {
+  float4 EM;
+  float4 A;   // cB, dt/tau, 1/(1 + dt/tau), 1/ds
+  float4 EO;
+  float4 Q;   // Q0, Q1, Q2, old cB
+  float4 TL;
 };
 
 __host__ __device__ inline int cell_index(const Geo& g, int i, int j) {

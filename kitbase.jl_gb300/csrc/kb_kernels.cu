@@ -10,58 +10,9 @@
 #include <stdio.h>
 
 #include "kb_kernels.cuh"
+#include "kb_flux.cuh"
 
 namespace kb {
-
-// ----------------------------------------------------------------- helpers
-
-__host__ __device__ inline int face_count(const Geo& g) {
-  return (g.nx + 1) * g.ny + (g.D == 2 ? g.nx * (g.ny + 1) : 0);
-}
-
-// Face f -> direction d, left cell, right cell (cell indices incl. ghosts),
-// index i (x position of the face / cell), j, and the step between cells along d.
-struct FaceGeo {
-  int d, cL, cR, step, iL, iR;  // iL/iR: index along d of the two cells
-  int fi, fj;                   // face coordinates
-};
-__host__ __device__ inline FaceGeo face_geo(const Geo& g, int f) {
-  FaceGeo r;
-  int nfx = (g.nx + 1) * g.ny;
-  if (f < nfx) {
-    r.d = 0;
-    r.fi = f % (g.nx + 1);
-    r.fj = f / (g.nx + 1);
-    r.cL = cell_index(g, r.fi - 1, r.fj);
-    r.cR = r.cL + 1;
-    r.step = 1;
-    r.iL = r.fi - 1;
-    r.iR = r.fi;
-  } else {
-    int q = f - nfx;
-    r.d = 1;
-    r.fi = q % g.nx;
-    r.fj = q / g.nx;
-    r.cL = cell_index(g, r.fi, r.fj - 1);
-    r.cR = cell_index(g, r.fi, r.fj);
-    r.step = g.nxt;
-    r.iL = r.fj - 1;
-    r.iR = r.fj;
-  }
-  return r;
-}
-
-// Face length: vertex distance of PSpace2D (src/Geometry/geo_struct.jl:101-107);
-// for x faces it depends on the row, for y faces on the column.
-__host__ __device__ inline double face_len(const Geo& g, int d, int fi, int fj) {
-  if (g.D == 1) return 1.0;
-  if (d == 0) {
-    double y = g.y0 + (fj + 1 - 0.5) * g.dy;
-    return fabs((y + 0.5 * g.dy) - (y - 0.5 * g.dy));
-  }
-  double x = g.x0 + (fi + 1 - 0.5) * g.dx;
-  return fabs((x + 0.5 * g.dx) - (x - 0.5 * g.dx));
-}
 
 // Classification of every face (0 not computed, 1 interior flux, 2 Maxwell wall):
 // evolve! computes faces idx0:idx1 (all faces when ghosts exist, interior
@@ -79,152 +30,6 @@ void face_kinds_host(const Geo& g, signed char* kind) {
     int side = r.d == 0 ? (pos == 0 ? 0 : (pos == nn ? 1 : -1)) : (pos == 0 ? 2 : (pos == nn ? 3 : -1));
     if (side >= 0 && g.bc[side] == BC_MAXWELL) k = 2;
     kind[f] = k;
-  }
-}
-
-template <typename R>
-__device__ __forceinline__ R dscale(double d);
-template <>
-__device__ __forceinline__ double dscale<double>(double d) { return d; }
-template <>
-__device__ __forceinline__ float dscale<float>(double d) { return float(1.0 / d); }
-
-template <typename R>
-__device__ __forceinline__ const R* vtab(const DevState& s, int which);
-template <>
-__device__ __forceinline__ const double* vtab<double>(const DevState& s, int which) {
-  return which == 0 ? s.u : (which == 1 ? s.v : s.wt);
-}
-template <>
-__device__ __forceinline__ const float* vtab<float>(const DevState& s, int which) {
-  return which == 0 ? s.uf : (which == 1 ? s.vf : s.wtf);
-}
-
-// Upwind face state of one distribution at one velocity: the reconstructed
-// value of the upwind cell (h + s dx/2 from the left, h - s dx/2 from the
-// right) and that cell's slope (flux_kfvs.jl:35-63 / :98-140 wrappers).
-template <typename R>
-__device__ __forceinline__ R upwind_state(const R* __restrict__ q, long vs, int up, int step,
-                                          int rule, bool left, int v, R dsc, R dxh, R& slope) {
-  R q0 = q[(long)up * vs + v];
-  R qm = (rule == 1 || rule == 3) ? q[(long)(up - step) * vs + v] : R(0);
-  R qp = (rule == 1 || rule == 2) ? q[(long)(up + step) * vs + v] : R(0);
-  R s = slope_of<R>(rule, qm, q0, qp, dsc);
-  slope = s;
-  return left ? q0 + s * dxh : q0 - s * dxh;
-}
-
-// Per-face coefficients in the storage precision.
-template <typename R>
-struct FP {
-  R rho_n, U, V, lam, cB, Mxi2, len;
-  R Mt[5];
-  R aL[4], aR[4], aT[4];
-};
-template <typename R>
-__device__ __forceinline__ FP<R> load_fp(const DevState& s, int f);
-template <>
-__device__ __forceinline__ FP<double> load_fp<double>(const DevState& s, int f) {
-  const FaceParam& p = s.fp[f];
-  FP<double> r;
-  double lam = p.prim[3];
-  r.rho_n = s.g.D == 1 ? p.prim[0] * sqrt(lam / PI) : p.prim[0] * (lam / PI);
-  r.U = p.prim[1];
-  r.V = p.prim[2];
-  r.lam = lam;
-  r.cB = s.g.K / (2.0 * lam);
-  r.Mxi2 = p.Mxi2;
-  r.len = p.len;
-  for (int k = 0; k < 5; ++k) r.Mt[k] = p.Mt[k];
-  for (int k = 0; k < 4; ++k) {
-    r.aL[k] = p.aL[k];
-    r.aR[k] = p.aR[k];
-    r.aT[k] = p.aT[k];
-  }
-  return r;
-}
-template <>
-__device__ __forceinline__ FP<float> load_fp<float>(const DevState& s, int f) {
-  const FaceParamF& p = s.fpf[f];
-  FP<float> r;
-  r.rho_n = p.rho_n;
-  r.U = p.U;
-  r.V = p.V;
-  r.lam = p.lam;
-  r.cB = p.cB;
-  r.Mxi2 = p.Mxi2;
-  r.len = p.len;
-  for (int k = 0; k < 5; ++k) r.Mt[k] = p.Mt[k];
-  for (int k = 0; k < 4; ++k) {
-    r.aL[k] = p.aL[k];
-    r.aR[k] = p.aR[k];
-    r.aT[k] = p.aT[k];
-  }
-  return r;
-}
-
-// Pointwise interface flux at one velocity (face-local frame).  Returns the
-// full fluxes fh, fb and the transport parts Th, Tb whose moments form the
-// discrete part of fw.
-//   KFVS  flux_kfvs.jl:303-337 (1D), :654-700 (2D)
-//   KCU   flux_kcu.jl:463-530 (1D), :898-970 (2D)
-//   UGKS  flux_ugks.jl:8-114 (1D), :121-253 (2D)
-template <typename R, int FLUX, int D>
-__device__ __forceinline__ void face_flux(const FP<R>& P, R dt, R un, R ut, bool pos, R h, R b,
-                                          R sh, R sb, R& fh, R& fb, R& Th, R& Tb) {
-  if (FLUX == FLUX_KFVS) {
-    R a = dt * un;
-    R c = R(0.5) * (dt * dt) * (un * un);
-    fh = a * h - c * sh;
-    fb = a * b - c * sb;
-    if (D == 2) {
-      fh *= P.len;
-      fb *= P.len;
-    }
-    Th = fh;
-    Tb = fb;
-  } else {
-    R du = un - P.U;
-    R e = du * du;
-    if (D == 2) {
-      R dv = ut - P.V;
-      e += dv * dv;
-    }
-    R H = P.rho_n * mexp(-P.lam * e);
-    R B = H * P.cB;
-    if (FLUX == FLUX_KCU) {
-      Th = P.Mt[1] * un * h;
-      Tb = P.Mt[1] * un * b;
-      fh = P.Mt[0] * un * H + Th;
-      fb = P.Mt[0] * un * B + Tb;
-    } else {
-      Th = P.Mt[3] * un * h - P.Mt[4] * (un * un) * sh;
-      Tb = P.Mt[3] * un * b - P.Mt[4] * (un * un) * sb;
-      const R* a = pos ? P.aL : P.aR;
-      R c2 = un * un;
-      if (D == 2) c2 += ut * ut;
-      R lin = a[0] + a[1] * un;
-      R linT = P.aT[0] + P.aT[1] * un;
-      R aE = a[D + 1], tE = P.aT[D + 1];
-      if (D == 2) {
-        lin += a[2] * ut;
-        linT += P.aT[2] * ut;
-      }
-      // (c2 H + B) = (c2 + cB) H ; (c2 B + Mxi2 H) = (cB c2 + Mxi2) H
-      R ph = lin + R(0.5) * aE * (c2 + P.cB);
-      R pT = linT + R(0.5) * tE * (c2 + P.cB);
-      R pb = P.cB * lin + R(0.5) * aE * (P.cB * c2 + P.Mxi2);
-      R pTb = P.cB * linT + R(0.5) * tE * (P.cB * c2 + P.Mxi2);
-      R m2 = P.Mt[1] * (un * un);
-      R m3 = P.Mt[2] * un;
-      R m1 = P.Mt[0] * un;
-      fh = H * (m1 + m2 * ph + m3 * pT) + Th;
-      fb = H * (m1 * P.cB + m2 * pb + m3 * pTb) + Tb;
-    }
-    if (D == 2) {
-      fh *= P.len;
-      fb *= P.len;
-    }
   }
 }
 
@@ -254,6 +59,68 @@ __global__ void k_wslope(DevState s) {
 
 // ------------------------------------------------------- face parameters
 
+// log2-form exponent of rho (lam/pi)^(D/2) exp(-lam ((un-U)^2 + (ut-V)^2)) as
+// E.x + E.y un + E.z ut + E.w c2.
+__device__ inline float4 maxwell_exp2(double rho_n, double U, double V, double lam) {
+  float4 E;
+  E.x = rho_n > 0.0 ? float(log2(rho_n) - lam * (U * U + V * V) * LOG2E) : -200.f;
+  E.y = float(2.0 * lam * U * LOG2E);
+  E.z = float(2.0 * lam * V * LOG2E);
+  E.w = float(-lam * LOG2E);
+  return E;
+}
+
+// FP32 monomial coefficients of the interface flux (see FaceCoef32).
+__device__ inline FaceCoef32 face_coef32(const Geo& g, const FaceParam& P, int flux, double dd) {
+  FaceCoef32 c;
+  float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+  c.E = c.T = c.G = c.Cp = c.Dp = c.Cm = c.Dm = z;
+  double len = P.len;
+  c.T.x = float(P.tr[0]);
+  c.T.y = float(P.tr[1] / dd);
+  if (flux == FLUX_KFVS) return c;
+  double lam = P.prim[3], rho = P.prim[0];
+  double rho_n = g.D == 1 ? rho * sqrt(lam / PI) : rho * (lam / PI);
+  c.E = maxwell_exp2(rho_n, P.prim[1], P.prim[2], lam);
+  double cB = g.K / (2.0 * lam);
+  const double* Mt = P.Mt;
+  if (flux == FLUX_KCU) {
+    c.T.z = float(Mt[0] * len);
+    c.T.w = float(Mt[0] * cB * len);
+    return c;
+  }
+  const int e = g.D + 1;  // index of the energy slope
+  const double* t = P.aT;
+  double tt = g.D == 2 ? t[2] : 0.0, Mxi2 = P.Mxi2;
+  c.T.z = float((Mt[0] + Mt[2] * (t[0] + 0.5 * t[e] * cB)) * len);
+  c.T.w = float((Mt[0] * cB + Mt[2] * (cB * t[0] + 0.5 * t[e] * Mxi2)) * len);
+  c.G.x = float(Mt[2] * tt * len);
+  c.G.y = float(0.5 * Mt[2] * t[e] * len);
+  c.G.z = float(Mt[2] * cB * tt * len);
+  c.G.w = float(0.5 * Mt[2] * cB * t[e] * len);
+  for (int sgn = 0; sgn < 2; ++sgn) {
+    const double* a = sgn == 0 ? P.aL : P.aR;
+    double at = g.D == 2 ? a[2] : 0.0;
+    float4 C, Dd;
+    C.x = float((Mt[1] * (a[0] + 0.5 * a[e] * cB) + Mt[2] * t[1]) * len);
+    C.y = float(Mt[1] * a[1] * len);
+    C.z = float(Mt[1] * at * len);
+    C.w = float(0.5 * Mt[1] * a[e] * len);
+    Dd.x = float((Mt[1] * (cB * a[0] + 0.5 * a[e] * Mxi2) + Mt[2] * cB * t[1]) * len);
+    Dd.y = float(Mt[1] * cB * a[1] * len);
+    Dd.z = float(Mt[1] * cB * at * len);
+    Dd.w = float(0.5 * Mt[1] * cB * a[e] * len);
+    if (sgn == 0) {
+      c.Cp = C;
+      c.Dp = Dd;
+    } else {
+      c.Cm = C;
+      c.Dm = Dd;
+    }
+  }
+  return c;
+}
+
 // Interface equilibrium from the two half Maxwellians (flux_kcu.jl:480-495,
 // flux_ugks.jl:47-56), then the KCU / UGKS time integrals, UGKS slopes and
 // the analytic part of fw.  One thread per face.
@@ -275,9 +142,11 @@ __global__ void k_face_param(DevState s, double dt) {
   for (int k = 0; k < 5; ++k) P.Mt[k] = 0;
   P.len = len;
   P.Mxi2 = 0;
-  P.pad = 0;
+  P.tr[0] = P.tr[1] = 0;
   if (FLUX == FLUX_KFVS) {
     P.mult = 1.0;
+    P.tr[0] = dt * len;
+    P.tr[1] = 0.5 * (dt * dt) * len;
   } else {
     // face states of w (local frame): w + dx/2 sw from the left, w - dx/2 sw from the right
     double wl[4], wr[4], wL[4], wR[4];
@@ -320,6 +189,7 @@ __global__ void k_face_param(DevState s, double dt) {
       moments_conserve(mi.Mu, mi.Mv, mi.Mxi, NW, 1, 0, 0, Muv);
       for (int k = 0; k < NW; ++k) P.fwa[k] = P.Mt[0] * p[0] * Muv[k] * len;
       P.mult = len;
+      P.tr[0] = P.Mt[1] * len;
     } else {
       double dL[4], dR[4];
       for (int k = 0; k < 4; ++k) {
@@ -358,9 +228,12 @@ __global__ void k_face_param(DevState s, double dt) {
       }
       P.Mxi2 = mi.Mxi[2];
       P.mult = len;
+      P.tr[0] = Mt[3] * len;
+      P.tr[1] = Mt[4] * len;
     }
   }
   s.fp[f] = P;
+  s.fc[f] = face_coef32(g, P, FLUX, r.d == 0 ? g.dx : g.dy);
   FaceParamF F;
   double lam = P.prim[3] > 0 ? P.prim[3] : 1.0;
   F.rho_n = float(g.D == 1 ? P.prim[0] * sqrt(lam / PI) : P.prim[0] * (lam / PI));
@@ -378,98 +251,6 @@ __global__ void k_face_param(DevState s, double dt) {
   F.len = float(len);
   F.pad[0] = F.pad[1] = 0.f;
   s.fpf[f] = F;
-}
-
-// ------------------------------------------------------------ face moments
-
-// fw of interior faces: analytic part + moments of the transport part of the
-// pointwise flux (flux_conserve!, src/Theory/theory_moments.jl:376-416, and
-// the fw updates of flux_kcu! / flux_ugks!), rotated to the global frame.
-// One warp per face; lanes stride over velocities.
-template <typename R, int D, int FLUX>
-__global__ void __launch_bounds__(256) k_face_moments(DevState s, double dt) {
-  const Geo& g = s.g;
-  int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (f >= s.nface_x + s.nface_y) return;
-  if (s.kind[f] != 1) return;
-  FaceGeo r = face_geo(g, f);
-  FP<R> P = load_fp<R>(s, f);
-  const R* H = (const R*)s.h[s.cur];
-  const R* Bq = (const R*)s.b[s.cur];
-  const R* U = vtab<R>(s, 0);
-  const R* V = vtab<R>(s, 1);
-  const R* W = vtab<R>(s, 2);
-  long vs = g.vstride;
-  int ruleL = slope_rule(g, r.d, r.iL), ruleR = slope_rule(g, r.d, r.iR);
-  R dsc = dscale<R>(r.d == 0 ? g.dx : g.dy);
-  R dxh = R(0.5 * (r.d == 0 ? g.dx : g.dy));
-  R rdt = R(dt);
-  Acc<R> a0, a1, a2, a3;
-  for (int v = lane; v < g.nvel; v += 32) {
-    R un, ut;
-    if (D == 1) {
-      un = U[v];
-      ut = R(0);
-    } else if (r.d == 0) {
-      un = U[v];
-      ut = V[v];
-    } else {
-      un = V[v];
-      ut = -U[v];
-    }
-    bool pos = un >= R(0);
-    int up = pos ? r.cL : r.cR;
-    int rule = pos ? ruleL : ruleR;
-    R sh, sb;
-    R h = upwind_state<R>(H, vs, up, r.step, rule, pos, v, dsc, dxh, sh);
-    R b = upwind_state<R>(Bq, vs, up, r.step, rule, pos, v, dsc, dxh, sb);
-    R fh, fb, Th, Tb;
-    if (FLUX == FLUX_KFVS) {
-      face_flux<R, FLUX, D>(P, rdt, un, ut, pos, h, b, sh, sb, fh, fb, Th, Tb);
-    } else if (FLUX == FLUX_KCU) {
-      Th = P.Mt[1] * un * h;
-      Tb = P.Mt[1] * un * b;
-    } else {
-      Th = P.Mt[3] * un * h - P.Mt[4] * (un * un) * sh;
-      Tb = P.Mt[3] * un * b - P.Mt[4] * (un * un) * sb;
-    }
-    R wT = W[v] * Th;
-    a0.add(wT);
-    a1.add(wT * un);
-    R c2 = un * un;
-    if (D == 2) {
-      a2.add(wT * ut);
-      c2 += ut * ut;
-    }
-    a3.add(wT * c2 + W[v] * Tb);
-  }
-  double S0 = a0.total(), S1 = a1.total(), S2 = D == 2 ? a2.total() : 0.0, S3 = a3.total();
-  if (lane == 0) {
-    const FaceParam& p = s.fp[f];
-    double m = p.mult;
-    double fl[4];
-    if (D == 1) {
-      fl[0] = p.fwa[0] + m * S0;
-      fl[1] = p.fwa[1] + m * S1;
-      fl[2] = p.fwa[2] + m * (0.5 * S3);
-      fl[3] = 0.0;
-    } else {
-      fl[0] = p.fwa[0] + m * S0;
-      fl[1] = p.fwa[1] + m * S1;
-      fl[2] = p.fwa[2] + m * S2;
-      fl[3] = p.fwa[3] + m * (0.5 * S3);
-    }
-    double* out = s.fw + (long)f * 4;
-    if (D == 2 && r.d == 1) {  // global_frame with n = (0, 1)
-      out[0] = fl[0];
-      out[1] = -fl[2];
-      out[2] = fl[1];
-      out[3] = fl[3];
-    } else {
-      for (int k = 0; k < 4; ++k) out[k] = fl[k];
-    }
-  }
 }
 
 // ------------------------------------------------------------ Maxwell walls
@@ -552,6 +333,12 @@ __global__ void __launch_bounds__(256) k_wall(DevState s, double dt) {
   double S0 = a0.total(), S1 = a1.total(), S2 = D == 2 ? a2.total() : 0.0, S3 = a3.total();
   if (lane == 0) {
     s.rhow[f] = rho;
+    FaceCoef32 wc;
+    float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    wc.G = wc.Cp = wc.Dp = wc.Cm = wc.Dm = z;
+    wc.E = maxwell_exp2(D == 1 ? rho * sqrt(lw / PI) : rho * (lw / PI), bw[1], bw[2], lw);
+    wc.T = make_float4(float(sc), 0.f, float(g.K / (2.0 * lw)), float(rot));
+    s.fc[f] = wc;
     double fl[4] = {S0 * sc, S1 * sc, 0.0, 0.0};
     if (D == 1) {
       fl[2] = 0.5 * S3 * sc;
@@ -585,46 +372,6 @@ __device__ inline int update_group(const Geo& g, int i, int j) {
   if (i == g.nx - 1) return g.bc[1] != BC_FIX ? 2 : 0;
   if (j == 0) return g.bc[2] != BC_FIX ? 2 : 0;
   return g.bc[3] != BC_FIX ? 2 : 0;
-}
-
-// heat_flux 2F1V / 2F2V (src/Theory/theory_moments.jl:530-531, :567-578) of the
-// old state.  One warp per updated cell (Shakhov only).
-template <typename R, int D>
-__global__ void __launch_bounds__(256) k_cell_q(DevState s) {
-  const Geo& g = s.g;
-  int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (t >= g.nx * g.ny) return;
-  int i = t % g.nx, j = t / g.nx;
-  int grp = update_group(g, i, j);
-  if (!grp) return;
-  int coll = (D == 1 && grp == 2) ? COLL_BGK : s.coll;
-  if (coll != COLL_SHAKHOV) return;
-  int c = cell_index(g, i, j);
-  const R* H = (const R*)s.h[s.cur] + (long)c * g.vstride;
-  const R* Bq = (const R*)s.b[s.cur] + (long)c * g.vstride;
-  const R* U = vtab<R>(s, 0);
-  const R* V = vtab<R>(s, 1);
-  const R* W = vtab<R>(s, 2);
-  R Uc = R(s.prim[(long)c * 4 + 1]);
-  R Vc = R(D == 2 ? s.prim[(long)c * 4 + 2] : 0.0);
-  Acc<R> a0, a1;
-  for (int v = lane; v < g.nvel; v += 32) {
-    R cu = U[v] - Uc;
-    if (D == 1) {
-      a0.add(W[v] * cu * (cu * cu) * H[v] + W[v] * cu * Bq[v]);
-    } else {
-      R cv = V[v] - Vc;
-      R c2 = cu * cu + cv * cv;
-      a0.add(W[v] * cu * c2 * H[v] + W[v] * cu * Bq[v]);
-      a1.add(W[v] * cv * c2 * H[v] + W[v] * cv * Bq[v]);
-    }
-  }
-  double q0 = a0.total(), q1 = D == 2 ? a1.total() : 0.0;
-  if (lane == 0) {
-    s.q[(long)c * 2 + 0] = 0.5 * q0;
-    s.q[(long)c * 2 + 1] = 0.5 * q1;
-  }
 }
 
 // step! scalar part (src/Solver/step_2f.jl:6-64, :179-249): Shakhov factors of
@@ -718,6 +465,29 @@ __global__ void __launch_bounds__(256) k_cell_param(DevState s, double dt) {
     F.upd = P.upd;
     F.coll = P.coll;
     s.cpf[c] = F;
+    CellCoef32 K;
+    float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    K.EM = K.EO = K.Q = K.TL = z;
+    if (P.upd) {
+      K.EM = maxwell_exp2(P.rho_n, P.U, P.V, P.lam);
+      double ds = D == 1 ? g.dx : g.dx * g.dy;
+      K.A = make_float4(float(P.cB), float(P.dtau), float(P.inv), float(1.0 / ds));
+      if (P.coll == COLL_SHAKHOV) {
+        K.EO = maxwell_exp2(P.o_rho_n, P.oU, P.oV, P.olam);
+        double s0 = P.sfac * P.q0, s1 = P.sfac * P.q1;
+        K.Q = make_float4(float(-(s0 * P.oU + s1 * P.oV)), float(s0), float(s1), float(P.ocB));
+        double l2 = 2.0 * P.olam;
+        K.TL = make_float4(float(l2 * (P.oU * P.oU + P.oV * P.oV) + g.K), float(-2.0 * l2 * P.oU),
+                           float(-2.0 * l2 * P.oV), float(l2));
+      } else {
+        K.EO.x = -200.f;
+      }
+    } else {
+      K.EM.x = -200.f;
+      K.EO.x = -200.f;
+      K.A = make_float4(0.f, 0.f, 1.f, 0.f);
+    }
+    s.cc[c] = K;
   }
   // deterministic block partials: interior (grp 1) and boundary (grp 2) sums
   for (int half = 0; half < 2; ++half) {
@@ -764,179 +534,89 @@ __global__ void k_residual(DevState s) {
 
 // ------------------------------------------------------------ cell update
 
+// Per-face constants of the update loop, built once per warp so the velocity
+// loop runs in the storage precision only.
 template <typename R>
-struct CP {
-  R rho_n, U, V, lam, cB, dtau, inv, o_rho_n, oU, oV, olam, ocB, s0, s1;
-  int upd, coll;
+struct FaceCtx {
+  int kind;             // 0 none, 1 interior, 2 wall
+  int cL, cR, step;     // cells on both sides and the cell step along the normal
+  int ruleL, ruleR;     // slope rules of the two cells along the normal
+  R dsc, dxh;           // 1/dx (FP32) or dx (FP64), dx/2
+  FP<R> P;              // interior coefficients
+  R wU, wV, wlam, wrn, wcB, wsc;  // wall: velocity, lambda, rho (lam/pi)^(D/2), K/(2 lam), len dt
+  int rot;
 };
-template <typename R>
-__device__ __forceinline__ CP<R> load_cp(const DevState& s, int c);
-template <>
-__device__ __forceinline__ CP<double> load_cp<double>(const DevState& s, int c) {
-  const CellParam& p = s.cp[c];
-  CP<double> r;
-  r.rho_n = p.rho_n; r.U = p.U; r.V = p.V; r.lam = p.lam; r.cB = p.cB;
-  r.dtau = p.dtau; r.inv = p.inv;
-  r.o_rho_n = p.o_rho_n; r.oU = p.oU; r.oV = p.oV; r.olam = p.olam; r.ocB = p.ocB;
-  r.s0 = p.sfac * p.q0; r.s1 = p.sfac * p.q1;
-  r.upd = p.upd; r.coll = p.coll;
-  return r;
-}
-template <>
-__device__ __forceinline__ CP<float> load_cp<float>(const DevState& s, int c) {
-  const CellParamF& p = s.cpf[c];
-  CP<float> r;
-  r.rho_n = p.rho_n; r.U = p.U; r.V = p.V; r.lam = p.lam; r.cB = p.cB;
-  r.dtau = p.dtau; r.inv = p.inv;
-  r.o_rho_n = p.o_rho_n; r.oU = p.oU; r.oV = p.oV; r.olam = p.olam; r.ocB = p.ocB;
-  r.s0 = p.sf0; r.s1 = p.sf1;
-  r.upd = p.upd; r.coll = p.coll;
-  return r;
+
+template <typename R, int D>
+__device__ __forceinline__ FaceCtx<R> make_ctx(const DevState& s, int f, int kind, bool right,
+                                               double dt) {
+  const Geo& g = s.g;
+  FaceCtx<R> x;
+  x.kind = kind;
+  FaceGeo r = face_geo(g, f);
+  x.cL = r.cL;
+  x.cR = r.cR;
+  x.step = r.step;
+  x.ruleL = slope_rule(g, r.d, r.iL);
+  x.ruleR = slope_rule(g, r.d, r.iR);
+  double dd = r.d == 0 ? g.dx : g.dy;
+  x.dsc = dscale<R>(dd);
+  x.dxh = R(0.5 * dd);
+  x.rot = right ? -1 : 1;
+  if (kind == 1) x.P = load_fp<R>(s, f);
+  if (kind == 2) {
+    const double* wp = s.wall + (long)f * 4;
+    double lw = D == 1 ? wp[2] : wp[3];
+    double rho = s.rhow[f];
+    x.wU = R(r.d == 0 ? wp[1] : wp[2]);
+    x.wV = R(D == 1 ? 0.0 : (r.d == 0 ? wp[2] : -wp[1]));
+    x.wlam = R(lw);
+    x.wrn = R(D == 1 ? rho * sqrt(lw / PI) : rho * (lw / PI));
+    x.wcB = R(g.K / (2.0 * lw));
+    x.wsc = R(D == 2 ? (r.d == 0 ? g.dy : g.dx) * dt : dt);
+  }
+  return x;
 }
 
-// Pointwise flux of one face of cell c at velocity v (the face is left of c
-// when `right` is false).
+// Pointwise flux of one face at velocity v (face-local velocities un, ut);
+// c is the interior cell next to a wall face.
 template <typename R, int D, int FLUX>
-__device__ __forceinline__ void cell_face_flux(const DevState& s, const R* H, const R* Bq,
-                                               int f, int kind, const FP<R>& P, int c, int d,
-                                               bool right, int v, R un, R ut, R dt, R& fh,
-                                               R& fb) {
-  const Geo& g = s.g;
-  long vs = g.vstride;
-  if (kind == 0) {
+__device__ __forceinline__ void ctx_flux(const FaceCtx<R>& x, const R* __restrict__ H,
+                                         const R* __restrict__ Bq, long vs, int c, int v,
+                                         R un, R ut, R dt, R& fh, R& fb) {
+  if (x.kind == 0) {
     fh = R(0);
     fb = R(0);
     return;
   }
-  if (kind == 2) {
-    // wall flux u h_wall len dt, h_wall = wall Maxwellian on incoming velocities
-    int rot = right ? -1 : 1;
-    bool in = un * R(rot) >= R(0);
-    const double* wp = s.wall + (long)f * 4;
-    double lw = D == 1 ? wp[2] : wp[3];
-    R sc = R(D == 2 ? (d == 0 ? g.dy : g.dx) * (double)dt : (double)dt);
+  if (x.kind == 2) {
+    // u h_wall len dt with h_wall the wall Maxwellian on incoming velocities
+    bool in = un * R(x.rot) >= R(0);
     R hw, bw;
     if (in) {
-      double Uw = d == 0 ? wp[1] : wp[2];
-      double Vw = D == 1 ? 0.0 : (d == 0 ? wp[2] : -wp[1]);
-      double rho = s.rhow[f];
-      R rn = R(D == 1 ? rho * sqrt(lw / PI) : rho * (lw / PI));
-      R du = un - R(Uw), e = du * du;
-      if (D == 2) { R dv = ut - R(Vw); e += dv * dv; }
-      hw = rn * mexp(-R(lw) * e);
-      bw = hw * R(g.K / (2.0 * lw));
+      R du = un - x.wU, e = du * du;
+      if (D == 2) {
+        R dv = ut - x.wV;
+        e += dv * dv;
+      }
+      hw = x.wrn * mexp(-x.wlam * e);
+      bw = hw * x.wcB;
     } else {
       hw = H[(long)c * vs + v];
       bw = Bq[(long)c * vs + v];
     }
-    fh = un * hw * sc;
-    fb = un * bw * sc;
+    fh = un * hw * x.wsc;
+    fb = un * bw * x.wsc;
     return;
   }
-  FaceGeo r = face_geo(g, f);
   bool pos = un >= R(0);
-  int up = pos ? r.cL : r.cR;
-  int rule = slope_rule(g, d, pos ? r.iL : r.iR);
-  R dsc = dscale<R>(d == 0 ? g.dx : g.dy);
-  R dxh = R(0.5 * (d == 0 ? g.dx : g.dy));
+  int up = pos ? x.cL : x.cR;
+  int rule = pos ? x.ruleL : x.ruleR;
   R sh, sb;
-  R h = upwind_state<R>(H, vs, up, r.step, rule, pos, v, dsc, dxh, sh);
-  R b = upwind_state<R>(Bq, vs, up, r.step, rule, pos, v, dsc, dxh, sb);
+  R h = upwind_state<R>(H, vs, up, x.step, rule, pos, v, x.dsc, x.dxh, sh);
+  R b = upwind_state<R>(Bq, vs, up, x.step, rule, pos, v, x.dsc, x.dxh, sb);
   R Th, Tb;
-  face_flux<R, FLUX, D>(P, dt, un, ut, pos, h, b, sh, sb, fh, fb, Th, Tb);
-}
-
-// Pointwise part of step!: h = (h + flux divergence / ds + dt/tau (M + S)) /
-// (1 + dt/tau) with the new Maxwellian M and the Shakhov term S of the old
-// state (src/Solver/step_2f.jl:56-63, :240-248).  One warp per cell
-// (ghost and fixed cells are copied to the output buffer).
-template <typename R, int D, int FLUX>
-__global__ void __launch_bounds__(256) k_update(DevState s, double dt) {
-  const Geo& g = s.g;
-  int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (c >= s.ncell) return;
-  const R* H = (const R*)s.h[s.cur];
-  const R* Bq = (const R*)s.b[s.cur];
-  R* Ho = (R*)s.h[s.cur ^ 1];
-  R* Bo = (R*)s.b[s.cur ^ 1];
-  long vs = g.vstride;
-  int ci = c % g.nxt - g.ngx, cj = c / g.nxt - g.ngy;
-  bool phys = ci >= 0 && ci < g.nx && cj >= 0 && cj < g.ny;
-  CP<R> C;
-  if (phys) C = load_cp<R>(s, c);
-  if (!phys || !C.upd) {
-    for (int v = lane; v < g.nvel; v += 32) {
-      Ho[(long)c * vs + v] = H[(long)c * vs + v];
-      Bo[(long)c * vs + v] = Bq[(long)c * vs + v];
-    }
-    return;
-  }
-  int fxL = cj * (g.nx + 1) + ci, fxR = fxL + 1;
-  int fyD = s.nface_x + cj * g.nx + ci, fyU = fyD + g.nx;
-  int kL = s.kind[fxL], kR = s.kind[fxR];
-  int kD = D == 2 ? s.kind[fyD] : 0, kU = D == 2 ? s.kind[fyU] : 0;
-  FP<R> PL, PR, PD, PU;
-  if (kL == 1) PL = load_fp<R>(s, fxL);
-  if (kR == 1) PR = load_fp<R>(s, fxR);
-  if (D == 2) {
-    if (kD == 1) PD = load_fp<R>(s, fyD);
-    if (kU == 1) PU = load_fp<R>(s, fyU);
-  }
-  const R* U = vtab<R>(s, 0);
-  const R* V = vtab<R>(s, 1);
-  R rdt = R(dt);
-  R ids = dscale<R>(D == 1 ? g.dx : g.dx * g.dy);
-  double dsd = D == 1 ? g.dx : g.dx * g.dy;
-  R Kf = R(g.K);
-  bool shak = C.coll == COLL_SHAKHOV;
-  for (int v = lane; v < g.nvel; v += 32) {
-    R u = U[v];
-    R vv = D == 2 ? V[v] : R(0);
-    R fhL, fbL, fhR, fbR, fhD = 0, fbD = 0, fhU = 0, fbU = 0;
-    cell_face_flux<R, D, FLUX>(s, H, Bq, fxL, kL, PL, c, 0, false, v, u, vv, rdt, fhL, fbL);
-    cell_face_flux<R, D, FLUX>(s, H, Bq, fxR, kR, PR, c, 0, true, v, u, vv, rdt, fhR, fbR);
-    if (D == 2) {
-      cell_face_flux<R, D, FLUX>(s, H, Bq, fyD, kD, PD, c, 1, false, v, vv, -u, rdt, fhD, fbD);
-      cell_face_flux<R, D, FLUX>(s, H, Bq, fyU, kU, PU, c, 1, true, v, vv, -u, rdt, fhU, fbU);
-    }
-    R du = u - C.U, e = du * du;
-    if (D == 2) { R dv = vv - C.V; e += dv * dv; }
-    R MH = C.rho_n * mexp(-C.lam * e);
-    R MB = MH * Kf / (R(2) * C.lam);
-    if (shak) {
-      R ou = u - C.oU, oe = ou * ou, cq = ou * C.s0;
-      if (D == 2) {
-        R ov = vv - C.oV;
-        oe += ov * ov;
-        cq += ov * C.s1;
-      }
-      R OH = C.o_rho_n * mexp(-C.olam * oe);
-      R OB = OH * Kf / (R(2) * C.olam);
-      R tl = R(2) * C.olam * oe + Kf;
-      MH += cq * (tl - R(5)) * OH;
-      MB += cq * (tl - R(3)) * OB;
-    }
-    R h0 = H[(long)c * vs + v], b0 = Bq[(long)c * vs + v];
-    R dh, db;
-    if (D == 1) {
-      dh = fhL - fhR;
-      db = fbL - fbR;
-    } else {
-      dh = fhL - fhR + fhD - fhU;
-      db = fbL - fbR + fbD - fbU;
-    }
-    R hn, bn;
-    if (sizeof(R) == 8) {
-      hn = (h0 + dh / R(dsd) + C.dtau * MH) / (R(1) + C.dtau);
-      bn = (b0 + db / R(dsd) + C.dtau * MB) / (R(1) + C.dtau);
-    } else {
-      hn = (h0 + dh * ids + C.dtau * MH) * C.inv;
-      bn = (b0 + db * ids + C.dtau * MB) * C.inv;
-    }
-    Ho[(long)c * vs + v] = hn;
-    Bo[(long)c * vs + v] = bn;
-  }
+  face_flux<R, FLUX, D>(x.P, dt, un, ut, pos, h, b, sh, sb, fh, fb, Th, Tb);
 }
 
 // ------------------------------------------------------------ ghost fill
@@ -1007,19 +687,17 @@ __global__ void k_faces_dump(DevState s, double dt, double* fh_out, double* fb_o
   const R* Bq = (const R*)s.b[s.cur];
   const R* U = vtab<R>(s, 0);
   const R* V = vtab<R>(s, 1);
-  FP<R> P;
-  if (kind == 1) P = load_fp<R>(s, f);
   int pos0 = r.d == 0 ? r.fi : r.fj;
   bool right = pos0 != 0;  // wall faces: the cell is on the left of the right / top wall
   int c = (kind == 2 && pos0 == 0) ? r.cR : r.cL;
+  FaceCtx<R> X = make_ctx<R, D>(s, f, kind, right, dt);
   for (int v = threadIdx.x; v < g.nvel; v += blockDim.x) {
     R un, ut;
     if (D == 1) { un = U[v]; ut = R(0); }
     else if (r.d == 0) { un = U[v]; ut = V[v]; }
     else { un = V[v]; ut = -U[v]; }
     R fh = 0, fb = 0;
-    if (kind != 0)
-      cell_face_flux<R, D, FLUX>(s, H, Bq, f, kind, P, c, r.d, right, v, un, ut, R(dt), fh, fb);
+    ctx_flux<R, D, FLUX>(X, H, Bq, g.vstride, c, v, un, ut, R(dt), fh, fb);
     fh_out[(long)f * g.nvel + v] = double(fh);
     fb_out[(long)f * g.nvel + v] = double(fb);
   }
@@ -1120,7 +798,7 @@ int launch_reconstruct(DevState& s, cudaStream_t st) {
   return 1;
 }
 
-template <typename R, int D>
+template <int D>
 static int evolve_t(DevState& s, double dt, cudaStream_t st) {
   int nf = s.nface_x + s.nface_y;
   int n = 0;
@@ -1130,44 +808,28 @@ static int evolve_t(DevState& s, double dt, cudaStream_t st) {
     default: k_face_param<FLUX_UGKS><<<nblk(nf, 128), 128, 0, st>>>(s, dt); break;
   }
   ++n;
-  unsigned gb = nblk((long)nf * 32, 256);
-  switch (s.flux) {
-    case FLUX_KFVS: k_face_moments<R, D, FLUX_KFVS><<<gb, 256, 0, st>>>(s, dt); break;
-    case FLUX_KCU: k_face_moments<R, D, FLUX_KCU><<<gb, 256, 0, st>>>(s, dt); break;
-    default: k_face_moments<R, D, FLUX_UGKS><<<gb, 256, 0, st>>>(s, dt); break;
-  }
-  ++n;
+  n += launch_moments(s, st);
   bool wall = false;
   for (int k = 0; k < 2 * D; ++k) wall |= s.g.bc[k] == BC_MAXWELL;
   if (wall) {
-    k_wall<R, D><<<gb, 256, 0, st>>>(s, dt);
+    unsigned gb = nblk((long)nf * 32, 256);
+    if (s.prec == 0) k_wall<double, D><<<gb, 256, 0, st>>>(s, dt);
+    else k_wall<float, D><<<gb, 256, 0, st>>>(s, dt);
     ++n;
   }
   return n;
 }
 
 int launch_evolve(DevState& s, double dt, cudaStream_t st) {
-  if (s.prec == 0) return s.g.D == 1 ? evolve_t<double, 1>(s, dt, st) : evolve_t<double, 2>(s, dt, st);
-  return s.g.D == 1 ? evolve_t<float, 1>(s, dt, st) : evolve_t<float, 2>(s, dt, st);
+  return s.g.D == 1 ? evolve_t<1>(s, dt, st) : evolve_t<2>(s, dt, st);
 }
 
 template <typename R, int D>
 static int update_t(DevState& s, double dt, cudaStream_t st) {
   int n = 0;
-  long ncp = (long)s.g.nx * s.g.ny;
-  if (s.coll == COLL_SHAKHOV) {
-    k_cell_q<R, D><<<nblk(ncp * 32, 256), 256, 0, st>>>(s);
-    ++n;
-  }
   k_cell_param<D><<<s.res_blocks, 256, 0, st>>>(s, dt);
   ++n;
-  unsigned gb = nblk((long)s.ncell * 32, 256);
-  switch (s.flux) {
-    case FLUX_KFVS: k_update<R, D, FLUX_KFVS><<<gb, 256, 0, st>>>(s, dt); break;
-    case FLUX_KCU: k_update<R, D, FLUX_KCU><<<gb, 256, 0, st>>>(s, dt); break;
-    default: k_update<R, D, FLUX_UGKS><<<gb, 256, 0, st>>>(s, dt); break;
-  }
-  ++n;
+  n += launch_march(s, dt, st);
   s.cur ^= 1;
   bool fill = false;
   for (int k = 0; k < 2 * D; ++k) fill |= s.g.bc[k] == BC_EXTRA || s.g.bc[k] == BC_PERIOD;

@@ -32,6 +32,8 @@ struct DevState {
   double* q;        // [ncell][2]
   CellParam* cp;    // [ncell]
   CellParamF* cpf;  // [ncell]
+  FaceCoef32* fc;   // [nface] FP32 coefficient blocks
+  CellCoef32* cc;   // [ncell] FP32 cell coefficients
   double* blockres; // [nblocks][16] residual partials
   double* residual; // [4]
   int* status;      // [1]
@@ -48,6 +50,10 @@ void face_kinds_host(const Geo& g, signed char* kind);
 int launch_reconstruct(DevState& s, cudaStream_t st);
 int launch_evolve(DevState& s, double dt, cudaStream_t st);
 int launch_update(DevState& s, double dt, cudaStream_t st);
+
+// Pass A (face moments, heat flux) and pass B (pointwise update), kb_march.cu.
+int launch_moments(DevState& s, cudaStream_t st);
+int launch_march(DevState& s, double dt, cudaStream_t st);
 
 // Materialise face fluxes fh / fb (double) of the current state, and slopes.
 int launch_faces_dump(DevState& s, double dt, double* fh, double* fb, cudaStream_t st);
