@@ -1,0 +1,461 @@
+"""Benchmark of the GB300 DVM time step (driver contract: one JSON line).
+
+Workload: the four-quadrant 2D2F2V solve sized for the HBM roofline -- 512 x 512
+cells, 64 x 64 Newton-Cotes velocities on [-6, 6]^2, UGKS flux, BGK relaxation,
+Kn = 1e-3, extrapolation boundaries with one ghost layer, seeded quadrant states
+(rho ~ U(0.1, 1.5), U, V ~ U(-0.5, 0.5), lambda ~ U(0.4, 1.2)).  One step =
+reconstruct! + evolve! + update! over all 1.07e9 cell-velocity points.
+
+  value      cell-velocity updates/s of the FP32-split form (FP32 h / b, FP64
+             moments, w, prim), state resident in HBM, CUDA events on the
+             library's stream; inputs (17 GB of state) are larger than L2.
+  e2e        the same through the C ABI with host buffers: upload of the FP64
+             host state from pinned memory, K steps, download of the state.
+  roofline   pass B (pointwise update, the dominant kernel): algorithmic bytes
+             (read h, b once + write h, b once = 16 B per cell-velocity in FP32)
+             / its CUDA-event time, against the measured HBM copy bandwidth.
+  fp64_plain the plain FP64 GPU path on the same workload.
+  cpu_baseline  the FP64 C oracle (restatement of the Julia reference; Julia
+             is not available) on a bounded sample with all host threads.
+
+--impl reference times that CPU restatement alone on the same metric.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "kitbase.jl_gb300"))
+
+WORKLOAD = dict(nx=512, ny=512, nu=64, nv=64, umax=6.0, Kn=1e-3, flux="ugks", coll="bgk",
+                bc="extra", ng=1, seed=20261203, cfl=0.5)
+METRIC = "DVM cell-velocity updates/s"
+UNIT = "cell-velocity updates/s"
+
+
+def quadrant_cfg(nx, ny, nu, nv, umax, Kn, flux, coll, bc, ng, seed, cfl, **_):
+    return dict(matter="gas", case="quadrant", space="2d2f2v", flux=flux, collision=coll,
+                nSpecies=1, interpOrder=2, limiter="vanleer", boundary=bc, cfl=cfl, maxTime=1.0,
+                x0=0.0, x1=1.0, nx=nx, nxg=ng, y0=0.0, y1=1.0, ny=ny, nyg=ng, umin=-umax,
+                umax=umax, nu=nu, vmin=-umax, vmax=umax, nv=nv, vMeshType="newton", knudsen=Kn,
+                mach=0.0, prandtl=2.0 / 3.0, inK=1.0, omega=0.81, alphaRef=1.0, omegaRef=0.5)
+
+
+def quadrant_state(KS, out_h=None, out_b=None):
+    """Vectorised init_fvm state of the quadrant preset (all cells incl. ghosts)."""
+    import kitgpu
+    ps, gas, vs = KS.ps, KS.gas, KS.vs
+    xm, ym = (ps.x0 + ps.x1) / 2, (ps.y0 + ps.y1) / 2
+    X = ps.x.T.ravel()  # cell order: x fastest
+    Y = ps.y.T.ravel()
+    q = np.where(X > xm, np.where(Y > ym, 0, 3), np.where(Y > ym, 1, 2))
+    quads = KS.ib.p["quads"]
+    W4 = np.array([kitgpu.prim_conserve(p, gas.gamma) for p in quads])
+    P4 = np.array([kitgpu.conserve_prim(w, gas.gamma) for w in W4])
+    u, v = vs.flat(vs.u), vs.flat(vs.v)
+    H4 = np.array([kitgpu.maxwellian(u, p, v) for p in P4])
+    B4 = H4 * gas.K / 2.0 / P4[:, -1:]
+    n = len(q)
+    h = out_h if out_h is not None else np.empty((n, len(u)))
+    b = out_b if out_b is not None else np.empty((n, len(u)))
+    for k in range(4):
+        m = q == k
+        h[m] = H4[k]
+        b[m] = B4[k]
+    return W4[q], P4[q], h, b
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in self.rows:
+            if len(r) >= 9:
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if args.impl == "ours" and torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return ws, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    if pg.get_backend() == "nccl":
+        t = t.cuda()
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_oracle(threads, nx=64):
+    """FP64 oracle on an nx x nx-cell sample of the workload (same velocity grid,
+    flux, collision and boundaries): (oracle, dt, cell-velocity points)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import kitgpu
+    import oracle as O
+    wl = dict(WORKLOAD, nx=nx, ny=nx)
+    KS = kitgpu.solver_set(quadrant_cfg(**wl))
+    cfg = kitgpu.kb_config(KS)
+    c = O.make_config(cfg.dim, cfg.nx, cfg.ny, cfg.ngx, cfg.ngy, cfg.nu, cfg.nv, cfg.flux,
+                      cfg.collision, [cfg.bc[k] for k in range(4)], cfg.interp_order, cfg.x0,
+                      cfg.x1, cfg.y0, cfg.y1, cfg.umax, cfg.vmax, cfg.K, cfg.gamma, cfg.mu_ref,
+                      cfg.omega, cfg.Pr)
+    vs = KS.vs
+    orc = O.Oracle(c, vs.flat(vs.u), vs.flat(vs.v), vs.flat(vs.weights), threads=threads)
+    w, p, h, b = quadrant_state(KS)
+    orc.set_state(w, p, h, b)
+    dt = orc.timestep(KS.set.cfl, 0.0, KS.set.maxTime)
+    return orc, dt, nx * nx * vs.nu * vs.nv
+
+
+def cpu_sample(threads, nsteps=None, nx=64):
+    """Oracle throughput on the sample: (updates/s, description, s per step)."""
+    orc, dt, cv = cpu_oracle(threads, nx)
+    orc.step(dt, 1)  # warm-up (page faults, thread pool)
+    if nsteps is None:
+        t0 = time.perf_counter()
+        orc.step(dt, 1)
+        one = time.perf_counter() - t0
+        nsteps = max(1, int(15.0 / max(one, 1e-3)))
+    t0 = time.perf_counter()
+    orc.step(dt, nsteps)
+    el = time.perf_counter() - t0
+    desc = ("%dx%d-cell sample of the workload (64x64 velocities, UGKS+BGK), %d step(s), "
+            "FP64 C oracle with OpenMP" % (nx, nx, nsteps))
+    return cv * nsteps / el, desc, el / nsteps
+
+
+def run_reference(args):
+    ws, rank, local, pg = dist_setup(args)
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    import kitgpu  # noqa: F401  (host-side setup only)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    nx = 64
+    orc, dt, cv = cpu_oracle(threads, nx)
+    for _ in range(args.warmup):
+        orc.step(dt, 1)
+    t0 = time.perf_counter()
+    orc.step(dt, args.steps)
+    el = time.perf_counter() - t0
+    val = cv * args.steps / el
+    desc = ("each step: one DVM step of a %dx%d-cell sample of the workload (64x64 velocities, "
+            "UGKS+BGK), FP64 C oracle with OpenMP" % (nx, nx))
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT,
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * el / max(args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "four-quadrant 2D2F2V 512x512 cells x 64x64 velocities, "
+                                   "UGKS + BGK, Kn=1e-3 (each step: a 64x64-cell sample)"},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": desc + "; Julia KitBase is not installable here, the "
+                                              "C restatement of its algorithm stands in"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local, pg = dist_setup(args)
+    torch.cuda.set_device(local)
+    import kitgpu
+    from kitgpu import _native as N
+    kitgpu.load()
+
+    wl = dict(WORKLOAD)
+    if args.small:
+        wl.update(nx=128, ny=128)
+    KS = kitgpu.solver_set(quadrant_cfg(**wl))
+    vs = KS.vs
+    ncell_phys = wl["nx"] * wl["ny"]
+    nvel = vs.nu * vs.nv
+    cv = ncell_phys * nvel  # cell-velocity updates per step
+    nxt, nyt = wl["nx"] + 2 * wl["ng"], wl["ny"] + 2 * wl["ng"]
+    ncell = nxt * nyt
+
+    # pinned host state (FP64, the reference's storage type)
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    h_host, b_host = pin((ncell, nvel)), pin((ncell, nvel))
+    w_host, p_host, _, _ = quadrant_state(KS, h_host, b_host)
+    w_host = np.ascontiguousarray(w_host)
+    p_host = np.ascontiguousarray(p_host)
+    h_out, b_out = pin((ncell, nvel)), pin((ncell, nvel))
+    w_out, p_out = np.zeros_like(w_host), np.zeros_like(p_host)
+
+    def make(prec):
+        hd = kitgpu.Handle(kitgpu.kb_config(KS, prec), vs.flat(vs.u), vs.flat(vs.v),
+                           vs.flat(vs.weights))
+        hd.upload(w_host, p_host, h_host, b_host)
+        return hd
+
+    hd = make("fp32")
+    dt = hd.timestep(KS.set.cfl, 0.0, KS.set.maxTime)
+    stream = torch.cuda.ExternalStream(hd.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    hd.step(dt, args.warmup)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    n0 = hd.launches()
+    barrier(pg)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    hd.step(dt, args.steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(pg)
+    ms = ev0.elapsed_time(ev1)
+    launches = hd.launches() - n0
+    clocks.stop()
+    ms = max_over_ranks(pg, ms)
+    value = cv * args.steps * ws / (ms / 1e3)
+
+    # per-stage kernel times (events around each kernel group) for the roofline
+    hd.set_timing(True)
+    nprof = max(2, min(args.steps, 5))
+    hd.step(dt, nprof)
+    st = hd.timing()
+    hd.set_timing(False)
+    upd_ms = st["update"][0] / st["update"][1]
+    mom_ms = st["moments"][0] / st["moments"][1]
+    step_ms = sum(v[0] for v in st.values()) / nprof
+    peak, peak_kind = measured_peaks()
+    alg_b = 16.0 * cv  # read h, b once + write h, b once, FP32
+    achieved = alg_b / (upd_ms / 1e3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "k_march_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tt = json.load(f)
+        traffic = tt.get("bytes_per_cv", 0) * cv or None
+
+    # end to end through the C ABI: pinned host state in, K steps, state out
+    barrier(pg)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hd.upload(w_host, p_host, h_host, b_host)
+    hd.step(dt, args.steps)
+    hd.call("kb_download_state", N.ptr(w_out), N.ptr(p_out), N.ptr(h_out), N.ptr(b_out))
+    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(pg, e2e_s)
+    h2d = (w_host.nbytes + p_host.nbytes + h_host.nbytes + b_host.nbytes) / args.steps
+    d2h = (w_out.nbytes + p_out.nbytes + h_out.nbytes + b_out.nbytes) / args.steps
+    e2e_val = cv * args.steps * ws / e2e_s
+    hd.close()
+
+    # plain FP64 GPU path on the same workload
+    fp64 = None
+    if not args.no_fp64:
+        h64 = make("fp64")
+        h64.step(dt, 1)
+        k64 = max(1, min(args.steps, 3))
+        torch.cuda.synchronize()
+        s64 = torch.cuda.ExternalStream(h64.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s64)
+        h64.step(dt, k64)
+        e1.record(s64)
+        torch.cuda.synchronize()
+        ms64 = max_over_ranks(pg, e0.elapsed_time(e1))
+        v64 = cv * k64 * ws / (ms64 / 1e3)
+        h64.set_timing(True)
+        h64.step(dt, 1)
+        t64 = h64.timing()
+        h64.close()
+        u64 = t64["update"][0] / t64["update"][1]
+        fp64 = {"value": v64, "unit": UNIT, "steps": k64, "ms_per_step": ms64 / k64,
+                "speedup_fp32_split": value / v64,
+                "roofline": {"bound": "hbm", "achieved": 32.0 * cv / (u64 / 1e3) / 1e9,
+                             "peak": peak, "unit": "GB/s",
+                             "frac": 32.0 * cv / (u64 / 1e3) / 1e9 / peak},
+                "stage_ms": {k: v[0] / max(v[1], 1) for k, v in t64.items()}}
+
+    # L-inf error of the FP32-split form against the FP64 path (pinned to the
+    # oracle at 1e-12 by the parity tests) on a 128x128-cell sub-case
+    err = None
+    if not args.no_error:
+        wl2 = dict(WORKLOAD, nx=128, ny=128)
+        KS2 = kitgpu.solver_set(quadrant_cfg(**wl2))
+        outs = {}
+        for prec in ("fp32", "fp64"):
+            hh = kitgpu.Handle(kitgpu.kb_config(KS2, prec), KS2.vs.flat(KS2.vs.u),
+                               KS2.vs.flat(KS2.vs.v), KS2.vs.flat(KS2.vs.weights))
+            w2, p2, h2, b2 = quadrant_state(KS2)
+            hh.upload(w2, p2, h2, b2)
+            dt2 = hh.timestep(KS2.set.cfl, 0.0, 1.0)
+            hh.step(dt2, args.err_steps)
+            outs[prec] = hh.download()
+            hh.close()
+        pa, pb = outs["fp32"]["prim"], outs["fp64"]["prim"]
+        e_rho = float(np.max(np.abs(pa[:, 0] - pb[:, 0]) / pb[:, 0]))
+        e_u = float(np.max(np.abs(pa[:, 1:3] - pb[:, 1:3]) * np.sqrt(pb[:, 3:4])))
+        e_t = float(np.max(np.abs(1 / pa[:, 3] - 1 / pb[:, 3]) * pb[:, 3]))
+        # heat flux from the distributions (theory_moments.jl:567-578)
+        def qflux(o):
+            u, v, wq = KS2.vs.flat(KS2.vs.u), KS2.vs.flat(KS2.vs.v), KS2.vs.flat(KS2.vs.weights)
+            P = o["prim"]
+            cu = u[None, :] - P[:, 1:2]
+            cvv = v[None, :] - P[:, 2:3]
+            c2 = cu * cu + cvv * cvv
+            q1 = 0.5 * ((wq * cu * c2 * o["h"]).sum(1) + (wq * cu * o["b"]).sum(1))
+            q2 = 0.5 * ((wq * cvv * c2 * o["h"]).sum(1) + (wq * cvv * o["b"]).sum(1))
+            return np.stack([q1, q2], 1)
+        qa, qb = qflux(outs["fp32"]), qflux(outs["fp64"])
+        e_q = float(np.max(np.abs(qa - qb)) / max(np.max(np.abs(qb)), 1e-300))
+        wa, wb = outs["fp32"]["w"], outs["fp64"]["w"]
+        err = {"case": "128x128 cells x 64x64 velocities, %d steps" % args.err_steps,
+               "rho": e_rho, "U": e_u, "T": e_t, "q_rel_to_max": e_q,
+               "mass_drift_fp32": float(abs(wa[:, 0].sum() - wb[:, 0].sum()) / wb[:, 0].sum()),
+               "reference": "FP64 GPU path (equal to the FP64 oracle within 1e-12 in tests)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        thr = os.cpu_count() or 1
+        v, desc, per = cpu_sample(thr)
+        cpu = {"value": v, "unit": UNIT, "cores": thr, "kind": "port", "sample": desc}
+
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "precision": "FP32 h, b and pointwise fluxes; FP64 moments (compensated), w, prim, q",
+        "data": "synthetic",
+        "config": {"workload": "four-quadrant 2D2F2V %dx%d cells x %dx%d velocities on [-6,6]^2, "
+                               "UGKS + BGK, Kn=1e-3, extrapolation boundaries"
+                               % (wl["nx"], wl["ny"], vs.nu, vs.nv),
+                   "cells": ncell_phys, "velocities": nvel, "cell_velocity_per_step": cv,
+                   "state_bytes_fp32": 4 * 4 * ncell * nvel,
+                   "l2": "inputs larger than L2 (state far above 129 MB), no flush",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "kernel": "k_march (pass B, pointwise update)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": alg_b, "launch_ms": upd_ms},
+        "step_roofline": {"achieved": alg_b / (ms / args.steps / 1e3) / 1e9, "unit": "GB/s",
+                          "frac": alg_b / (ms / args.steps / 1e3) / 1e9 / peak,
+                          "note": "whole step (pass A + pass B + small kernels), 16 B per cv"},
+        "stage_ms": {k: v[0] / max(v[1], 1) for k, v in st.items()},
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "note": "kb_upload_state (FP64 pinned host) + K kb_step + kb_download_state"},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "fp64_plain": fp64,
+        "linf_error_vs_fp64": err,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--small", action="store_true", help="128x128 cells instead of 512x512")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-error", action="store_true")
+    ap.add_argument("--err-steps", type=int, default=40)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -163,6 +163,21 @@ int kb_device_bytes(kb_handle_t* h, int64_t* bytes);
 /* Number of kernel launches issued by this handle since creation. */
 int kb_launch_count(kb_handle_t* h, int64_t* count);
 
+/* Per-stage kernel timing of kb_step, measured with CUDA events on the
+ * handle's stream.  Stages: 0 w slopes (reconstruct!), 1 face parameters,
+ * 2 face moments (fw, heat flux), 3 Maxwell walls, 4 cell parameters
+ * (w, prim, tau), 5 pointwise update of h and b, 6 ghost fill + residual.
+ * kb_set_timing(h, 1) enables and resets the counters; kb_get_timing returns
+ * the accumulated milliseconds and step counts per stage.  No reference
+ * counterpart (the reference only wraps solve! in @showprogress). */
+#define KB_NSTAGE 7
+int kb_set_timing(kb_handle_t* h, int enable);
+int kb_get_timing(kb_handle_t* h, double* ms, int64_t* count);
+
+/* The cudaStream_t (as void*) the handle launches on, so callers can order
+ * their own work or CUDA events against it. */
+int kb_get_stream(kb_handle_t* h, void** stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,6 +33,11 @@ struct kb_handle {
   long stage_elems = 0;
   double* d_scalar = nullptr; // [8] scratch scalars
   bool evolved = false;
+  // per-stage kernel timing (kb_set_timing): CUDA events on the handle stream
+  bool timing = false;
+  std::vector<cudaEvent_t> events;
+  double stage_ms[KB_NSTAGE] = {0};
+  int64_t stage_n[KB_NSTAGE] = {0};
 };
 
 static thread_local std::string g_err;
@@ -271,6 +276,7 @@ int kb_create(const kb_config_t* cfg, const double* u, const double* v, const do
 int kb_destroy(kb_handle_t* h) {
   if (!h) return KB_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   for (void* p : h->allocs) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -418,18 +424,87 @@ int kb_update(kb_handle_t* h, double dt, double* residual) {
   return read_residual(h, residual);
 }
 
+// One step as kernel groups with an event after each group (stage k ends at
+// event k+1).
+static int timed_step(kb_handle* h, double dt, cudaEvent_t* ev) {
+  cudaStream_t st = h->stream;
+  int n = 0;
+  cudaEventRecord(ev[0], st);
+  n += kb::launch_reconstruct(h->s, st);
+  cudaEventRecord(ev[1], st);
+  n += kb::launch_face_param(h->s, dt, st);
+  cudaEventRecord(ev[2], st);
+  n += kb::launch_moments(h->s, st);
+  cudaEventRecord(ev[3], st);
+  n += kb::launch_wall(h->s, dt, st);
+  cudaEventRecord(ev[4], st);
+  n += kb::launch_cell_param(h->s, dt, st);
+  cudaEventRecord(ev[5], st);
+  n += kb::launch_march(h->s, dt, st);
+  cudaEventRecord(ev[6], st);
+  n += kb::launch_finish(h->s, st);
+  cudaEventRecord(ev[7], st);
+  return n;
+}
+
 int kb_step(kb_handle_t* h, double dt, int32_t nsteps, double* residual) {
   if (!h) return fail(KB_ERR_ARG, "kb_step: null handle");
   if (!(dt > 0.0)) return fail(KB_ERR_ARG, "kb_step: dt must be positive");
   if (nsteps < 0) return fail(KB_ERR_ARG, "kb_step: nsteps must be >= 0");
-  for (int s = 0; s < nsteps; ++s) {
-    int n = kb::launch_reconstruct(h->s, h->stream);
-    n += kb::launch_evolve(h->s, dt, h->stream);
-    n += kb::launch_update(h->s, dt, h->stream);
-    KB_TRY(check_launch(h, n));
+  if (h->timing) {
+    size_t need = (size_t)nsteps * (KB_NSTAGE + 1);
+    while (h->events.size() < need) {
+      cudaEvent_t e;
+      KB_CUDA(cudaEventCreate(&e));
+      h->events.push_back(e);
+    }
+    for (int s = 0; s < nsteps; ++s)
+      KB_TRY(check_launch(h, timed_step(h, dt, &h->events[(size_t)s * (KB_NSTAGE + 1)])));
+    KB_TRY(sync(h));
+    for (int s = 0; s < nsteps; ++s) {
+      cudaEvent_t* ev = &h->events[(size_t)s * (KB_NSTAGE + 1)];
+      for (int k = 0; k < KB_NSTAGE; ++k) {
+        float ms = 0.f;
+        KB_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+        h->stage_ms[k] += ms;
+        h->stage_n[k] += 1;
+      }
+    }
+  } else {
+    for (int s = 0; s < nsteps; ++s) {
+      int n = kb::launch_reconstruct(h->s, h->stream);
+      n += kb::launch_evolve(h->s, dt, h->stream);
+      n += kb::launch_update(h->s, dt, h->stream);
+      KB_TRY(check_launch(h, n));
+    }
   }
   h->evolved = false;
   return read_residual(h, residual);
+}
+
+int kb_set_timing(kb_handle_t* h, int enable) {
+  if (!h) return fail(KB_ERR_ARG, "kb_set_timing: null handle");
+  h->timing = enable != 0;
+  for (int k = 0; k < KB_NSTAGE; ++k) {
+    h->stage_ms[k] = 0.0;
+    h->stage_n[k] = 0;
+  }
+  return KB_OK;
+}
+
+int kb_get_timing(kb_handle_t* h, double* ms, int64_t* count) {
+  if (!h || !ms) return fail(KB_ERR_ARG, "kb_get_timing: null argument");
+  for (int k = 0; k < KB_NSTAGE; ++k) {
+    ms[k] = h->stage_ms[k];
+    if (count) count[k] = h->stage_n[k];
+  }
+  return KB_OK;
+}
+
+int kb_get_stream(kb_handle_t* h, void** stream) {
+  if (!h || !stream) return fail(KB_ERR_ARG, "kb_get_stream: null argument");
+  *stream = (void*)h->stream;
+  return KB_OK;
 }
 
 int kb_download_faces(kb_handle_t* h, double dt, double* fw, double* fh, double* fb) {

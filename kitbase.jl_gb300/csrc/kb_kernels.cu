@@ -798,38 +798,48 @@ int launch_reconstruct(DevState& s, cudaStream_t st) {
   return 1;
 }
 
-template <int D>
-static int evolve_t(DevState& s, double dt, cudaStream_t st) {
+int launch_face_param(DevState& s, double dt, cudaStream_t st) {
   int nf = s.nface_x + s.nface_y;
-  int n = 0;
   switch (s.flux) {
     case FLUX_KFVS: k_face_param<FLUX_KFVS><<<nblk(nf, 128), 128, 0, st>>>(s, dt); break;
     case FLUX_KCU: k_face_param<FLUX_KCU><<<nblk(nf, 128), 128, 0, st>>>(s, dt); break;
     default: k_face_param<FLUX_UGKS><<<nblk(nf, 128), 128, 0, st>>>(s, dt); break;
   }
-  ++n;
-  n += launch_moments(s, st);
+  return 1;
+}
+
+int launch_wall(DevState& s, double dt, cudaStream_t st) {
   bool wall = false;
-  for (int k = 0; k < 2 * D; ++k) wall |= s.g.bc[k] == BC_MAXWELL;
-  if (wall) {
-    unsigned gb = nblk((long)nf * 32, 256);
-    if (s.prec == 0) k_wall<double, D><<<gb, 256, 0, st>>>(s, dt);
-    else k_wall<float, D><<<gb, 256, 0, st>>>(s, dt);
-    ++n;
+  for (int k = 0; k < 2 * s.g.D; ++k) wall |= s.g.bc[k] == BC_MAXWELL;
+  if (!wall) return 0;
+  int nf = s.nface_x + s.nface_y;
+  unsigned gb = nblk((long)nf * 32, 256);
+  if (s.g.D == 1) {
+    if (s.prec == 0) k_wall<double, 1><<<gb, 256, 0, st>>>(s, dt);
+    else k_wall<float, 1><<<gb, 256, 0, st>>>(s, dt);
+  } else {
+    if (s.prec == 0) k_wall<double, 2><<<gb, 256, 0, st>>>(s, dt);
+    else k_wall<float, 2><<<gb, 256, 0, st>>>(s, dt);
   }
-  return n;
+  return 1;
 }
 
 int launch_evolve(DevState& s, double dt, cudaStream_t st) {
-  return s.g.D == 1 ? evolve_t<1>(s, dt, st) : evolve_t<2>(s, dt, st);
+  int n = launch_face_param(s, dt, st);
+  n += launch_moments(s, st);
+  n += launch_wall(s, dt, st);
+  return n;
+}
+
+int launch_cell_param(DevState& s, double dt, cudaStream_t st) {
+  if (s.g.D == 1) k_cell_param<1><<<s.res_blocks, 256, 0, st>>>(s, dt);
+  else k_cell_param<2><<<s.res_blocks, 256, 0, st>>>(s, dt);
+  return 1;
 }
 
 template <typename R, int D>
-static int update_t(DevState& s, double dt, cudaStream_t st) {
+static int finish_t(DevState& s, cudaStream_t st) {
   int n = 0;
-  k_cell_param<D><<<s.res_blocks, 256, 0, st>>>(s, dt);
-  ++n;
-  n += launch_march(s, dt, st);
   s.cur ^= 1;
   bool fill = false;
   for (int k = 0; k < 2 * D; ++k) fill |= s.g.bc[k] == BC_EXTRA || s.g.bc[k] == BC_PERIOD;
@@ -847,9 +857,16 @@ static int update_t(DevState& s, double dt, cudaStream_t st) {
   return n;
 }
 
+int launch_finish(DevState& s, cudaStream_t st) {
+  if (s.prec == 0) return s.g.D == 1 ? finish_t<double, 1>(s, st) : finish_t<double, 2>(s, st);
+  return s.g.D == 1 ? finish_t<float, 1>(s, st) : finish_t<float, 2>(s, st);
+}
+
 int launch_update(DevState& s, double dt, cudaStream_t st) {
-  if (s.prec == 0) return s.g.D == 1 ? update_t<double, 1>(s, dt, st) : update_t<double, 2>(s, dt, st);
-  return s.g.D == 1 ? update_t<float, 1>(s, dt, st) : update_t<float, 2>(s, dt, st);
+  int n = launch_cell_param(s, dt, st);
+  n += launch_march(s, dt, st);
+  n += launch_finish(s, st);
+  return n;
 }
 
 template <typename R, int D>

@@ -51,6 +51,13 @@ int launch_reconstruct(DevState& s, cudaStream_t st);
 int launch_evolve(DevState& s, double dt, cudaStream_t st);
 int launch_update(DevState& s, double dt, cudaStream_t st);
 
+// The same step split into its kernel groups (per-stage timing):
+// evolve = face_param + moments + wall; update = cell_param + march + finish.
+int launch_face_param(DevState& s, double dt, cudaStream_t st);
+int launch_wall(DevState& s, double dt, cudaStream_t st);
+int launch_cell_param(DevState& s, double dt, cudaStream_t st);
+int launch_finish(DevState& s, cudaStream_t st);
+
 // Pass A (face moments, heat flux) and pass B (pointwise update), kb_march.cu.
 int launch_moments(DevState& s, cudaStream_t st);
 int launch_march(DevState& s, double dt, cudaStream_t st);

@@ -17,6 +17,8 @@
 // and written once.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "kb_kernels.cuh"
 #include "kb_flux.cuh"
 
@@ -38,6 +40,20 @@ __device__ __forceinline__ double vl_diff(int rule, double qm, double q0, double
   if (rule == 2) return b;
   if (rule == 3) return a;
   return 0.0;
+}
+
+// 2^x on the MUFU unit (flushes results below 2^-126 to zero).
+__device__ __forceinline__ float ex2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Rule-dispatching slope; FAST = interior cell (van Leer only).
+template <bool FAST, typename R>
+__device__ __forceinline__ R slope(int rule, R qm, R q0, R qp, R epsd) {
+  if (FAST) return vl_diff(1, qm, q0, qp, epsd);
+  return vl_diff(rule, qm, q0, qp, epsd);
 }
 
 template <typename R>
@@ -143,6 +159,8 @@ __global__ void __launch_bounds__(128) k_mom(DevState s) {
     qa[c][1].init();
   }
 
+  auto run = [&](auto fast_tag) {
+  constexpr bool FAST = decltype(fast_tag)::value;
   int it = 0;
   for (int v0 = 0; v0 < g.nvel; v0 += 32, ++it) {
     const int v = v0 + lane;
@@ -155,21 +173,21 @@ __global__ void __launch_bounds__(128) k_mom(DevState s) {
     R hx[TS + 4], bx[TS + 4];
 #pragma unroll
     for (int w = 0; w < TS + 4; ++w) {
-      hx[w] = ldq(H, base[w] + v, ex[w] && ok);
-      bx[w] = ldq(Bq, base[w] + v, ex[w] && ok);
+      hx[w] = ldq(H, base[w] + v, (FAST || ex[w]) && ok);
+      bx[w] = ldq(Bq, base[w] + v, (FAST || ex[w]) && ok);
     }
     R dh[TS + 2], db[TS + 2];  // slopes of cells w = 1 .. TS+2
 #pragma unroll
     for (int w = 1; w <= TS + 2; ++w) {
-      dh[w - 1] = vl_diff(rule[w], hx[w - 1], hx[w], hx[w + 1], epsd);
-      db[w - 1] = vl_diff(rule[w], bx[w - 1], bx[w], bx[w + 1], epsd);
+      dh[w - 1] = slope<FAST>(rule[w], hx[w - 1], hx[w], hx[w + 1], epsd);
+      db[w - 1] = slope<FAST>(rule[w], bx[w - 1], bx[w], bx[w + 1], epsd);
     }
     const bool pos = un >= R(0);
     const R c2 = un * un + ut * ut;
     const R un2 = un * un;
 #pragma unroll
     for (int f = 0; f < TS + 1; ++f) {
-      if (!act[f]) continue;
+      if (FAST ? f == TS : !act[f]) continue;
       R hu = pos ? hx[f + 1] : hx[f + 2];
       R bu = pos ? bx[f + 1] : bx[f + 2];
       R su = pos ? dh[f] : dh[f + 1];
@@ -207,6 +225,12 @@ __global__ void __launch_bounds__(128) k_mom(DevState s) {
       }
     }
   }
+  };
+  bool fast = g.interp == 2 && p0 >= 2 && p0 + TS <= n - 2 && nf == TS;
+#pragma unroll
+  for (int f = 0; f < TS; ++f) fast = fast && act[f];
+  if (fast) run(std::true_type{});
+  else run(std::false_type{});
 #pragma unroll
   for (int f = 0; f < TS + 1; ++f) {
     if (!act[f]) continue;
@@ -264,6 +288,16 @@ template <>
 struct FEv<float> {
   float4 E, T, G, C, Dd;
   int kind;
+  template <bool FAST>
+  __device__ __forceinline__ void load_interior(const DevState& s, int f, bool pos) {
+    kind = 1;
+    const FaceCoef32& c = s.fc[f];
+    E = c.E;
+    T = c.T;
+    G = c.G;
+    C = pos ? c.Cp : c.Cm;
+    Dd = pos ? c.Dp : c.Dm;
+  }
   __device__ __forceinline__ void load(const DevState& s, int f, bool pos) {
     kind = s.kind[f];
     if (kind == 0) return;
@@ -285,6 +319,10 @@ struct FEv<double> {
   double dd;  // cell size along the face normal
   double wU, wV, wlam, wrn, wcB, wsc, rot;
   int kind;
+  template <bool FAST>
+  __device__ __forceinline__ void load_interior(const DevState& s, int f, bool pos) {
+    load(s, f, pos);
+  }
   __device__ __forceinline__ void load(const DevState& s, int f, bool pos) {
     (void)pos;
     kind = s.kind[f];
@@ -331,24 +369,24 @@ struct Mono {
 // Interface flux of one face at this thread's velocity.  hu, bu: upwind cell
 // values; su, sb: upwind slopes times dx; side = +0.5 when the upwind cell is
 // on the left, -0.5 on the right; hc, bc: the interior cell of a wall face.
-template <int D, int FLUX>
+template <int D, int FLUX, bool FAST = false>
 __device__ __forceinline__ void eval_face(const FEv<float>& e, const Mono<float>& M, float side,
                                           float hu, float bu, float su, float sb, float hc,
                                           float bc, double dt, float& fh, float& fb) {
   (void)dt;
-  if (e.kind == 0) {
+  if (!FAST && e.kind == 0) {
     fh = 0.f;
     fb = 0.f;
     return;
   }
   const float un = M.un;
-  if (e.kind == 2) {
+  if (!FAST && e.kind == 2) {
     // u h_wall len dt, h_wall the wall Maxwellian on incoming velocities
     // (src/Flux/flux_boundary.jl:39-61, :190-220)
     bool in = un * e.T.w >= 0.f;
     float hw, bw;
     if (in) {
-      hw = exp2f(e.E.x + e.E.y * un + e.E.z * M.ut + e.E.w * M.c2);
+      hw = ex2(e.E.x + e.E.y * un + e.E.z * M.ut + e.E.w * M.c2);
       bw = hw * e.T.z;
     } else {
       hw = hc;
@@ -365,7 +403,7 @@ __device__ __forceinline__ void eval_face(const FEv<float>& e, const Mono<float>
   fh = a * hf - c * su;
   fb = a * bf - c * sb;
   if (FLUX == FLUX_KFVS) return;
-  const float Hm = exp2f(e.E.x + e.E.y * un + e.E.z * M.ut + e.E.w * M.c2);
+  const float Hm = ex2(e.E.x + e.E.y * un + e.E.z * M.ut + e.E.w * M.c2);
   float ph = e.T.z * M.m[0];
   float pb = e.T.w * M.m[0];
   if (FLUX == FLUX_UGKS) {
@@ -380,18 +418,18 @@ __device__ __forceinline__ void eval_face(const FEv<float>& e, const Mono<float>
   fb += Hm * pb;
 }
 
-template <int D, int FLUX>
+template <int D, int FLUX, bool FAST = false>
 __device__ __forceinline__ void eval_face(const FEv<double>& e, const Mono<double>& M,
                                           double side, double hu, double bu, double su,
                                           double sb, double hc, double bc, double dt,
                                           double& fh, double& fb) {
-  if (e.kind == 0) {
+  if (!FAST && e.kind == 0) {
     fh = 0.0;
     fb = 0.0;
     return;
   }
   const double un = M.un, ut = M.ut;
-  if (e.kind == 2) {
+  if (!FAST && e.kind == 2) {
     bool in = un * e.rot >= 0.0;
     double hw, bw;
     if (in) {
@@ -421,10 +459,10 @@ __device__ __forceinline__ void eval_face(const FEv<double>& e, const Mono<doubl
 __device__ __forceinline__ void relax(const CellCoef32& k, bool shak, float u, float vv,
                                       float c2, float h0, float b0, float dh, float db,
                                       float& hn, float& bn) {
-  float M = exp2f(k.EM.x + k.EM.y * u + k.EM.z * vv + k.EM.w * c2);
+  float M = ex2(k.EM.x + k.EM.y * u + k.EM.z * vv + k.EM.w * c2);
   float MH = M, MB = M * k.A.x;
   if (shak) {
-    float OH = exp2f(k.EO.x + k.EO.y * u + k.EO.z * vv + k.EO.w * c2);
+    float OH = ex2(k.EO.x + k.EO.y * u + k.EO.z * vv + k.EO.w * c2);
     float cq = (k.Q.x + k.Q.y * u + k.Q.z * vv) * OH;
     float tl = k.TL.x + k.TL.y * u + k.TL.z * vv + k.TL.w * c2;
     MH += cq * (tl - 5.f);
@@ -547,13 +585,14 @@ __global__ void __launch_bounds__(128) k_march(DevState s, double dt, int RY) {
     }
   }
 
-  for (int j = j0; j < j1; ++j) {
+  auto row = [&](int j, auto fast_tag) {
+    constexpr bool FAST = decltype(fast_tag)::value;
     R xh[TX + 4], xb[TX + 4];
     const long rb = rowb(j);
     if (D == 2) {
 #pragma unroll
       for (int c = 0; c < TX; ++c) {
-        bool e = exx[c + 2] && rowok(j + 2);
+        bool e = FAST || (exx[c + 2] && rowok(j + 2));
         yh[3][c] = ldq(H, rowb(j + 2) + colw[c + 2], e);
         yb[3][c] = ldq(Bq, rowb(j + 2) + colw[c + 2], e);
         xh[c + 2] = yh[1][c];
@@ -568,10 +607,10 @@ __global__ void __launch_bounds__(128) k_march(DevState s, double dt, int RY) {
     }
 #pragma unroll
     for (int w = 0; w < 2; ++w) {
-      xh[w] = ldq(H, rb + colw[w], exx[w]);
-      xb[w] = ldq(Bq, rb + colw[w], exx[w]);
-      xh[TX + 2 + w] = ldq(H, rb + colw[TX + 2 + w], exx[TX + 2 + w]);
-      xb[TX + 2 + w] = ldq(Bq, rb + colw[TX + 2 + w], exx[TX + 2 + w]);
+      xh[w] = ldq(H, rb + colw[w], FAST || exx[w]);
+      xb[w] = ldq(Bq, rb + colw[w], FAST || exx[w]);
+      xh[TX + 2 + w] = ldq(H, rb + colw[TX + 2 + w], FAST || exx[TX + 2 + w]);
+      xb[TX + 2 + w] = ldq(Bq, rb + colw[TX + 2 + w], FAST || exx[TX + 2 + w]);
     }
     // y faces above row j
     R fyh2[TX], fyb2[TX];
@@ -581,28 +620,29 @@ __global__ void __launch_bounds__(128) k_march(DevState s, double dt, int RY) {
       for (int c = 0; c < TX; ++c) {
         FEv<R> e;
         e.kind = 0;
-        if (c < ncol) e.load(s, s.nface_x + (j + 1) * g.nx + i0 + c, py);
+        if (FAST) e.template load_interior<FAST>(s, s.nface_x + (j + 1) * g.nx + i0 + c, py);
+        else if (c < ncol) e.load(s, s.nface_x + (j + 1) * g.nx + i0 + c, py);
         R hu, bu, su, sb;
         if (py) {
           hu = yh[1][c];
           bu = yb[1][c];
-          su = vl_diff(rlo, yh[0][c], yh[1][c], yh[2][c], epsy);
-          sb = vl_diff(rlo, yb[0][c], yb[1][c], yb[2][c], epsy);
+          su = slope<FAST>(rlo, yh[0][c], yh[1][c], yh[2][c], epsy);
+          sb = slope<FAST>(rlo, yb[0][c], yb[1][c], yb[2][c], epsy);
         } else {
           hu = yh[2][c];
           bu = yb[2][c];
-          su = vl_diff(rhi, yh[1][c], yh[2][c], yh[3][c], epsy);
-          sb = vl_diff(rhi, yb[1][c], yb[2][c], yb[3][c], epsy);
+          su = slope<FAST>(rhi, yh[1][c], yh[2][c], yh[3][c], epsy);
+          sb = slope<FAST>(rhi, yb[1][c], yb[2][c], yb[3][c], epsy);
         }
-        eval_face<D, FLUX>(e, MY, sys, hu, bu, su, sb, yh[1][c], yb[1][c], dt, fyh2[c], fyb2[c]);
+        eval_face<D, FLUX, FAST>(e, MY, sys, hu, bu, su, sb, yh[1][c], yb[1][c], dt, fyh2[c], fyb2[c]);
       }
     }
     // x slopes of cells w = 1 .. TX+2 and the x faces of row j
     R dh[TX + 2], db[TX + 2];
 #pragma unroll
     for (int w = 1; w <= TX + 2; ++w) {
-      dh[w - 1] = vl_diff(rx[w], xh[w - 1], xh[w], xh[w + 1], epsx);
-      db[w - 1] = vl_diff(rx[w], xb[w - 1], xb[w], xb[w + 1], epsx);
+      dh[w - 1] = slope<FAST>(rx[w], xh[w - 1], xh[w], xh[w + 1], epsx);
+      db[w - 1] = slope<FAST>(rx[w], xb[w - 1], xb[w], xb[w + 1], epsx);
     }
     R fxh[TX + 1], fxb[TX + 1];
 #pragma unroll
@@ -610,19 +650,20 @@ __global__ void __launch_bounds__(128) k_march(DevState s, double dt, int RY) {
       FEv<R> e;
       e.kind = 0;
       const int fi = i0 + f;
-      if (f <= ncol) e.load(s, j * (g.nx + 1) + fi, px);
+      if (FAST) e.template load_interior<FAST>(s, j * (g.nx + 1) + fi, px);
+      else if (f <= ncol) e.load(s, j * (g.nx + 1) + fi, px);
       R hu = px ? xh[f + 1] : xh[f + 2];
       R bu = px ? xb[f + 1] : xb[f + 2];
       R su = px ? dh[f] : dh[f + 1];
       R sb = px ? db[f] : db[f + 1];
       R hc = fi == 0 ? xh[f + 2] : xh[f + 1];
       R bc = fi == 0 ? xb[f + 2] : xb[f + 1];
-      eval_face<D, FLUX>(e, MX, sxs, hu, bu, su, sb, hc, bc, dt, fxh[f], fxb[f]);
+      eval_face<D, FLUX, FAST>(e, MX, sxs, hu, bu, su, sb, hc, bc, dt, fxh[f], fxb[f]);
     }
     // update the cells of row j
 #pragma unroll
     for (int c = 0; c < TX; ++c) {
-      if (c >= ncol) continue;
+      if (!FAST && c >= ncol) continue;
       const int cell = cell_index(g, i0 + c, j);
       R dhh = fxh[c] - fxh[c + 1];
       R dbb = fxb[c] - fxb[c + 1];
@@ -654,6 +695,11 @@ __global__ void __launch_bounds__(128) k_march(DevState s, double dt, int RY) {
         fyb[c] = fyb2[c];
       }
     }
+  };
+  const bool fastx = g.interp == 2 && i0 >= 2 && i0 + TX <= g.nx - 2;
+  for (int j = j0; j < j1; ++j) {
+    if (fastx && (D == 1 || (j >= 1 && j <= g.ny - 3))) row(j, std::true_type{});
+    else row(j, std::false_type{});
   }
 }
 

@@ -70,7 +70,11 @@ SIGNATURES = {
     "kb_status": [_H],
     "kb_device_bytes": [_H, ctypes.POINTER(ctypes.c_int64)],
     "kb_launch_count": [_H, ctypes.POINTER(ctypes.c_int64)],
+    "kb_set_timing": [_H, ctypes.c_int],
+    "kb_get_timing": [_H, _D, ctypes.POINTER(ctypes.c_int64)],
+    "kb_get_stream": [_H, ctypes.POINTER(ctypes.c_void_p)],
 }
+STAGES = ("reconstruct", "face_param", "moments", "wall", "cell_param", "update", "finish")
 
 
 def load(path=None):

@@ -152,6 +152,20 @@ class Handle:
         self.call("kb_launch_count", ctypes.byref(n))
         return n.value
 
+    def set_timing(self, on=True):
+        self.call("kb_set_timing", 1 if on else 0)
+
+    def timing(self):
+        ms = np.zeros(len(N.STAGES))
+        n = (ctypes.c_int64 * len(N.STAGES))()
+        self.call("kb_get_timing", N.ptr(ms), n)
+        return {k: (ms[i], n[i]) for i, k in enumerate(N.STAGES)}
+
+    def stream(self):
+        p = ctypes.c_void_p()
+        self.call("kb_get_stream", ctypes.byref(p))
+        return p.value
+
     def device_bytes(self):
         n = ctypes.c_int64()
         self.call("kb_device_bytes", ctypes.byref(n))

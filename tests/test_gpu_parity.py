@@ -39,6 +39,10 @@ CASES_2D = [
     ("quadrant-kcu-shakhov-extra", quadrant(flux="kcu", coll="shakhov", Kn=1e-2)),
     ("quadrant-kfvs-shakhov-fix", quadrant(flux="kfvs", coll="shakhov", bc="fix", ng=0)),
     ("quadrant-ugks-shakhov-fix-rect", quadrant(nx=9, ny=7, nu=11, nv=13, coll="shakhov", bc="fix", ng=0)),
+    # grids wide enough for the interior (branch-free) strips and segments
+    ("quadrant-ugks-shakhov-extra-16", quadrant(nx=17, ny=18, nu=8, nv=8, coll="shakhov", Kn=1e-2)),
+    ("cavity-kfvs-shakhov-maxwell-16", cavity(nx=16, ny=19, nu=8, nv=6, flux="kfvs")),
+    ("cavity-kcu-bgk-maxwell-16", cavity(nx=18, ny=16, nu=10, nv=8, coll="bgk")),
 ]
 
 
