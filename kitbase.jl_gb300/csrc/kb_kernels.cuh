@@ -7,8 +7,13 @@
 namespace kb {
 
 // Device buffers of one solve (owned by kb_handle, see kb_abi.cu).
+// Tunable launch shapes (kb_set_tuning); 0 selects the built-in default.
+enum { KB_TUNE_MARCH_TX = 0, KB_TUNE_MARCH_RY = 1, KB_TUNE_MARCH_BS = 2, KB_TUNE_MOM_TS = 3,
+       TUNE_N = 4 };
+
 struct DevState {
   Geo g;
+  int tune[TUNE_N];
   int prec;   // 0: FP64, 1: FP32 split
   int flux, coll;
   const double* u;  // velocity tables [vstride]

@@ -505,17 +505,19 @@ __device__ __forceinline__ void relax(const CP<double>& C, double ds, double u, 
 }
 
 // Pass B: one thread per velocity, CTA = (strip of TX columns, RY rows,
-// blockDim.x velocities).  Window rows yh[0..3] = rows j-1 .. j+2.
-template <typename R, int D, int FLUX, int TX>
-__global__ void __launch_bounds__(128) k_march(DevState s, double dt, int RY) {
+// BS velocities).  Window rows wh[0..3] = rows j-1 .. j+2 of the strip; the
+// next window row and the next row's 4-cell x halo are loaded one iteration
+// ahead so their latency overlaps the current row's arithmetic.
+template <typename R, int D, int FLUX, int TX, int BS>
+__global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march(DevState s, double dt, int RY) {
   const Geo& g = s.g;
-  const int v = blockIdx.z * blockDim.x + threadIdx.x;
+  const int v = blockIdx.z * BS + threadIdx.x;
   if (v >= g.nvel) return;
   const int i0 = blockIdx.x * TX;
   const int ncol = min(TX, g.nx - i0);
   const int j0 = D == 2 ? blockIdx.y * RY : 0;
   const int j1 = D == 2 ? min(g.ny, j0 + RY) : 1;
-  const long vs = g.vstride;
+  const int vs = g.vstride;
   const R* __restrict__ H = (const R*)s.h[s.cur];
   const R* __restrict__ Bq = (const R*)s.b[s.cur];
   R* __restrict__ Ho = (R*)s.h[s.cur ^ 1];
@@ -534,35 +536,48 @@ __global__ void __launch_bounds__(128) k_march(DevState s, double dt, int RY) {
 
   bool exx[TX + 4];
   int rx[TX + 4];
-  long colw[TX + 4];
+  int coff[TX + 4];  // offset of (column, v) inside a row
 #pragma unroll
   for (int w = 0; w < TX + 4; ++w) {
     int i = i0 - 2 + w;
     exx[w] = i >= -g.ngx && i < g.nx + g.ngx;
     rx[w] = slope_rule(g, 0, i);
-    colw[w] = (long)(i + g.ngx) * vs + v;
+    coff[w] = exx[w] ? (i + g.ngx) * vs + v : 0;
   }
   const long rows = (long)g.nxt * vs;
   auto rowok = [&](int j) { return j >= -g.ngy && j < g.ny + g.ngy; };
-  auto rowb = [&](int j) { return (long)(j + g.ngy) * rows; };
-
-  R yh[4][TX], yb[4][TX];
-  R fyh[TX], fyb[TX];
-  if (D == 2) {
-    // prologue: rows j0-2 .. j0+1 and the y face below row j0
-    R ph[TX], pb[TX];
+  auto tile = [&](int j, R* th, R* tb) {
+    const bool rk = rowok(j);
+    const long ro = rk ? (long)(j + g.ngy) * rows : 0;
 #pragma unroll
     for (int c = 0; c < TX; ++c) {
-      bool e = exx[c + 2];
-      ph[c] = ldq(H, rowb(j0 - 2) + colw[c + 2], e && rowok(j0 - 2));
-      pb[c] = ldq(Bq, rowb(j0 - 2) + colw[c + 2], e && rowok(j0 - 2));
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        int j = j0 - 1 + k;
-        yh[k][c] = ldq(H, rowb(j) + colw[c + 2], e && rowok(j));
-        yb[k][c] = ldq(Bq, rowb(j) + colw[c + 2], e && rowok(j));
-      }
+      const bool e = rk && exx[c + 2];
+      th[c] = ldq(H + ro, coff[c + 2], e);
+      tb[c] = ldq(Bq + ro, coff[c + 2], e);
     }
+  };
+  auto halo = [&](int j, R* hh, R* hb) {
+    const bool rk = rowok(j);
+    const long ro = rk ? (long)(j + g.ngy) * rows : 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int w = k < 2 ? k : TX + k;
+      hh[k] = ldq(H + ro, coff[w], rk && exx[w]);
+      hb[k] = ldq(Bq + ro, coff[w], rk && exx[w]);
+    }
+  };
+
+  R wh[4][TX], wb[4][TX];
+  R nh[TX], nb[TX];
+  R hh[4], hb[4], nhh[4], nhb[4];
+  R fyh[TX], fyb[TX];
+  if (D == 2) {
+    // prologue: rows j0-2 .. j0+2, the halo of row j0 and the y face below row j0
+    R ph[TX], pb[TX];
+    tile(j0 - 2, ph, pb);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) tile(j0 - 1 + k, wh[k], wb[k]);
+    halo(j0, hh, hb);
     const int rlo = slope_rule(g, 1, j0 - 1), rhi = slope_rule(g, 1, j0);
 #pragma unroll
     for (int c = 0; c < TX; ++c) {
@@ -571,46 +586,42 @@ __global__ void __launch_bounds__(128) k_march(DevState s, double dt, int RY) {
       if (c < ncol) e.load(s, s.nface_x + j0 * g.nx + i0 + c, py);
       R hu, bu, su, sb;
       if (py) {
-        hu = yh[0][c];
-        bu = yb[0][c];
-        su = vl_diff(rlo, ph[c], yh[0][c], yh[1][c], epsy);
-        sb = vl_diff(rlo, pb[c], yb[0][c], yb[1][c], epsy);
+        hu = wh[0][c];
+        bu = wb[0][c];
+        su = vl_diff(rlo, ph[c], wh[0][c], wh[1][c], epsy);
+        sb = vl_diff(rlo, pb[c], wb[0][c], wb[1][c], epsy);
       } else {
-        hu = yh[1][c];
-        bu = yb[1][c];
-        su = vl_diff(rhi, yh[0][c], yh[1][c], yh[2][c], epsy);
-        sb = vl_diff(rhi, yb[0][c], yb[1][c], yb[2][c], epsy);
+        hu = wh[1][c];
+        bu = wb[1][c];
+        su = vl_diff(rhi, wh[0][c], wh[1][c], wh[2][c], epsy);
+        sb = vl_diff(rhi, wb[0][c], wb[1][c], wb[2][c], epsy);
       }
-      eval_face<D, FLUX>(e, MY, sys, hu, bu, su, sb, yh[1][c], yb[1][c], dt, fyh[c], fyb[c]);
+      eval_face<D, FLUX>(e, MY, sys, hu, bu, su, sb, wh[1][c], wb[1][c], dt, fyh[c], fyb[c]);
     }
+  } else {
+    tile(0, wh[1], wb[1]);
+    halo(0, hh, hb);
   }
 
   auto row = [&](int j, auto fast_tag) {
     constexpr bool FAST = decltype(fast_tag)::value;
+    // prefetch the next window row and the next row's halo
+    if (D == 2 && j + 1 < j1) {
+      tile(j + 3, nh, nb);
+      halo(j + 1, nhh, nhb);
+    }
     R xh[TX + 4], xb[TX + 4];
-    const long rb = rowb(j);
-    if (D == 2) {
 #pragma unroll
-      for (int c = 0; c < TX; ++c) {
-        bool e = FAST || (exx[c + 2] && rowok(j + 2));
-        yh[3][c] = ldq(H, rowb(j + 2) + colw[c + 2], e);
-        yb[3][c] = ldq(Bq, rowb(j + 2) + colw[c + 2], e);
-        xh[c + 2] = yh[1][c];
-        xb[c + 2] = yb[1][c];
-      }
-    } else {
-#pragma unroll
-      for (int c = 0; c < TX; ++c) {
-        xh[c + 2] = ldq(H, colw[c + 2], exx[c + 2]);
-        xb[c + 2] = ldq(Bq, colw[c + 2], exx[c + 2]);
-      }
+    for (int c = 0; c < TX; ++c) {
+      xh[c + 2] = wh[1][c];
+      xb[c + 2] = wb[1][c];
     }
 #pragma unroll
-    for (int w = 0; w < 2; ++w) {
-      xh[w] = ldq(H, rb + colw[w], FAST || exx[w]);
-      xb[w] = ldq(Bq, rb + colw[w], FAST || exx[w]);
-      xh[TX + 2 + w] = ldq(H, rb + colw[TX + 2 + w], FAST || exx[TX + 2 + w]);
-      xb[TX + 2 + w] = ldq(Bq, rb + colw[TX + 2 + w], FAST || exx[TX + 2 + w]);
+    for (int k = 0; k < 2; ++k) {
+      xh[k] = hh[k];
+      xb[k] = hb[k];
+      xh[TX + 2 + k] = hh[2 + k];
+      xb[TX + 2 + k] = hb[2 + k];
     }
     // y faces above row j
     R fyh2[TX], fyb2[TX];
@@ -624,17 +635,18 @@ __global__ void __launch_bounds__(128) k_march(DevState s, double dt, int RY) {
         else if (c < ncol) e.load(s, s.nface_x + (j + 1) * g.nx + i0 + c, py);
         R hu, bu, su, sb;
         if (py) {
-          hu = yh[1][c];
-          bu = yb[1][c];
-          su = slope<FAST>(rlo, yh[0][c], yh[1][c], yh[2][c], epsy);
-          sb = slope<FAST>(rlo, yb[0][c], yb[1][c], yb[2][c], epsy);
+          hu = wh[1][c];
+          bu = wb[1][c];
+          su = slope<FAST>(rlo, wh[0][c], wh[1][c], wh[2][c], epsy);
+          sb = slope<FAST>(rlo, wb[0][c], wb[1][c], wb[2][c], epsy);
         } else {
-          hu = yh[2][c];
-          bu = yb[2][c];
-          su = slope<FAST>(rhi, yh[1][c], yh[2][c], yh[3][c], epsy);
-          sb = slope<FAST>(rhi, yb[1][c], yb[2][c], yb[3][c], epsy);
+          hu = wh[2][c];
+          bu = wb[2][c];
+          su = slope<FAST>(rhi, wh[1][c], wh[2][c], wh[3][c], epsy);
+          sb = slope<FAST>(rhi, wb[1][c], wb[2][c], wb[3][c], epsy);
         }
-        eval_face<D, FLUX, FAST>(e, MY, sys, hu, bu, su, sb, yh[1][c], yb[1][c], dt, fyh2[c], fyb2[c]);
+        eval_face<D, FLUX, FAST>(e, MY, sys, hu, bu, su, sb, wh[1][c], wb[1][c], dt, fyh2[c],
+                                 fyb2[c]);
       }
     }
     // x slopes of cells w = 1 .. TX+2 and the x faces of row j
@@ -661,6 +673,7 @@ __global__ void __launch_bounds__(128) k_march(DevState s, double dt, int RY) {
       eval_face<D, FLUX, FAST>(e, MX, sxs, hu, bu, su, sb, hc, bc, dt, fxh[f], fxb[f]);
     }
     // update the cells of row j
+    const long ro = (long)(j + g.ngy) * rows;
 #pragma unroll
     for (int c = 0; c < TX; ++c) {
       if (!FAST && c >= ncol) continue;
@@ -679,20 +692,27 @@ __global__ void __launch_bounds__(128) k_march(DevState s, double dt, int RY) {
         const CP<double> C = load_cp<double>(s, cell);
         relax(C, ds, u, vv, Kf, D, xh[c + 2], xb[c + 2], dhh, dbb, hn, bn);
       }
-      Ho[rb + colw[c + 2]] = hn;
-      Bo[rb + colw[c + 2]] = bn;
+      Ho[ro + coff[c + 2]] = hn;
+      Bo[ro + coff[c + 2]] = bn;
     }
     if (D == 2) {
 #pragma unroll
       for (int c = 0; c < TX; ++c) {
-        yh[0][c] = yh[1][c];
-        yb[0][c] = yb[1][c];
-        yh[1][c] = yh[2][c];
-        yb[1][c] = yb[2][c];
-        yh[2][c] = yh[3][c];
-        yb[2][c] = yb[3][c];
+        wh[0][c] = wh[1][c];
+        wb[0][c] = wb[1][c];
+        wh[1][c] = wh[2][c];
+        wb[1][c] = wb[2][c];
+        wh[2][c] = wh[3][c];
+        wb[2][c] = wb[3][c];
+        wh[3][c] = nh[c];
+        wb[3][c] = nb[c];
         fyh[c] = fyh2[c];
         fyb[c] = fyb2[c];
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        hh[k] = nhh[k];
+        hb[k] = nhb[k];
       }
     }
   };
@@ -711,22 +731,28 @@ constexpr int TS_MOM = 4;   // faces per warp in pass A
 constexpr int TX_MARCH = 4; // columns per strip in pass B
 constexpr int RY_MARCH = 32;
 
-template <typename R, int D, int FLUX>
-static int mom_t(DevState& s, cudaStream_t st) {
+template <typename R, int D, int FLUX, int TS>
+static int mom_go(DevState& s, cudaStream_t st) {
   const Geo& g = s.g;
   int n = 0;
-  long wx = (long)((g.nx + TS_MOM - 1) / TS_MOM) * g.ny;
+  long wx = (long)((g.nx + TS - 1) / TS) * g.ny;
   if (s.coll == COLL_SHAKHOV)
-    k_mom<R, D, FLUX, TS_MOM, true, 0><<<nblk2(wx * 32, 128), 128, 0, st>>>(s);
+    k_mom<R, D, FLUX, TS, true, 0><<<nblk2(wx * 32, 128), 128, 0, st>>>(s);
   else
-    k_mom<R, D, FLUX, TS_MOM, false, 0><<<nblk2(wx * 32, 128), 128, 0, st>>>(s);
+    k_mom<R, D, FLUX, TS, false, 0><<<nblk2(wx * 32, 128), 128, 0, st>>>(s);
   ++n;
   if (D == 2) {
-    long wy = (long)((g.ny + TS_MOM - 1) / TS_MOM) * g.nx;
-    k_mom<R, D, FLUX, TS_MOM, false, 1><<<nblk2(wy * 32, 128), 128, 0, st>>>(s);
+    long wy = (long)((g.ny + TS - 1) / TS) * g.nx;
+    k_mom<R, D, FLUX, TS, false, 1><<<nblk2(wy * 32, 128), 128, 0, st>>>(s);
     ++n;
   }
   return n;
+}
+
+template <typename R, int D, int FLUX>
+static int mom_t(DevState& s, cudaStream_t st) {
+  if (s.tune[KB_TUNE_MOM_TS] == 2) return mom_go<R, D, FLUX, 2>(s, st);
+  return mom_go<R, D, FLUX, TS_MOM>(s, st);
 }
 
 int launch_moments(DevState& s, cudaStream_t st) {
@@ -745,13 +771,31 @@ int launch_moments(DevState& s, cudaStream_t st) {
 #undef KB_MOM
 }
 
+template <typename R, int D, int FLUX, int TX, int BS>
+static void march_go(DevState& s, double dt, cudaStream_t st) {
+  const Geo& g = s.g;
+  const int ry = s.tune[KB_TUNE_MARCH_RY] > 0 ? s.tune[KB_TUNE_MARCH_RY] : RY_MARCH;
+  dim3 grid((g.nx + TX - 1) / TX, D == 2 ? (g.ny + ry - 1) / ry : 1, (g.nvel + BS - 1) / BS);
+  k_march<R, D, FLUX, TX, BS><<<grid, BS, 0, st>>>(s, dt, ry);
+}
+
 template <typename R, int D, int FLUX>
 static int march_t(DevState& s, double dt, cudaStream_t st) {
-  const Geo& g = s.g;
-  const int bs = 128;
-  dim3 grid((g.nx + TX_MARCH - 1) / TX_MARCH, D == 2 ? (g.ny + RY_MARCH - 1) / RY_MARCH : 1,
-            (g.nvel + bs - 1) / bs);
-  k_march<R, D, FLUX, TX_MARCH><<<grid, bs, 0, st>>>(s, dt, RY_MARCH);
+  const int tx = s.tune[KB_TUNE_MARCH_TX] > 0 ? s.tune[KB_TUNE_MARCH_TX] : TX_MARCH;
+  const int bs = s.tune[KB_TUNE_MARCH_BS] > 0 ? s.tune[KB_TUNE_MARCH_BS] : 128;
+  if (tx == 2) {
+    if (bs == 64) march_go<R, D, FLUX, 2, 64>(s, dt, st);
+    else if (bs == 256) march_go<R, D, FLUX, 2, 256>(s, dt, st);
+    else march_go<R, D, FLUX, 2, 128>(s, dt, st);
+  } else if (tx == 8) {
+    if (bs == 64) march_go<R, D, FLUX, 8, 64>(s, dt, st);
+    else if (bs == 256) march_go<R, D, FLUX, 8, 256>(s, dt, st);
+    else march_go<R, D, FLUX, 8, 128>(s, dt, st);
+  } else {
+    if (bs == 64) march_go<R, D, FLUX, 4, 64>(s, dt, st);
+    else if (bs == 256) march_go<R, D, FLUX, 4, 256>(s, dt, st);
+    else march_go<R, D, FLUX, 4, 128>(s, dt, st);
+  }
   return 1;
 }
 

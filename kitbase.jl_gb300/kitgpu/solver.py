@@ -161,6 +161,15 @@ class Handle:
         self.call("kb_get_timing", N.ptr(ms), n)
         return {k: (ms[i], n[i]) for i, k in enumerate(N.STAGES)}
 
+    def set_tuning(self, march_tx=0, march_ry=0, march_bs=0, mom_ts=0):
+        arr = (ctypes.c_int32 * 4)(march_tx, march_ry, march_bs, mom_ts)
+        self.call("kb_set_tuning", arr, 4)
+
+    def tuning(self):
+        arr = (ctypes.c_int32 * 4)()
+        self.call("kb_get_tuning", arr, 4)
+        return dict(zip(("march_tx", "march_ry", "march_bs", "mom_ts"), list(arr)))
+
     def stream(self):
         p = ctypes.c_void_p()
         self.call("kb_get_stream", ctypes.byref(p))

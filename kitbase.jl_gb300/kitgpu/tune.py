@@ -1,0 +1,97 @@
+"""Autotuner of the launch shapes of the two HBM passes.
+
+For a handle it times candidate shapes of the pointwise update pass (columns
+per strip, rows per CTA, threads per CTA) and of the moment pass (faces per
+warp) with the library's own CUDA-event stage timing, on the handle's real
+state, and keeps the fastest.  Results are cached per problem signature
+(dimension, velocity count, flux, collision, precision, grid size class) in a
+JSON file so repeated solves of the same shape skip the search.
+
+The search advances the solution by a few steps; callers that need the
+original state re-upload it (bench.py does) or tune on a copy.
+"""
+import itertools
+import json
+import os
+
+from . import _native as N
+
+CACHE = os.environ.get("KITGPU_TUNE_CACHE",
+                       os.path.join(os.path.expanduser("~"), ".cache", "kitgpu_tune.json"))
+
+MARCH_TX = (2, 4, 8)
+MARCH_BS = (64, 128, 256)
+MARCH_RY = (16, 32, 64)
+MOM_TS = (2, 4)
+
+
+def signature(handle):
+    c = handle.cfg
+    cells = c.nx * (c.ny if c.dim == 2 else 1)
+    size = "small" if cells < 4096 else ("medium" if cells < 65536 else "large")
+    return "d%d-v%d-f%d-c%d-p%d-%s" % (c.dim, handle.nvel, c.flux, c.collision, c.precision, size)
+
+
+def _load():
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _save(d):
+    try:
+        os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+        with open(CACHE, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+    except OSError:
+        pass
+
+
+def _time(handle, dt, steps):
+    handle.set_timing(True)
+    handle.step(dt, steps)
+    t = handle.timing()
+    handle.set_timing(False)
+    upd = t["update"][0] / max(t["update"][1], 1)
+    mom = t["moments"][0] / max(t["moments"][1], 1)
+    return upd, mom
+
+
+def autotune(handle, dt, steps=2, use_cache=True, verbose=False):
+    """Pick the fastest launch shapes for `handle`; returns the chosen dict and
+    the per-candidate timings (ms per step of each pass)."""
+    key = signature(handle)
+    cache = _load() if use_cache else {}
+    if use_cache and key in cache:
+        best = cache[key]
+        handle.set_tuning(**best)
+        return best, None
+    res_march = {}
+    ry_opts = MARCH_RY if handle.dim == 2 else (1,)
+    for tx, bs, ry in itertools.product(MARCH_TX, MARCH_BS, ry_opts):
+        handle.set_tuning(march_tx=tx, march_ry=ry, march_bs=bs, mom_ts=0)
+        handle.step(dt, 1)  # warm-up of this shape
+        upd, _ = _time(handle, dt, steps)
+        res_march[(tx, bs, ry)] = upd
+        if verbose:
+            print("march tx=%d bs=%d ry=%d: %.3f ms" % (tx, bs, ry, upd), flush=True)
+    tx, bs, ry = min(res_march, key=res_march.get)
+    res_mom = {}
+    for ts in MOM_TS:
+        handle.set_tuning(march_tx=tx, march_ry=ry, march_bs=bs, mom_ts=ts)
+        handle.step(dt, 1)
+        _, mom = _time(handle, dt, steps)
+        res_mom[ts] = mom
+        if verbose:
+            print("moments ts=%d: %.3f ms" % (ts, mom), flush=True)
+    ts = min(res_mom, key=res_mom.get)
+    best = dict(march_tx=tx, march_ry=ry, march_bs=bs, mom_ts=ts)
+    handle.set_tuning(**best)
+    if use_cache:
+        cache[key] = best
+        _save(cache)
+    timings = {"march": {"tx%d-bs%d-ry%d" % k: v for k, v in res_march.items()},
+               "moments": {"ts%d" % k: v for k, v in res_mom.items()}}
+    return best, timings
