@@ -267,14 +267,21 @@ def run_ours(args):
     h_out, b_out = pin((ncell, nvel)), pin((ncell, nvel))
     w_out, p_out = np.zeros_like(w_host), np.zeros_like(p_host)
 
-    def make(prec):
+    def make(prec, tuning=None):
         hd = kitgpu.Handle(kitgpu.kb_config(KS, prec), vs.flat(vs.u), vs.flat(vs.v),
                            vs.flat(vs.weights))
         hd.upload(w_host, p_host, h_host, b_host)
+        if tuning:
+            hd.set_tuning(**tuning)
         return hd
 
     hd = make("fp32")
     dt = hd.timestep(KS.set.cfl, 0.0, KS.set.maxTime)
+    # launch shapes from the project autotuner (advances the state a few steps;
+    # the state is re-uploaded before timing)
+    from kitgpu import tune
+    best, _ = tune.autotune(hd, dt, steps=1, use_cache=not args.retune)
+    hd.upload(w_host, p_host, h_host, b_host)
     stream = torch.cuda.ExternalStream(hd.stream())
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
@@ -427,6 +434,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h,
                 "note": "kb_upload_state (FP64 pinned host) + K kb_step + kb_download_state"},
         "gpu_launches": launches,
+        "tuning": best,
         "clocks": clocks.summary(),
         "fp64_plain": fp64,
         "linf_error_vs_fp64": err,
@@ -449,6 +457,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-error", action="store_true")
     ap.add_argument("--err-steps", type=int, default=40)
+    ap.add_argument("--retune", action="store_true", help="ignore the autotuner cache")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
