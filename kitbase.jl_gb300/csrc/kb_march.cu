@@ -284,6 +284,7 @@ template <typename R>
 struct FEv;
 
 // FP32: monomial form of FaceCoef32.
+constexpr bool FLUX_NEEDS_G = true;
 template <>
 struct FEv<float> {
   float4 E, T, G, C, Dd;
@@ -294,9 +295,12 @@ struct FEv<float> {
     const FaceCoef32& c = s.fc[f];
     E = c.E;
     T = c.T;
-    G = c.G;
-    C = pos ? c.Cp : c.Cm;
-    Dd = pos ? c.Dp : c.Dm;
+    if (FLUX_NEEDS_G) {
+      G = c.G;
+      const float4* cd = pos ? &c.Cp : &c.Cm;
+      C = cd[0];
+      Dd = cd[1];
+    }
   }
   __device__ __forceinline__ void load(const DevState& s, int f, bool pos) {
     kind = s.kind[f];
@@ -603,8 +607,13 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
     halo(0, hh, hb);
   }
 
-  auto row = [&](int j, auto fast_tag) {
+  auto row = [&](int j, auto fast_tag, auto sign_tag) {
     constexpr bool FAST = decltype(fast_tag)::value;
+    constexpr int SG = decltype(sign_tag)::value;
+    // compile-time upwind sides when the warp's velocities share their signs
+    const bool qx = SG == 0 ? px : (SG == 1 || SG == 2);
+    const bool qy = SG == 0 ? py : (SG == 1 || SG == 3);
+    const R qxs = qx ? R(0.5) : R(-0.5), qys = qy ? R(0.5) : R(-0.5);
     // prefetch the next window row and the next row's halo
     if (D == 2 && j + 1 < j1) {
       tile(j + 3, nh, nb);
@@ -631,10 +640,10 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
       for (int c = 0; c < TX; ++c) {
         FEv<R> e;
         e.kind = 0;
-        if (FAST) e.template load_interior<FAST>(s, s.nface_x + (j + 1) * g.nx + i0 + c, py);
-        else if (c < ncol) e.load(s, s.nface_x + (j + 1) * g.nx + i0 + c, py);
+        if (FAST) e.template load_interior<FAST>(s, s.nface_x + (j + 1) * g.nx + i0 + c, qy);
+        else if (c < ncol) e.load(s, s.nface_x + (j + 1) * g.nx + i0 + c, qy);
         R hu, bu, su, sb;
-        if (py) {
+        if (qy) {
           hu = wh[1][c];
           bu = wb[1][c];
           su = slope<FAST>(rlo, wh[0][c], wh[1][c], wh[2][c], epsy);
@@ -645,7 +654,7 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
           su = slope<FAST>(rhi, wh[1][c], wh[2][c], wh[3][c], epsy);
           sb = slope<FAST>(rhi, wb[1][c], wb[2][c], wb[3][c], epsy);
         }
-        eval_face<D, FLUX, FAST>(e, MY, sys, hu, bu, su, sb, wh[1][c], wb[1][c], dt, fyh2[c],
+        eval_face<D, FLUX, FAST>(e, MY, qys, hu, bu, su, sb, wh[1][c], wb[1][c], dt, fyh2[c],
                                  fyb2[c]);
       }
     }
@@ -662,15 +671,15 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
       FEv<R> e;
       e.kind = 0;
       const int fi = i0 + f;
-      if (FAST) e.template load_interior<FAST>(s, j * (g.nx + 1) + fi, px);
-      else if (f <= ncol) e.load(s, j * (g.nx + 1) + fi, px);
-      R hu = px ? xh[f + 1] : xh[f + 2];
-      R bu = px ? xb[f + 1] : xb[f + 2];
-      R su = px ? dh[f] : dh[f + 1];
-      R sb = px ? db[f] : db[f + 1];
+      if (FAST) e.template load_interior<FAST>(s, j * (g.nx + 1) + fi, qx);
+      else if (f <= ncol) e.load(s, j * (g.nx + 1) + fi, qx);
+      R hu = qx ? xh[f + 1] : xh[f + 2];
+      R bu = qx ? xb[f + 1] : xb[f + 2];
+      R su = qx ? dh[f] : dh[f + 1];
+      R sb = qx ? db[f] : db[f + 1];
       R hc = fi == 0 ? xh[f + 2] : xh[f + 1];
       R bc = fi == 0 ? xb[f + 2] : xb[f + 1];
-      eval_face<D, FLUX, FAST>(e, MX, sxs, hu, bu, su, sb, hc, bc, dt, fxh[f], fxb[f]);
+      eval_face<D, FLUX, FAST>(e, MX, qxs, hu, bu, su, sb, hc, bc, dt, fxh[f], fxb[f]);
     }
     // update the cells of row j
     const long ro = (long)(j + g.ngy) * rows;
@@ -717,9 +726,24 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
     }
   };
   const bool fastx = g.interp == 2 && i0 >= 2 && i0 + TX <= g.nx - 2;
+  // warp-uniform velocity signs select a sign-specialised interior row body
+  const unsigned am = __activemask();
+  const unsigned bx = __ballot_sync(am, px), by = __ballot_sync(am, py);
+  const int sg = (bx != 0 && bx != am) || (by != 0 && by != am)
+                     ? 0 : (bx == am ? (by == am ? 1 : 2) : (by == am ? 3 : 4));
+  using T0 = std::integral_constant<int, 0>;
   for (int j = j0; j < j1; ++j) {
-    if (fastx && (D == 1 || (j >= 1 && j <= g.ny - 3))) row(j, std::true_type{});
-    else row(j, std::false_type{});
+    if (fastx && (D == 1 || (j >= 1 && j <= g.ny - 3))) {
+      switch (sg) {
+        case 1: row(j, std::true_type{}, std::integral_constant<int, 1>{}); break;
+        case 2: row(j, std::true_type{}, std::integral_constant<int, 2>{}); break;
+        case 3: row(j, std::true_type{}, std::integral_constant<int, 3>{}); break;
+        case 4: row(j, std::true_type{}, std::integral_constant<int, 4>{}); break;
+        default: row(j, std::true_type{}, T0{}); break;
+      }
+    } else {
+      row(j, std::false_type{}, T0{});
+    }
   }
 }
 
