@@ -389,6 +389,20 @@ static void recon2(double* s, const double* qL, const double* qR, long n, double
 
 /* reconstruct! 1D2F (src/Solver/solver_reconstruction.jl:101-153) and
  * 2D2F (:475-620). */
+/* per-thread scratch sized for the current OpenMP team (threads may change
+ * between calls through kbo_set_threads) */
+static void ensure_scratch(kbo_t* o) {
+  int nt = 1;
+#ifdef _OPENMP
+  nt = omp_get_max_threads();
+#endif
+  if (nt > o->ntmp) {
+    free(o->tmp);
+    o->tmp = malloc(sizeof(double) * (long)nt * 16 * o->nvel);
+    o->ntmp = nt;
+  }
+}
+
 void kbo_reconstruct(kbo_t* o) {
   if (o->c.interp_order == 1) return;
   int nx = o->c.nx, ny = o->c.ny, NW = o->NW;
@@ -884,6 +898,7 @@ static void interior_face(kbo_t* o, long cl, long cr, int d, double len, double 
 /* evolve! 1D2F (src/Solver/solver_evolution.jl:64-89) + evolve_boundary!
  * (src/Solver/evolve_boundary.jl:4-47); 2D2F (:608-679) + (:52-178). */
 void kbo_evolve(kbo_t* o, double dt) {
+  ensure_scratch(o);
   int nx = o->c.nx, ny = o->c.ny;
   long nv = o->nvel;
   int i0 = o->c.ngx > 0 ? 1 : 2, i1 = o->c.ngx > 0 ? nx + 1 : nx;
@@ -1069,6 +1084,7 @@ static void copy_ctr(kbo_t* o, long dst, long src) { /* copy_ctr!, src/Struct/st
 /* update! 1D (src/Solver/solver_update.jl:61-93) + update_boundary!
  * (src/Solver/update_boundary.jl:6-61); 2D (:193-246) + (:172-306). */
 void kbo_update(kbo_t* o, double dt, double* residual) {
+  ensure_scratch(o);
   int nx = o->c.nx, ny = o->c.ny, NW = o->NW;
   long nv = o->nvel;
   int coll = o->c.collision;
