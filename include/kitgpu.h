@@ -187,6 +187,33 @@ int kb_get_tuning(kb_handle_t* h, int32_t* params, int32_t n);
  * their own work or CUDA events against it. */
 int kb_get_stream(kb_handle_t* h, void** stream);
 
+/* ------------------------------------------------------------------ batch
+ * Many independent 1D2F1V solves with uneven cell counts and velocity grids,
+ * advanced by one persistent kernel launch per step over a flattened ragged
+ * index, two steps captured as a CUDA graph.  Each instance is what the
+ * reference would run as its own solve! (src/Solver/solver_main.jl:12-76) with
+ * KFVS, BGK / Shakhov, fixed boundaries and van Leer slopes; a launch is the
+ * loop of that call over all instances.  Instance b has nx[b] cells (plus
+ * ngx[b] ghost layers per side) on [x0[b], x1[b]] and nu[b] <= 256 velocities;
+ * u_all / w_all concatenate the velocity tables.  States concatenate the
+ * instances: w, prim [cells][3], h, b [cells][nu of its instance]. */
+typedef struct kb_batch kb_batch_t;
+int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t* nx, const int32_t* ngx,
+                    const int32_t* nu, const double* x0, const double* x1, const double* umax,
+                    const double* mu_ref, const double* u_all, const double* w_all,
+                    kb_batch_t** out);
+int kb_batch_destroy(kb_batch_t* b);
+int kb_batch_upload(kb_batch_t* b, const double* w, const double* prim, const double* hdist,
+                    const double* bdist);
+int kb_batch_download(kb_batch_t* b, double* w, double* prim, double* hdist, double* bdist);
+/* Per-instance CFL time step (timestep, src/Solver/solver_main.jl:240-288). */
+int kb_batch_timestep(kb_batch_t* b, double cfl, double* dt_out);
+int kb_batch_set_dt(kb_batch_t* b, const double* dt);
+/* nsteps steps; an instance whose residual max falls below tol stops (its
+ * state is carried unchanged).  residual [n][4] and active [n] may be NULL. */
+int kb_batch_step(kb_batch_t* b, int32_t nsteps, double tol, double* residual, int32_t* active);
+int kb_batch_info(kb_batch_t* b, int64_t* elems, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

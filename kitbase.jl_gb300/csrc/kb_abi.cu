@@ -47,6 +47,8 @@ static int fail(int code, const std::string& msg) {
   return code;
 }
 
+void kb::set_error(const std::string& msg) { g_err = msg; }
+
 #define KB_CUDA(call)                                                                   \
   do {                                                                                  \
     cudaError_t e_ = (call);                                                            \

@@ -1,0 +1,726 @@
+// kb_batch.cu -- many independent 1D2F1V solves (uneven cell counts and
+// velocity grids) advanced by ONE persistent kernel launch per time step.
+//
+// Ragged layout: instance b owns cells [cell_off[b], cell_off[b] + nxt[b])
+// (ghosts included) and a velocity table at vel_off[b] of length nu[b]; its
+// distributions start at elem_off[b] in the flat h / b arrays and are
+// [cell][nu[b]] (velocity fastest).  A CTA takes instances from a work counter
+// (largest first) and runs the whole step of an instance:
+//   A  face moments fw (one thread per face looping over velocities, blocked
+//      compensated sums) and the old heat flux q (one thread per cell)
+//   C  cell parameters: w, prim, tau, residual terms (one thread per cell),
+//      block-reduced residual and the instance's convergence flag
+//   D  pointwise KFVS flux + BGK / Shakhov relaxation (one thread per
+//      velocity, marching the cells with a register window)
+// Covers the configuration of the batched shock-structure ensemble: KFVS,
+// BGK or Shakhov, fixed boundaries, van Leer, up to 256 velocities.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/kitgpu.h"
+#include "kb_device.cuh"
+#include "kb_kernels.cuh"
+
+namespace kb {
+
+struct BatchDev {
+  int n;                 // instances
+  const int* order;      // processing order (largest first)
+  const int* nx;         // physical cells
+  const int* ng;         // ghost layers
+  const int* nu;         // velocities
+  const long* cell_off;  // first cell (incl. ghosts)
+  const long* elem_off;  // first distribution element
+  const int* vel_off;    // velocity table offset
+  const double* dx;      // cell size
+  const double* dt;      // time step
+  const double* mu;      // reference viscosity
+  const double* u;       // velocity tables (FP64)
+  const double* wt;
+  const float* uf;       // FP32 copies
+  const float* wtf;
+  double* w;             // [cell][4] (3 used)
+  double* prim;          // [cell][4]
+  double* fw;            // [instance faces][4] scratch: face flux per instance (nx+1 each)
+  const long* face_off;
+  double* q;             // [cell] old heat flux
+  double* cp;            // [cell][16] cell coefficients (see k_batch_step)
+  double* residual;      // [n][4]
+  int* active;           // [n] 1 while not converged
+  int* counter;          // work counter
+  int* status;
+  double K, gamma, omega, Pr, tol;
+  int coll;
+};
+
+template <typename R>
+__device__ __forceinline__ R bvl(int rule, R qm, R q0, R qp, R epsd) {
+  R a = q0 - qm, b = qp - q0;
+  if (rule == 1) return (a * fabs(b) + b * fabs(a)) / (fabs(a) + fabs(b) + epsd);
+  return R(0);
+}
+
+// 1D slope rule: van Leer everywhere inside when ghosts exist, boundary cells
+// flat without ghosts (src/Solver/solver_reconstruction.jl:101-153).
+__device__ __forceinline__ int brule(int i, int nx, int ng) {
+  if (i < 0 || i >= nx) return 0;
+  if (ng == 0 && (i == 0 || i == nx - 1)) return 0;
+  return 1;
+}
+
+template <typename R>
+struct BSum;
+template <>
+struct BSum<float> {
+  float p;
+  DF d;
+  __device__ __forceinline__ void init() { p = 0.f; d.hi = d.lo = 0.f; }
+  __device__ __forceinline__ void add(float x) { p += x; }
+  __device__ __forceinline__ void flush() { df_add(d, p); p = 0.f; }
+  __device__ __forceinline__ double get() { flush(); return (double)d.hi + (double)d.lo; }
+};
+template <>
+struct BSum<double> {
+  double p;
+  __device__ __forceinline__ void init() { p = 0.0; }
+  __device__ __forceinline__ void add(double x) { p += x; }
+  __device__ __forceinline__ void flush() {}
+  __device__ __forceinline__ double get() { return p; }
+};
+
+template <typename R>
+__device__ __forceinline__ const R* btab(const BatchDev& B, int which);
+template <>
+__device__ __forceinline__ const double* btab<double>(const BatchDev& B, int which) {
+  return which == 0 ? B.u : B.wt;
+}
+template <>
+__device__ __forceinline__ const float* btab<float>(const BatchDev& B, int which) {
+  return which == 0 ? B.uf : B.wtf;
+}
+
+template <typename R, int BS>
+__global__ void __launch_bounds__(BS) k_batch_step(BatchDev B, const R* __restrict__ Hin,
+                                                    const R* __restrict__ Bin, R* __restrict__ Hout,
+                                                    R* __restrict__ Bout) {
+  __shared__ int s_b;
+  __shared__ double red[BS / 32][8];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (;;) {
+    if (tid == 0) s_b = atomicAdd(B.counter, 1);
+    __syncthreads();
+    const int slot = s_b;
+    __syncthreads();
+    if (slot >= B.n) return;
+    const int b = B.order[slot];
+    const int nx = B.nx[b], ng = B.ng[b], nu = B.nu[b];
+    const long c0 = B.cell_off[b], e0 = B.elem_off[b];
+    const int nxt = nx + 2 * ng;
+    const R* Hi = Hin + e0;
+    const R* Bi = Bin + e0;
+    R* Ho = Hout + e0;
+    R* Bo = Bout + e0;
+    if (!B.active[b]) {  // converged: carry the state over
+      for (long k = tid; k < (long)nxt * nu; k += BS) {
+        Ho[k] = Hi[k];
+        Bo[k] = Bi[k];
+      }
+      continue;
+    }
+    const R* U = btab<R>(B, 0) + B.vel_off[b];
+    const R* W = btab<R>(B, 1) + B.vel_off[b];
+    const double dx = B.dx[b], dt = B.dt[b];
+    const R epsd = R(1.e-7 * dx);
+    double* fw = B.fw + B.face_off[b] * 4;
+    // ---- A: face moments (faces 1 .. nx-1 bound the stepped cells) and q
+    const R T3 = R(dt), T4 = R(0.5 * dt * dt / dx);
+    for (int f = 1 + tid; f <= nx - 1; f += BS) {
+      BSum<R> s0, s1, s2;
+      s0.init();
+      s1.init();
+      s2.init();
+      const int iL = f - 1, iR = f;
+      const int rL = brule(iL, nx, ng), rR = brule(iR, nx, ng);
+      const R* hL = Hi + (long)(iL + ng) * nu;
+      const R* bL = Bi + (long)(iL + ng) * nu;
+      for (int v = 0; v < nu; ++v) {
+        R u = U[v];
+        bool pos = u >= R(0);
+        const R* hc = pos ? hL : hL + nu;
+        const R* bc = pos ? bL : bL + nu;
+        int r = pos ? rL : rR;
+        R h0 = hc[v], b0 = bc[v];
+        R sh = R(0), sb = R(0);
+        if (r == 1) {
+          sh = bvl<R>(1, hc[v - nu], h0, hc[v + nu], epsd);
+          sb = bvl<R>(1, bc[v - nu], b0, bc[v + nu], epsd);
+        }
+        R side = pos ? R(0.5) : R(-0.5);
+        R hf = h0 + side * sh, bf = b0 + side * sb;
+        R fh = T3 * u * hf - T4 * (u * u) * sh;
+        R fb = T3 * u * bf - T4 * (u * u) * sb;
+        R wf = W[v] * fh;
+        s0.add(wf);
+        s1.add(wf * u);
+        s2.add(wf * u * u + W[v] * fb);
+        if ((v & 7) == 7) {
+          s0.flush();
+          s1.flush();
+          s2.flush();
+        }
+      }
+      double* o = fw + (long)f * 4;
+      o[0] = s0.get();
+      o[1] = s1.get();
+      o[2] = 0.5 * s2.get();
+    }
+    if (B.coll == COLL_SHAKHOV) {
+      for (int i = 1 + tid; i <= nx - 2; i += BS) {
+        BSum<R> s;
+        s.init();
+        const R* hc = Hi + (long)(i + ng) * nu;
+        const R* bc = Bi + (long)(i + ng) * nu;
+        R Uc = R(B.prim[(c0 + i + ng) * 4 + 1]);
+        for (int v = 0; v < nu; ++v) {
+          R cu = U[v] - Uc;
+          s.add(W[v] * cu * (cu * cu * hc[v] + bc[v]));
+          if ((v & 7) == 7) s.flush();
+        }
+        B.q[c0 + i + ng] = 0.5 * s.get();
+      }
+    }
+    __syncthreads();
+    // ---- C: cell parameters of the stepped cells 1 .. nx-2 (fixed ends)
+    double rr[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 1 + tid; i <= nx - 2; i += BS) {
+      const long c = c0 + i + ng;
+      double* w = B.w + c * 4;
+      double* p = B.prim + c * 4;
+      const double* fL = fw + (long)i * 4;
+      const double* fR = fw + (long)(i + 1) * 4;
+      double wo[3] = {w[0], w[1], w[2]};
+      double lo = p[2], rho_o = p[0], Uo = p[1];
+      for (int k = 0; k < 3; ++k) w[k] += (fL[k] - fR[k]) / dx;
+      double pn[4];
+      conserve_prim(w, 3, B.gamma, pn);
+      p[0] = pn[0];
+      p[1] = pn[1];
+      p[2] = pn[2];
+      for (int k = 0; k < 3; ++k) {
+        double d = w[k] - wo[k];
+        rr[k] += d * d;
+        rr[3 + k] += fabs(w[k]);
+      }
+      double lam = pn[2];
+      double tau = vhs_time(pn[0], lam, B.mu[b], B.omega);
+      if (!(pn[0] > 0.0) || !(lam > 0.0) || !isfinite(pn[0]) || !isfinite(lam)) atomicOr(B.status, 1);
+      double* k = B.cp + c * 16;
+      k[0] = pn[0] * sqrt(lam / PI);  // new Maxwellian
+      k[1] = pn[1];
+      k[2] = lam;
+      k[3] = B.K / (2.0 * lam);
+      k[4] = dt / tau;
+      k[5] = 1.0 / (1.0 + dt / tau);
+      k[6] = rho_o * sqrt(lo / PI);  // old Maxwellian (Shakhov)
+      k[7] = Uo;
+      k[8] = lo;
+      k[9] = B.K / (2.0 * lo);
+      k[10] = B.coll == COLL_SHAKHOV ? 0.8 * (1.0 - B.Pr) * (lo * lo) / rho_o * B.q[c] : 0.0;
+    }
+    // residual (src/Solver/solver_update.jl:86-88; fixed ends add zero)
+    for (int k = 0; k < 6; ++k) {
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) rr[k] += __shfl_xor_sync(0xffffffffu, rr[k], m);
+    }
+    if (lane == 0)
+      for (int k = 0; k < 6; ++k) red[wid][k] = rr[k];
+    __syncthreads();
+    if (tid == 0) {
+      double t[6] = {0, 0, 0, 0, 0, 0};
+      for (int w8 = 0; w8 < BS / 32; ++w8)
+        for (int k = 0; k < 6; ++k) t[k] += red[w8][k];
+      double mx = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        // fixed ends contribute sqrt(0 * 2) / (0 + 1e-7) = 0 (update_boundary.jl:41-44)
+        double r = sqrt(t[k] * nx) / (t[3 + k] + 1.e-7);
+        B.residual[b * 4 + k] = r;
+        mx = fmax(mx, r);
+      }
+      if (mx < B.tol) B.active[b] = 0;
+    }
+    __syncthreads();
+    // ---- D: pointwise update, one thread per velocity marching the cells
+    for (int v = tid; v < nu; v += BS) {
+      const R u = U[v];
+      const bool pos = u >= R(0);
+      const R side = pos ? R(0.5) : R(-0.5);
+      auto at = [&](const R* q, int i) { return q[(long)(i + ng) * nu + v]; };
+      // fixed end cells keep their state
+      Ho[(long)ng * nu + v] = at(Hi, 0);
+      Bo[(long)ng * nu + v] = at(Bi, 0);
+      Ho[(long)(nx - 1 + ng) * nu + v] = at(Hi, nx - 1);
+      Bo[(long)(nx - 1 + ng) * nu + v] = at(Bi, nx - 1);
+      // window: cells i-1, i, i+1 around the upwind cell of face i (between i-1 and i)
+      auto face = [&](int f, R& fh, R& fb) {
+        int up = pos ? f - 1 : f;
+        int r = brule(up, nx, ng);
+        R h0 = at(Hi, up), b0 = at(Bi, up);
+        R sh = R(0), sb = R(0);
+        if (r == 1) {
+          sh = bvl<R>(1, at(Hi, up - 1), h0, at(Hi, up + 1), epsd);
+          sb = bvl<R>(1, at(Bi, up - 1), b0, at(Bi, up + 1), epsd);
+        }
+        R hf = h0 + side * sh, bf = b0 + side * sb;
+        fh = T3 * u * hf - T4 * (u * u) * sh;
+        fb = T3 * u * bf - T4 * (u * u) * sb;
+      };
+      R fhL, fbL;
+      face(1, fhL, fbL);
+      for (int i = 1; i <= nx - 2; ++i) {
+        R fhR, fbR;
+        face(i + 1, fhR, fbR);
+        const long c = c0 + i + ng;
+        const double* k = B.cp + c * 16;
+        R h0 = at(Hi, i), b0 = at(Bi, i);
+        R du = u - R(k[1]);
+        R M = R(k[0]) * mexp(-R(k[2]) * du * du);
+        R MH = M, MB = M * R(k[3]);
+        if (B.coll == COLL_SHAKHOV) {
+          R ou = u - R(k[7]);
+          R OH = R(k[6]) * mexp(-R(k[8]) * ou * ou);
+          R cq = R(k[10]) * ou;
+          R tl = R(2) * R(k[8]) * ou * ou + R(B.K);
+          MH += cq * (tl - R(5)) * OH;
+          MB += cq * (tl - R(3)) * OH * R(k[9]);
+        }
+        R dtau = R(k[4]);
+        R hn, bn;
+        if (sizeof(R) == 8) {
+          hn = (h0 + (fhL - fhR) / R(dx) + dtau * MH) / (R(1) + dtau);
+          bn = (b0 + (fbL - fbR) / R(dx) + dtau * MB) / (R(1) + dtau);
+        } else {
+          R idx = R(1.0 / dx), inv = R(k[5]);
+          hn = (h0 + (fhL - fhR) * idx + dtau * MH) * inv;
+          bn = (b0 + (fbL - fbR) * idx + dtau * MB) * inv;
+        }
+        Ho[(long)(i + ng) * nu + v] = hn;
+        Bo[(long)(i + ng) * nu + v] = bn;
+        fhL = fhR;
+        fbL = fbR;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_batch_timestep(BatchDev B, const double* umax, double cfl, double* dt_out) {
+  const int b = blockIdx.x;
+  __shared__ double red[256];
+  const int nx = B.nx[b], ng = B.ng[b];
+  double m = 0.0;
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+    const double* p = B.prim + (B.cell_off[b] + i + ng) * 4;
+    double sos = pow(0.5 * B.gamma / p[2], 0.5);
+    m = fmax(m, (fmax(umax[b], fabs(p[1])) + sos) / B.dx[b]);
+  }
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s >= 1; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) dt_out[b] = cfl / red[0];
+}
+
+template <typename R>
+__global__ void k_batch_convert(R* dst, const double* src, long n) {
+  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = (R)src[t];
+}
+template <typename R>
+__global__ void k_batch_back(double* dst, const R* src, long n) {
+  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = (double)src[t];
+}
+
+}  // namespace kb
+
+// ---------------------------------------------------------------- C ABI
+
+struct kb_batch {
+  kb::BatchDev d;
+  int prec = 0;
+  int n = 0;
+  long ncell = 0, nelem = 0, nface = 0, nvel = 0;
+  void* h[2] = {nullptr, nullptr};
+  void* bq[2] = {nullptr, nullptr};
+  int cur = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  std::vector<int> nx, ng, nu;
+  std::vector<long> cell_off, elem_off;
+  double* d_stage = nullptr;
+  double* d_umax = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_cur = -1;
+  int grid = 0;
+  int64_t launches = 0;
+};
+
+static int bfail(int code, const std::string& m) {
+  kb::set_error(m);
+  return code;
+}
+
+static int balloc(kb_batch* B, void** p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (cudaMalloc(p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return bfail(KB_ERR_NOMEM, "cudaMalloc failed (" + std::to_string(bytes) + " bytes)");
+  }
+  B->allocs.push_back(*p);
+  return KB_OK;
+}
+
+extern "C" int kb_batch_destroy(kb_batch_t* B) {
+  if (!B) return KB_OK;
+  if (B->stream) cudaStreamSynchronize(B->stream);
+  if (B->graph) cudaGraphExecDestroy(B->graph);
+  for (void* p : B->allocs) cudaFree(p);
+  if (B->stream) cudaStreamDestroy(B->stream);
+  delete B;
+  return KB_OK;
+}
+
+extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t* nx,
+                               const int32_t* ngx, const int32_t* nu, const double* x0,
+                               const double* x1, const double* umax, const double* mu_ref,
+                               const double* u_all, const double* w_all, kb_batch_t** out) {
+  if (!base || n <= 0 || !nx || !ngx || !nu || !x0 || !x1 || !umax || !mu_ref || !u_all ||
+      !w_all || !out)
+    return bfail(KB_ERR_ARG, "kb_batch_create: null argument or empty batch");
+  if (base->dim != 1) return bfail(KB_ERR_CONFIG, "batched solves are 1D2F1V");
+  if (base->flux != KB_FLUX_KFVS) return bfail(KB_ERR_CONFIG, "batched solves use KFVS");
+  if (base->bc[0] != KB_BC_FIX || base->bc[1] != KB_BC_FIX)
+    return bfail(KB_ERR_CONFIG, "batched solves use fixed boundaries");
+  if (base->interp_order != 2) return bfail(KB_ERR_CONFIG, "batched solves use van Leer slopes");
+  if (base->precision != KB_PREC_FP64 && base->precision != KB_PREC_FP32)
+    return bfail(KB_ERR_CONFIG, "unknown precision");
+  for (int b = 0; b < n; ++b) {
+    if (nx[b] < 3 || nu[b] < 1 || nu[b] > 256 || ngx[b] < 0 || ngx[b] > 2 || !(x1[b] > x0[b]))
+      return bfail(KB_ERR_CONFIG, "instance " + std::to_string(b) +
+                                      ": need nx >= 3, 1 <= nu <= 256, 0 <= ng <= 2, x1 > x0");
+  }
+  kb_batch* B = new kb_batch();
+  B->prec = base->precision;
+  B->n = n;
+  B->nx.assign(nx, nx + n);
+  B->ng.assign(ngx, ngx + n);
+  B->nu.assign(nu, nu + n);
+  std::vector<long> face_off(n), vel_off_l(n);
+  std::vector<int> vel_off(n);
+  std::vector<double> dx(n), dt(n, 0.0), mu(mu_ref, mu_ref + n);
+  B->cell_off.resize(n);
+  B->elem_off.resize(n);
+  long cells = 0, elems = 0, faces = 0, vels = 0;
+  for (int b = 0; b < n; ++b) {
+    B->cell_off[b] = cells;
+    B->elem_off[b] = elems;
+    face_off[b] = faces;
+    vel_off[b] = (int)vels;
+    long nxt = nx[b] + 2 * ngx[b];
+    cells += nxt;
+    elems += nxt * nu[b];
+    faces += nx[b] + 1;
+    vels += nu[b];
+    dx[b] = (x1[b] - x0[b]) / nx[b];
+  }
+  B->ncell = cells;
+  B->nelem = elems;
+  B->nface = faces;
+  B->nvel = vels;
+  // largest instances first
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+    return (long)nx[a] * nu[a] > (long)nx[c] * nu[c];
+  });
+  auto fail_out = [&](int rc) {
+    kb_batch_destroy(B);
+    return rc;
+  };
+  if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail_out(bfail(KB_ERR_CUDA, "cudaStreamCreate failed"));
+  void* p;
+  int rc;
+#define BALLOC(dst, T, count)                                              \
+  if ((rc = balloc(B, &p, sizeof(T) * (size_t)(count))) != KB_OK) return fail_out(rc); \
+  dst = (T*)p;
+  int *d_order, *d_nx, *d_ng, *d_nu, *d_vo, *d_active, *d_counter, *d_status;
+  long *d_co, *d_eo, *d_fo;
+  double *d_dx, *d_dt, *d_mu, *d_u, *d_w, *d_wv, *d_prim, *d_fw, *d_q, *d_cp, *d_res;
+  float *d_uf, *d_wf;
+  BALLOC(d_order, int, n);
+  BALLOC(d_nx, int, n);
+  BALLOC(d_ng, int, n);
+  BALLOC(d_nu, int, n);
+  BALLOC(d_vo, int, n);
+  BALLOC(d_active, int, n);
+  BALLOC(d_counter, int, 2);
+  BALLOC(d_status, int, 1);
+  BALLOC(d_co, long, n);
+  BALLOC(d_eo, long, n);
+  BALLOC(d_fo, long, n);
+  BALLOC(d_dx, double, n);
+  BALLOC(d_dt, double, n);
+  BALLOC(d_mu, double, n);
+  BALLOC(d_u, double, vels);
+  BALLOC(d_wv, double, vels);
+  BALLOC(d_uf, float, vels);
+  BALLOC(d_wf, float, vels);
+  BALLOC(d_w, double, cells * 4);
+  BALLOC(d_prim, double, cells * 4);
+  BALLOC(d_fw, double, faces * 4);
+  BALLOC(d_q, double, cells);
+  BALLOC(d_cp, double, cells * 16);
+  BALLOC(d_res, double, (size_t)n * 4);
+  BALLOC(B->d_umax, double, n);
+  size_t esz = B->prec == KB_PREC_FP64 ? 8 : 4;
+  for (int k = 0; k < 2; ++k) {
+    if ((rc = balloc(B, &B->h[k], esz * elems)) != KB_OK) return fail_out(rc);
+    if ((rc = balloc(B, &B->bq[k], esz * elems)) != KB_OK) return fail_out(rc);
+  }
+  BALLOC(B->d_stage, double, elems);
+#undef BALLOC
+  std::vector<float> uf(u_all, u_all + vels), wf(w_all, w_all + vels);
+  std::vector<int> ones(n, 1);
+  bool ok = true;
+  ok &= cudaMemcpy(d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_nx, nx, sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_ng, ngx, sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_nu, nu, sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_vo, vel_off.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_active, ones.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_co, B->cell_off.data(), sizeof(long) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_eo, B->elem_off.data(), sizeof(long) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_fo, face_off.data(), sizeof(long) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_dx, dx.data(), sizeof(double) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_dt, dt.data(), sizeof(double) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_mu, mu.data(), sizeof(double) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_u, u_all, sizeof(double) * vels, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_wv, w_all, sizeof(double) * vels, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_uf, uf.data(), sizeof(float) * vels, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_wf, wf.data(), sizeof(float) * vels, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(B->d_umax, umax, sizeof(double) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemset(d_status, 0, sizeof(int)) == cudaSuccess;
+  ok &= cudaMemset(d_q, 0, sizeof(double) * cells) == cudaSuccess;
+  ok &= cudaMemset(d_fw, 0, sizeof(double) * faces * 4) == cudaSuccess;
+  ok &= cudaMemset(d_res, 0, sizeof(double) * n * 4) == cudaSuccess;
+  if (!ok) return fail_out(bfail(KB_ERR_CUDA, "batch table upload failed"));
+  kb::BatchDev& d = B->d;
+  d.n = n;
+  d.order = d_order;
+  d.nx = d_nx;
+  d.ng = d_ng;
+  d.nu = d_nu;
+  d.cell_off = d_co;
+  d.elem_off = d_eo;
+  d.vel_off = d_vo;
+  d.dx = d_dx;
+  d.dt = d_dt;
+  d.mu = d_mu;
+  d.u = d_u;
+  d.wt = d_wv;
+  d.uf = d_uf;
+  d.wtf = d_wf;
+  d.w = d_w;
+  d.prim = d_prim;
+  d.fw = d_fw;
+  d.face_off = d_fo;
+  d.q = d_q;
+  d.cp = d_cp;
+  d.residual = d_res;
+  d.active = d_active;
+  d.counter = d_counter;
+  d.status = d_status;
+  d.K = base->K;
+  d.gamma = base->gamma;
+  d.omega = base->omega;
+  d.Pr = base->Pr;
+  d.tol = 0.0;
+  d.coll = base->collision;
+  int dev = 0, sms = 1, per = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (B->prec == KB_PREC_FP64)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb::k_batch_step<double, 256>, 256, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb::k_batch_step<float, 256>, 256, 0);
+  B->grid = std::min(n, std::max(1, sms * per));
+  *out = B;
+  return KB_OK;
+}
+
+extern "C" int kb_batch_upload(kb_batch_t* B, const double* w, const double* prim,
+                               const double* h, const double* bq) {
+  if (!B || !w || !prim || !h || !bq) return bfail(KB_ERR_ARG, "kb_batch_upload: null argument");
+  std::vector<double> w4(B->ncell * 4, 0.0), p4(B->ncell * 4, 0.0);
+  for (long c = 0; c < B->ncell; ++c)
+    for (int k = 0; k < 3; ++k) {
+      w4[c * 4 + k] = w[c * 3 + k];
+      p4[c * 4 + k] = prim[c * 3 + k];
+    }
+  if (cudaMemcpy(B->d.w, w4.data(), sizeof(double) * w4.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(B->d.prim, p4.data(), sizeof(double) * p4.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bfail(KB_ERR_CUDA, "kb_batch_upload: copy failed");
+  const long n = B->nelem;
+  const unsigned g = (unsigned)((n + 255) / 256);
+  for (int which = 0; which < 2; ++which) {
+    const double* src = which == 0 ? h : bq;
+    if (cudaMemcpy(B->d_stage, src, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+      return bfail(KB_ERR_CUDA, "kb_batch_upload: copy failed");
+    for (int k = 0; k < 2; ++k) {
+      void* dst = which == 0 ? B->h[k] : B->bq[k];
+      if (B->prec == KB_PREC_FP64)
+        kb::k_batch_convert<double><<<g, 256, 0, B->stream>>>((double*)dst, B->d_stage, n);
+      else
+        kb::k_batch_convert<float><<<g, 256, 0, B->stream>>>((float*)dst, B->d_stage, n);
+      B->launches++;
+    }
+    cudaStreamSynchronize(B->stream);
+  }
+  std::vector<int> ones(B->n, 1);
+  cudaMemcpy((void*)B->d.active, ones.data(), sizeof(int) * B->n, cudaMemcpyHostToDevice);
+  cudaMemset(B->d.status, 0, sizeof(int));
+  B->cur = 0;
+  if (cudaGetLastError() != cudaSuccess) return bfail(KB_ERR_CUDA, "kb_batch_upload failed");
+  return KB_OK;
+}
+
+extern "C" int kb_batch_download(kb_batch_t* B, double* w, double* prim, double* h, double* bq) {
+  if (!B) return bfail(KB_ERR_ARG, "kb_batch_download: null handle");
+  cudaStreamSynchronize(B->stream);
+  if (w || prim) {
+    std::vector<double> w4(B->ncell * 4), p4(B->ncell * 4);
+    cudaMemcpy(w4.data(), B->d.w, sizeof(double) * w4.size(), cudaMemcpyDeviceToHost);
+    cudaMemcpy(p4.data(), B->d.prim, sizeof(double) * p4.size(), cudaMemcpyDeviceToHost);
+    for (long c = 0; c < B->ncell; ++c)
+      for (int k = 0; k < 3; ++k) {
+        if (w) w[c * 3 + k] = w4[c * 4 + k];
+        if (prim) prim[c * 3 + k] = p4[c * 4 + k];
+      }
+  }
+  const long n = B->nelem;
+  const unsigned g = (unsigned)((n + 255) / 256);
+  for (int which = 0; which < 2; ++which) {
+    double* dst = which == 0 ? h : bq;
+    if (!dst) continue;
+    const void* src = which == 0 ? B->h[B->cur] : B->bq[B->cur];
+    if (B->prec == KB_PREC_FP64)
+      kb::k_batch_back<double><<<g, 256, 0, B->stream>>>(B->d_stage, (const double*)src, n);
+    else
+      kb::k_batch_back<float><<<g, 256, 0, B->stream>>>(B->d_stage, (const float*)src, n);
+    B->launches++;
+    cudaStreamSynchronize(B->stream);
+    cudaMemcpy(dst, B->d_stage, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  }
+  if (cudaGetLastError() != cudaSuccess) return bfail(KB_ERR_CUDA, "kb_batch_download failed");
+  return KB_OK;
+}
+
+extern "C" int kb_batch_timestep(kb_batch_t* B, double cfl, double* dt_out) {
+  if (!B) return bfail(KB_ERR_ARG, "kb_batch_timestep: null handle");
+  kb::k_batch_timestep<<<B->n, 256, 0, B->stream>>>(B->d, B->d_umax, cfl, (double*)B->d.dt);
+  B->launches++;
+  cudaStreamSynchronize(B->stream);
+  if (dt_out) cudaMemcpy(dt_out, B->d.dt, sizeof(double) * B->n, cudaMemcpyDeviceToHost);
+  if (cudaGetLastError() != cudaSuccess) return bfail(KB_ERR_CUDA, "kb_batch_timestep failed");
+  return KB_OK;
+}
+
+extern "C" int kb_batch_set_dt(kb_batch_t* B, const double* dt) {
+  if (!B || !dt) return bfail(KB_ERR_ARG, "kb_batch_set_dt: null argument");
+  if (cudaMemcpy((void*)B->d.dt, dt, sizeof(double) * B->n, cudaMemcpyHostToDevice) != cudaSuccess)
+    return bfail(KB_ERR_CUDA, "kb_batch_set_dt failed");
+  return KB_OK;
+}
+
+static void batch_launch(kb_batch* B, int cur) {
+  cudaMemsetAsync(B->d.counter, 0, sizeof(int), B->stream);
+  if (B->prec == KB_PREC_FP64)
+    kb::k_batch_step<double, 256><<<B->grid, 256, 0, B->stream>>>(
+        B->d, (const double*)B->h[cur], (const double*)B->bq[cur], (double*)B->h[cur ^ 1],
+        (double*)B->bq[cur ^ 1]);
+  else
+    kb::k_batch_step<float, 256><<<B->grid, 256, 0, B->stream>>>(
+        B->d, (const float*)B->h[cur], (const float*)B->bq[cur], (float*)B->h[cur ^ 1],
+        (float*)B->bq[cur ^ 1]);
+}
+
+// Two steps (ping and pong) captured once as a CUDA graph and replayed.
+static int batch_graph(kb_batch* B) {
+  if (B->graph && B->graph_cur == B->cur) return KB_OK;
+  if (B->graph) {
+    cudaGraphExecDestroy(B->graph);
+    B->graph = nullptr;
+  }
+  cudaGraph_t g;
+  if (cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return bfail(KB_ERR_CUDA, "graph capture failed to start");
+  batch_launch(B, B->cur);
+  batch_launch(B, B->cur ^ 1);
+  if (cudaStreamEndCapture(B->stream, &g) != cudaSuccess)
+    return bfail(KB_ERR_CUDA, "graph capture failed");
+  cudaError_t e = cudaGraphInstantiate(&B->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return bfail(KB_ERR_CUDA, "graph instantiation failed");
+  B->graph_cur = B->cur;
+  return KB_OK;
+}
+
+extern "C" int kb_batch_step(kb_batch_t* B, int32_t nsteps, double tol, double* residual,
+                             int32_t* active) {
+  if (!B) return bfail(KB_ERR_ARG, "kb_batch_step: null handle");
+  if (nsteps < 0) return bfail(KB_ERR_ARG, "kb_batch_step: nsteps must be >= 0");
+  if (B->d.tol != tol) {
+    B->d.tol = tol;
+    if (B->graph) {
+      cudaGraphExecDestroy(B->graph);
+      B->graph = nullptr;
+    }
+  }
+  int rc = batch_graph(B);
+  if (rc != KB_OK) return rc;
+  int pairs = nsteps / 2;
+  for (int k = 0; k < pairs; ++k) {
+    if (cudaGraphLaunch(B->graph, B->stream) != cudaSuccess)
+      return bfail(KB_ERR_CUDA, "graph launch failed");
+    B->launches += 2;
+  }
+  if (nsteps & 1) {
+    batch_launch(B, B->cur);
+    B->launches++;
+    B->cur ^= 1;
+  }
+  if (cudaStreamSynchronize(B->stream) != cudaSuccess)
+    return bfail(KB_ERR_CUDA, std::string("batch step failed: ") + cudaGetErrorString(cudaGetLastError()));
+  if (residual)
+    cudaMemcpy(residual, B->d.residual, sizeof(double) * 4 * B->n, cudaMemcpyDeviceToHost);
+  if (active) cudaMemcpy(active, B->d.active, sizeof(int) * B->n, cudaMemcpyDeviceToHost);
+  int st = 0;
+  cudaMemcpy(&st, B->d.status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (st) return bfail(KB_ERR_NUMERIC, "non-finite or non-positive density / lambda in a batched solve");
+  return KB_OK;
+}
+
+extern "C" int kb_batch_info(kb_batch_t* B, int64_t* elems, int64_t* launches) {
+  if (!B) return bfail(KB_ERR_ARG, "kb_batch_info: null handle");
+  if (elems) *elems = B->nelem;
+  if (launches) *launches = B->launches;
+  return KB_OK;
+}

@@ -2,15 +2,20 @@
 // DVM kernels (kb_kernels.cu).
 #pragma once
 
+#include <string>
+
 #include "kb_device.cuh"
 
 namespace kb {
 
-// Device buffers of one solve (owned by kb_handle, see kb_abi.cu).
+// Record the message returned by kb_last_error() for this host thread.
+void set_error(const std::string& msg);
+
 // Tunable launch shapes (kb_set_tuning); 0 selects the built-in default.
 enum { KB_TUNE_MARCH_TX = 0, KB_TUNE_MARCH_RY = 1, KB_TUNE_MARCH_BS = 2, KB_TUNE_MOM_TS = 3,
        TUNE_N = 4 };
 
+// Device buffers of one solve (owned by kb_handle, see kb_abi.cu).
 struct DevState {
   Geo g;
   int tune[TUNE_N];
