@@ -446,6 +446,80 @@ def run_ours(args):
     return 0
 
 
+def run_batch(args):
+    """Batched shock-structure ensemble: 512 instances, FP32 split, one
+    persistent launch per step (CUDA graph), against the plain FP64 GPU path
+    looped per instance."""
+    import torch
+    import kitgpu
+    from kitgpu import batch as KB
+    torch.cuda.set_device(0)
+    kitgpu.load()
+    sets = KB.solver_sets(KB.shock_ensemble(args.instances))
+    out = {"workload": "batched ensemble of %d 1D shock-structure solves (Mach U(1.2,8), cells "
+                       "U{50..400}, velocities U{48..200}), KFVS + Shakhov, Kn=1" % len(sets)}
+    for prec in ("fp32", "fp64"):
+        bt = KB.Batch(sets, prec)
+        bt.upload_initial()
+        bt.timestep()
+        bt.step(args.warmup)
+        cv = bt.cell_velocity_points()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bt.step(args.steps)
+        el = time.perf_counter() - t0
+        out[prec] = {"value": cv * args.steps / el, "unit": UNIT, "ms_per_step": 1e3 * el / args.steps}
+        if prec == "fp32":
+            bt.upload_initial()
+            bt.timestep()
+            t0 = time.perf_counter()
+            left = bt.run_to_steady(tol=1e-8, max_steps=args.max_steady, chunk=500)
+            out["fp32"]["steady"] = {"tol": 1e-8, "steps": bt.steps, "seconds": time.perf_counter() - t0,
+                                     "unconverged": left}
+        bt.close()
+    # plain FP64 GPU path, one handle per instance, looped
+    sample = sets[:: max(1, len(sets) // args.loop_sample)][: args.loop_sample]
+    hs = []
+    for KS in sample:
+        ctr, face = kitgpu.init_fvm(KS, "fp64")
+        hs.append((ctr.handle, kitgpu.timestep(KS, ctr, 0.0), KS.ps.nx * KS.vs.nu))
+    for h, dt, _ in hs:
+        h.step(dt, 2)
+    t0 = time.perf_counter()
+    for h, dt, _ in hs:
+        h.step(dt, args.loop_steps)
+    el = time.perf_counter() - t0
+    out["fp64_loop"] = {"value": sum(c for _, _, c in hs) * args.loop_steps / el, "unit": UNIT,
+                        "instances_sampled": len(hs)}
+    out["speedup_fp32_batch_vs_fp64_loop"] = out["fp32"]["value"] / out["fp64_loop"]["value"]
+    print(json.dumps({"metric": METRIC, "workload": "batch", "result": out}), flush=True)
+    return 0
+
+
+def run_serve(args):
+    """Served mixed stream (Poisson arrivals), FP32 split vs plain FP64."""
+    import torch
+    import kitgpu
+    from kitgpu import serve as S
+    torch.cuda.set_device(0)
+    kitgpu.load()
+    res = {}
+    for prec in ("fp32", "fp64"):
+        reqs = S.mixed_stream(rate=args.rate, duration=args.duration, seed=20261203,
+                              max_steps=args.max_steps, tol=1e-6)
+        srv = S.Server(precision=prec, hbm_budget=args.hbm_gb << 30, max_slots=args.slots,
+                       chunk=args.chunk)
+        res[prec] = srv.run(reqs)
+    res["throughput_ratio_fp32_vs_fp64"] = res["fp32"]["throughput"] / res["fp64"]["throughput"]
+    print(json.dumps({"metric": METRIC + " and p50/p99 latency", "workload": "serve",
+                      "stream": {"rate_per_s": args.rate, "duration_s": args.duration,
+                                 "mix": "60% 1D Sod (cells 64..2048, velocities 32..256), 40% 2D "
+                                        "cavity (16^2..128^2 cells, 16^2..48^2 velocities, "
+                                        "Kn 1e-4..1)", "max_steps": args.max_steps, "tol": 1e-6},
+                      "result": res}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -458,11 +532,26 @@ def main():
     ap.add_argument("--no-error", action="store_true")
     ap.add_argument("--err-steps", type=int, default=40)
     ap.add_argument("--retune", action="store_true", help="ignore the autotuner cache")
+    ap.add_argument("--workload", choices=("quadrant", "batch", "serve"), default="quadrant")
+    ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--max-steady", type=int, default=40000)
+    ap.add_argument("--loop-sample", type=int, default=64)
+    ap.add_argument("--loop-steps", type=int, default=20)
+    ap.add_argument("--rate", type=float, default=50.0)
+    ap.add_argument("--duration", type=float, default=4.0)
+    ap.add_argument("--max-steps", type=int, default=200)
+    ap.add_argument("--slots", type=int, default=64)
+    ap.add_argument("--chunk", type=int, default=20)
+    ap.add_argument("--hbm-gb", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 

@@ -140,6 +140,15 @@ int kb_update(kb_handle_t* h, double dt, double* residual);
  * Replaces the body of the solve! loop (src/Solver/solver_main.jl:32-72). */
 int kb_step(kb_handle_t* h, double dt, int32_t nsteps, double* residual);
 
+/* Asynchronous form of kb_step for serving many solves at once: enqueue
+ * nsteps steps on the handle's stream and return immediately; the residual of
+ * the last step is copied to pinned host memory behind the steps.  kb_query
+ * sets *ready = 1 once they finished (then fills residual, dim+2 doubles, may
+ * be NULL) and 0 while they run.  No reference counterpart: the reference's
+ * solve! blocks until maxTime. */
+int kb_step_async(kb_handle_t* h, double dt, int32_t nsteps);
+int kb_query(kb_handle_t* h, double* residual, int32_t* ready);
+
 /* Face fluxes of the last kb_evolve, materialised for inspection: fw in the
  * global frame [nface][dim+2], fh, fb [nface][nu*nv].  x faces first
  * ((nx+1)*ny, i fastest), then y faces (nx*(ny+1)).  Faces that the

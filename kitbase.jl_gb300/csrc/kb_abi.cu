@@ -33,6 +33,10 @@ struct kb_handle {
   long stage_elems = 0;
   double* d_scalar = nullptr; // [8] scratch scalars
   bool evolved = false;
+  // asynchronous stepping (kb_step_async / kb_query)
+  double* h_res = nullptr;    // pinned host copy of residual[4] + status
+  cudaEvent_t ev_done = nullptr;
+  bool pending = false;
   // per-stage kernel timing (kb_set_timing): CUDA events on the handle stream
   bool timing = false;
   std::vector<cudaEvent_t> events;
@@ -280,6 +284,8 @@ int kb_destroy(kb_handle_t* h) {
   if (!h) return KB_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
+  if (h->ev_done) cudaEventDestroy(h->ev_done);
+  if (h->h_res) cudaFreeHost(h->h_res);
   for (void* p : h->allocs) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -483,6 +489,52 @@ int kb_step(kb_handle_t* h, double dt, int32_t nsteps, double* residual) {
   }
   h->evolved = false;
   return read_residual(h, residual);
+}
+
+int kb_step_async(kb_handle_t* h, double dt, int32_t nsteps) {
+  if (!h) return fail(KB_ERR_ARG, "kb_step_async: null handle");
+  if (!(dt > 0.0)) return fail(KB_ERR_ARG, "kb_step_async: dt must be positive");
+  if (nsteps < 0) return fail(KB_ERR_ARG, "kb_step_async: nsteps must be >= 0");
+  if (!h->h_res) {
+    KB_CUDA(cudaMallocHost((void**)&h->h_res, sizeof(double) * 5));
+    KB_CUDA(cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming));
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    int n = kb::launch_reconstruct(h->s, h->stream);
+    n += kb::launch_evolve(h->s, dt, h->stream);
+    n += kb::launch_update(h->s, dt, h->stream);
+    KB_TRY(check_launch(h, n));
+  }
+  KB_CUDA(cudaMemcpyAsync(h->h_res, h->s.residual, sizeof(double) * 4, cudaMemcpyDeviceToHost,
+                          h->stream));
+  KB_CUDA(cudaMemcpyAsync(h->h_res + 4, h->s.status, sizeof(int), cudaMemcpyDeviceToHost,
+                          h->stream));
+  KB_CUDA(cudaEventRecord(h->ev_done, h->stream));
+  h->pending = true;
+  h->evolved = false;
+  return KB_OK;
+}
+
+int kb_query(kb_handle_t* h, double* residual, int32_t* ready) {
+  if (!h || !ready) return fail(KB_ERR_ARG, "kb_query: null argument");
+  if (!h->pending) {
+    *ready = 1;
+    return KB_OK;
+  }
+  cudaError_t e = cudaEventQuery(h->ev_done);
+  if (e == cudaErrorNotReady) {
+    *ready = 0;
+    return KB_OK;
+  }
+  if (e != cudaSuccess) return fail(KB_ERR_CUDA, std::string("kb_query: ") + cudaGetErrorString(e));
+  *ready = 1;
+  h->pending = false;
+  if (residual)
+    for (int k = 0; k < h->s.g.NW; ++k) residual[k] = h->h_res[k];
+  int st = 0;
+  std::memcpy(&st, h->h_res + 4, sizeof(int));
+  if (st) return fail(KB_ERR_NUMERIC, "non-finite or non-positive density / lambda after a step");
+  return KB_OK;
 }
 
 int kb_set_timing(kb_handle_t* h, int enable) {

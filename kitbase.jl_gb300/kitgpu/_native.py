@@ -74,6 +74,8 @@ SIGNATURES = {
     "kb_get_timing": [_H, _D, ctypes.POINTER(ctypes.c_int64)],
     "kb_get_stream": [_H, ctypes.POINTER(ctypes.c_void_p)],
     "kb_set_tuning": [_H, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32],
+    "kb_step_async": [_H, ctypes.c_double, ctypes.c_int32],
+    "kb_query": [_H, _D, ctypes.POINTER(ctypes.c_int32)],
     "kb_get_tuning": [_H, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32],
 }
 STAGES = ("reconstruct", "face_param", "moments", "wall", "cell_param", "update", "finish")

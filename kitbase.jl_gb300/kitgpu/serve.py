@@ -1,0 +1,189 @@
+"""Continuous-batching service for a stream of DVM solves.
+
+Requests arrive over time (Poisson); each admitted request owns a libkitgpu
+handle with its own CUDA stream, so the steps of all resident requests run
+concurrently on the GPU.  The loop admits queued requests whenever a slot and
+the HBM budget allow, enqueues a chunk of steps for every resident request
+(kb_step_async), polls completions (kb_query) and retires a request when its
+residual (reference definition, src/Solver/solver_update.jl:86-88) falls below
+the tolerance or it reaches its step limit; its final state is downloaded and
+its memory returned to the budget before the next admission.
+
+The mixed stream: 60 % 1D Sod tubes (cells log-uniform in [64, 2048],
+velocities in [32, 256]) and 40 % 2D lid-driven cavities (cells log-uniform
+in [16^2, 128^2], velocity grids in [16^2, 48^2], Kn log-uniform in
+[1e-4, 1]).
+"""
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .setup import solver_set
+from .solver import Handle, initial_state, kb_config, wall_states
+
+
+def sod_request(nx, nu, Kn=1e-3):
+    return dict(matter="gas", case="sod", space="1d2f1v", flux="kfvs", collision="shakhov",
+                nSpecies=1, interpOrder=2, limiter="vanleer", boundary="fix", cfl=0.5,
+                maxTime=1e9, x0=0.0, x1=1.0, nx=int(nx), nxg=0, umin=-5.0, umax=5.0,
+                nu=int(nu), vMeshType="newton", knudsen=Kn, mach=0.0, prandtl=2.0 / 3.0,
+                inK=2.0, omega=0.81, alphaRef=1.0, omegaRef=0.5)
+
+
+def cavity_request(n, nv, Kn):
+    return dict(matter="gas", case="cavity", space="2d2f2v", flux="kcu", collision="shakhov",
+                nSpecies=1, interpOrder=2, limiter="vanleer", boundary="maxwell", cfl=0.8,
+                maxTime=1e9, x0=0.0, x1=1.0, nx=int(n), nxg=0, y0=0.0, y1=1.0, ny=int(n), nyg=0,
+                umin=-5.0, umax=5.0, nu=int(nv), vmin=-5.0, vmax=5.0, nv=int(nv),
+                vMeshType="newton", knudsen=float(Kn), mach=0.0, prandtl=2.0 / 3.0, inK=1.0,
+                omega=0.72, alphaRef=1.0, omegaRef=0.5, uLid=0.15, vLid=0.0, tLid=1.0)
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float
+    config: dict
+    max_steps: int
+    tol: float
+    # filled by the server
+    admitted: float = None
+    finished: float = None
+    steps: int = 0
+    residual: np.ndarray = None
+    result: dict = None
+    cv_per_step: int = 0
+    bytes: int = 0
+
+    @property
+    def latency(self):
+        return None if self.finished is None else self.finished - self.arrival
+
+
+def mixed_stream(rate, duration, seed=20261203, max_steps=200, tol=1e-6, frac_1d=0.6,
+                 scale=1.0):
+    """Poisson arrivals at `rate` per second over `duration` seconds.  `scale`
+    shrinks the size ranges (tests use small requests)."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        if rng.uniform() < frac_1d:
+            nx = int(round(math.exp(rng.uniform(math.log(64), math.log(2048))) * scale))
+            nu = int(rng.integers(32, 257) * min(1.0, scale * 4))
+            cfg = sod_request(max(nx, 8), max(nu, 16))
+        else:
+            n = int(round(math.exp(rng.uniform(math.log(16), math.log(128))) * scale))
+            nv = int(rng.integers(16, 49))
+            Kn = math.exp(rng.uniform(math.log(1e-4), math.log(1.0)))
+            cfg = cavity_request(max(n, 4), nv, Kn)
+        out.append(Request(len(out), t, cfg, max_steps, tol))
+    return out
+
+
+def estimate_bytes(cfg, precision):
+    """Device bytes of a handle for `cfg` (distributions x2 buffers dominate)."""
+    d = int(cfg["space"][0])
+    ncell = (cfg["nx"] + 2 * cfg.get("nxg", 0)) * ((cfg["ny"] + 2 * cfg.get("nyg", 0)) if d == 2 else 1)
+    nvel = cfg["nu"] * (cfg["nv"] if d == 2 else 1)
+    esz = 4 if precision == "fp32" else 8
+    nface = (cfg["nx"] + 1) * (cfg.get("ny", 1) if d == 2 else 1) * (2 if d == 2 else 1)
+    return 4 * ncell * ((nvel + 3) // 4 * 4) * esz + ncell * 1024 + nface * 512 + (1 << 20)
+
+
+@dataclass
+class Server:
+    precision: str = "fp32"
+    hbm_budget: int = 64 << 30
+    max_slots: int = 64
+    chunk: int = 20
+    done: list = field(default_factory=list)
+
+    def run(self, requests, time_scale=1.0, keep_results=False, on_retire=None):
+        """Serve `requests` (sorted by arrival).  Arrival times are honoured in
+        wall time divided by time_scale.  Returns summary metrics."""
+        pending = sorted(requests, key=lambda r: r.arrival)
+        queue, active = [], []
+        used = 0
+        t0 = time.perf_counter()
+        cv_total = 0
+        i = 0
+        while i < len(pending) or queue or active:
+            now = (time.perf_counter() - t0) * time_scale
+            while i < len(pending) and pending[i].arrival <= now:
+                queue.append(pending[i])
+                i += 1
+            # admission: FIFO while a slot and the HBM budget allow
+            while queue and len(active) < self.max_slots:
+                r = queue[0]
+                need = estimate_bytes(r.config, self.precision)
+                if used + need > self.hbm_budget and active:
+                    break
+                queue.pop(0)
+                KS = solver_set(r.config)
+                vs = KS.vs
+                if KS.dim == 1:
+                    h = Handle(kb_config(KS, self.precision), vs.u, None, vs.weights)
+                else:
+                    h = Handle(kb_config(KS, self.precision), vs.flat(vs.u), vs.flat(vs.v),
+                               vs.flat(vs.weights))
+                w, p, hd, bd = initial_state(KS)
+                h.upload(w, p, hd, bd)
+                for side, prim in enumerate(wall_states(KS)):
+                    if KS.set.boundary[side] == "maxwell":
+                        h.set_wall(side, prim)
+                r.dt = h.timestep(KS.set.cfl, 0.0, KS.set.maxTime)
+                r.handle = h
+                r.bytes = need
+                r.cv_per_step = h.cfg.nx * (h.cfg.ny if h.dim == 2 else 1) * h.nvel
+                r.admitted = (time.perf_counter() - t0) * time_scale
+                used += need
+                active.append(r)
+                r.inflight = 0
+            # enqueue a chunk for every idle resident request
+            for r in active:
+                if r.inflight == 0:
+                    n = min(self.chunk, r.max_steps - r.steps)
+                    r.handle.step_async(r.dt, n)
+                    r.inflight = n
+            # poll completions
+            still = []
+            for r in active:
+                ready, res = r.handle.query()
+                if not ready:
+                    still.append(r)
+                    continue
+                r.steps += r.inflight
+                cv_total += r.inflight * r.cv_per_step
+                r.inflight = 0
+                r.residual = res
+                if r.steps >= r.max_steps or float(np.max(res)) < r.tol:
+                    if keep_results:
+                        r.result = r.handle.download(("w", "prim"))
+                    r.finished = (time.perf_counter() - t0) * time_scale
+                    r.handle.close()
+                    r.handle = None
+                    used -= r.bytes
+                    self.done.append(r)
+                    if on_retire:
+                        on_retire(r)
+                else:
+                    still.append(r)
+            active = still
+            if not active and not queue and i < len(pending):
+                # idle until the next arrival
+                wait = (pending[i].arrival - now) / time_scale
+                if wait > 0:
+                    time.sleep(min(wait, 0.01))
+        wall = time.perf_counter() - t0
+        lat = np.array([r.latency for r in self.done if r.latency is not None]) / time_scale
+        return dict(requests=len(self.done), wall_s=wall, cv_updates=cv_total,
+                    throughput=cv_total / wall if wall > 0 else 0.0,
+                    p50_s=float(np.percentile(lat, 50)) if len(lat) else None,
+                    p99_s=float(np.percentile(lat, 99)) if len(lat) else None,
+                    precision=self.precision, max_slots=self.max_slots,
+                    hbm_budget=self.hbm_budget)

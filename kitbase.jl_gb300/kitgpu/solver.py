@@ -130,6 +130,16 @@ class Handle:
         self.call("kb_step", float(dt), int(n), N.ptr(r))
         return r[: self.nw]
 
+    def step_async(self, dt, n=1):
+        self.call("kb_step_async", float(dt), int(n))
+
+    def query(self):
+        """(ready, residual) of the last step_async."""
+        r = np.zeros(4)
+        ready = ctypes.c_int32()
+        self.call("kb_query", N.ptr(r), ctypes.byref(ready))
+        return bool(ready.value), r[: self.nw]
+
     def faces(self, dt):
         fw = np.zeros((self.nface, self.nw))
         fh = np.zeros((self.nface, self.nvel))
