@@ -559,18 +559,15 @@ int kb_get_timing(kb_handle_t* h, double* ms, int64_t* count) {
 int kb_set_tuning(kb_handle_t* h, const int32_t* params, int32_t n) {
   if (!h || (!params && n > 0)) return fail(KB_ERR_ARG, "kb_set_tuning: null argument");
   if (n < 0 || n > kb::TUNE_N) return fail(KB_ERR_ARG, "kb_set_tuning: bad parameter count");
-  static const int allowed_tx[] = {0, 2, 4, 8}, allowed_bs[] = {0, 64, 128, 256};
   for (int k = 0; k < n; ++k) {
     int p = params[k];
     bool ok = true;
-    if (k == kb::KB_TUNE_MARCH_TX) ok = p == 0 || p == 2 || p == 4 || p == 8;
+    if (k == kb::KB_TUNE_MARCH_TX) ok = p == 0 || p == 2 || p == 4;
     if (k == kb::KB_TUNE_MARCH_RY) ok = p >= 0 && p <= 4096;
-    if (k == kb::KB_TUNE_MARCH_BS) ok = p == 0 || p == 64 || p == 128 || p == 256;
+    if (k == kb::KB_TUNE_MARCH_BS) ok = p == 0 || p == 64 || p == 128;
     if (k == kb::KB_TUNE_MOM_TS) ok = p == 0 || p == 2 || p == 4;
     if (!ok) return fail(KB_ERR_ARG, "kb_set_tuning: value out of range for parameter " + std::to_string(k));
   }
-  (void)allowed_tx;
-  (void)allowed_bs;
   for (int k = 0; k < n; ++k) h->s.tune[k] = params[k];
   return KB_OK;
 }

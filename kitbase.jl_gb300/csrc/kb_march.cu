@@ -1,842 +1,40 @@
-// kb_march.cu -- the two HBM passes of one DVM time step.
-//
-// Pass A (k_mom): fw of every interior face and the old heat flux q of every
-// cell.  A warp owns a line segment of TS faces (along x or y) and loops over
-// ALL velocities, lanes striding by 32; the cells of the segment stencil are
-// held in a register window, so each cell value is loaded once per segment
-// and each van Leer slope is formed once.  Per-lane partial sums are
-// compensated (FP32 blocks flushed into double-float accumulators on the FP32
-// path) and combined once per face by a fixed shuffle tree, so fw is
-// deterministic and each face has exactly one writer.
-//
-// Pass B (k_march): the pointwise update of h and b.  A thread owns one
-// velocity; a CTA owns a strip of TX columns, a chunk of rows and a chunk of
-// velocities and marches up the rows with a four-row register window.  Every
-// x-face and y-face flux is evaluated once per velocity and added to both
-// neighbouring cells, so h and b are read once (plus a 4-cell x halo per row)
-// and written once.
-#include <cuda_runtime.h>
-
-#include <type_traits>
-
+// kb_march.cu -- dispatch of the two HBM passes to the per-precision /
+// per-flux instantiations (kb_march_f32_*.cu, kb_march_f64_*.cu).
 #include "kb_kernels.cuh"
-#include "kb_flux.cuh"
 
 namespace kb {
 
-// van Leer slope times dx, from raw differences: dx * vanleer(a/dx, b/dx)
-// = (a|b| + b|a|) / (|a| + |b| + 1e-7 dx) (src/Reconstruction/recon_limiter.jl:17-19);
-// rules 2 / 3 are the one-sided reconstruct2! differences.
-__device__ __forceinline__ float vl_diff(int rule, float qm, float q0, float qp, float epsd) {
-  float a = q0 - qm, b = qp - q0;
-  if (rule == 1) return __fdividef(a * fabsf(b) + b * fabsf(a), fabsf(a) + fabsf(b) + epsd);
-  if (rule == 2) return b;
-  if (rule == 3) return a;
-  return 0.f;
-}
-__device__ __forceinline__ double vl_diff(int rule, double qm, double q0, double qp, double epsd) {
-  double a = q0 - qm, b = qp - q0;
-  if (rule == 1) return (a * fabs(b) + b * fabs(a)) / (fabs(a) + fabs(b) + epsd);
-  if (rule == 2) return b;
-  if (rule == 3) return a;
-  return 0.0;
-}
-
-// 2^x on the MUFU unit (flushes results below 2^-126 to zero).
-__device__ __forceinline__ float ex2(float x) {
-  float y;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
-// Rule-dispatching slope; FAST = interior cell (van Leer only).
-template <bool FAST, typename R>
-__device__ __forceinline__ R slope(int rule, R qm, R q0, R qp, R epsd) {
-  if (FAST) return vl_diff(1, qm, q0, qp, epsd);
-  return vl_diff(rule, qm, q0, qp, epsd);
-}
-
-template <typename R>
-__device__ __forceinline__ R ldq(const R* __restrict__ q, long idx, bool ok) {
-  return ok ? __ldg(q + idx) : R(0);
-}
-
-// Blocked compensated accumulator: plain partial sums, flushed into a
-// double-float (TwoSum) accumulator; FP64 path sums in double directly.
-template <typename R>
-struct BAcc;
-template <>
-struct BAcc<float> {
-  float p;
-  DF d;
-  __device__ __forceinline__ void init() { p = 0.f; d.hi = 0.f; d.lo = 0.f; }
-  __device__ __forceinline__ void add(float x) { p += x; }
-  __device__ __forceinline__ void flush() { df_add(d, p); p = 0.f; }
-  __device__ __forceinline__ double total() { flush(); return df_warp_sum(d); }
-};
-template <>
-struct BAcc<double> {
-  double p;
-  __device__ __forceinline__ void init() { p = 0.0; }
-  __device__ __forceinline__ void add(double x) { p += x; }
-  __device__ __forceinline__ void flush() {}
-  __device__ __forceinline__ double total() { return warp_sum(p); }
-};
-
-// ------------------------------------------------------------------ pass A
-
-// DIR 0: x faces, segments along x in each row; DIR 1: y faces, segments
-// along y in each column.  Face f of a segment sits between cells p-1 and p
-// along the line with p = p0 + f; cells p0-2 .. p0+TS+1 form the window.
-template <typename R, int D, int FLUX, int TS, bool SHAK, int DIR>
-__global__ void __launch_bounds__(128) k_mom(DevState s) {
-  const Geo& g = s.g;
-  const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int n = DIR == 0 ? g.nx : g.ny;          // cells along the line
-  const int ng = DIR == 0 ? g.ngx : g.ngy;
-  const int nlines = DIR == 0 ? g.ny : g.nx;
-  const int nseg = (n + TS - 1) / TS;
-  if (gw >= nseg * nlines) return;
-  const int line = gw / nseg, sg = gw - line * nseg;
-  const int p0 = sg * TS;
-  const int ncell = min(TS, n - p0);
-  const int nf = ncell + (sg == nseg - 1 ? 1 : 0);  // faces p0 .. p0+nf-1
-  const long vs = g.vstride;
-  const R* __restrict__ H = (const R*)s.h[s.cur];
-  const R* __restrict__ Bq = (const R*)s.b[s.cur];
-  const R* __restrict__ U = vtab<R>(s, 0);
-  const R* __restrict__ V = vtab<R>(s, 1);
-  const R* __restrict__ W = vtab<R>(s, 2);
-  const double dd = DIR == 0 ? g.dx : g.dy;
-  const R epsd = R(1.e-7 * dd);
-
-  long base[TS + 4];
-  bool ex[TS + 4];
-  int rule[TS + 4];
-#pragma unroll
-  for (int w = 0; w < TS + 4; ++w) {
-    int p = p0 - 2 + w;
-    ex[w] = p >= -ng && p < n + ng;
-    int c = DIR == 0 ? cell_index(g, p, line) : cell_index(g, line, p);
-    base[w] = ex[w] ? (long)c * vs : 0;
-    rule[w] = slope_rule(g, DIR, p);
-  }
-  int fidx[TS + 1];
-  bool act[TS + 1];
-  R t3[TS + 1], t4[TS + 1];
-#pragma unroll
-  for (int f = 0; f < TS + 1; ++f) {
-    int p = p0 + f;
-    fidx[f] = DIR == 0 ? line * (g.nx + 1) + p : s.nface_x + p * g.nx + line;
-    act[f] = f < nf && s.kind[fidx[f]] == 1;
-    t3[f] = R(0);
-    t4[f] = R(0);
-    if (act[f]) {
-      const FaceParam& P = s.fp[fidx[f]];
-      t3[f] = R(P.tr[0]);
-      t4[f] = R(P.tr[1] / dd);
-    }
-  }
-  R oU[TS], oV[TS];
-  if (SHAK) {
-#pragma unroll
-    for (int c = 0; c < TS; ++c) {
-      int cc = base[c + 2] / vs;
-      oU[c] = R(s.prim[(long)cc * 4 + 1]);
-      oV[c] = R(D == 2 ? s.prim[(long)cc * 4 + 2] : 0.0);
-    }
-  }
-  BAcc<R> acc[TS + 1][4];
-  BAcc<R> qa[SHAK ? TS : 1][2];
-#pragma unroll
-  for (int f = 0; f < TS + 1; ++f)
-#pragma unroll
-    for (int k = 0; k < 4; ++k) acc[f][k].init();
-#pragma unroll
-  for (int c = 0; c < (SHAK ? TS : 1); ++c) {
-    qa[c][0].init();
-    qa[c][1].init();
-  }
-
-  auto run = [&](auto fast_tag) {
-  constexpr bool FAST = decltype(fast_tag)::value;
-  int it = 0;
-  for (int v0 = 0; v0 < g.nvel; v0 += 32, ++it) {
-    const int v = v0 + lane;
-    const bool ok = v < g.nvel;
-    R u = ok ? U[v] : R(0);
-    R vv = (ok && D == 2) ? V[v] : R(0);
-    R om = ok ? W[v] : R(0);
-    R un = DIR == 0 ? u : vv;
-    R ut = DIR == 0 ? vv : -u;
-    R hx[TS + 4], bx[TS + 4];
-#pragma unroll
-    for (int w = 0; w < TS + 4; ++w) {
-      hx[w] = ldq(H, base[w] + v, (FAST || ex[w]) && ok);
-      bx[w] = ldq(Bq, base[w] + v, (FAST || ex[w]) && ok);
-    }
-    R dh[TS + 2], db[TS + 2];  // slopes of cells w = 1 .. TS+2
-#pragma unroll
-    for (int w = 1; w <= TS + 2; ++w) {
-      dh[w - 1] = slope<FAST>(rule[w], hx[w - 1], hx[w], hx[w + 1], epsd);
-      db[w - 1] = slope<FAST>(rule[w], bx[w - 1], bx[w], bx[w + 1], epsd);
-    }
-    const bool pos = un >= R(0);
-    const R c2 = un * un + ut * ut;
-    const R un2 = un * un;
-#pragma unroll
-    for (int f = 0; f < TS + 1; ++f) {
-      if (FAST ? f == TS : !act[f]) continue;
-      R hu = pos ? hx[f + 1] : hx[f + 2];
-      R bu = pos ? bx[f + 1] : bx[f + 2];
-      R su = pos ? dh[f] : dh[f + 1];
-      R sb = pos ? db[f] : db[f + 1];
-      R hf = hu + (pos ? R(0.5) : R(-0.5)) * su;
-      R bf = bu + (pos ? R(0.5) : R(-0.5)) * sb;
-      R Th = t3[f] * un * hf - t4[f] * un2 * su;
-      R Tb = t3[f] * un * bf - t4[f] * un2 * sb;
-      R wT = om * Th;
-      acc[f][0].add(wT);
-      acc[f][1].add(wT * un);
-      if (D == 2) acc[f][2].add(wT * ut);
-      acc[f][3].add(wT * c2 + om * Tb);
-    }
-    if (SHAK) {
-#pragma unroll
-      for (int c = 0; c < TS; ++c) {
-        R cu = u - oU[c];
-        R cv = vv - oV[c];
-        R c2o = cu * cu + cv * cv;
-        R hc = hx[c + 2], bc = bx[c + 2];
-        qa[c][0].add(om * cu * c2o * hc + om * cu * bc);
-        if (D == 2) qa[c][1].add(om * cv * c2o * hc + om * cv * bc);
-      }
-    }
-    if ((it & 3) == 3) {
-#pragma unroll
-      for (int f = 0; f < TS + 1; ++f)
-#pragma unroll
-        for (int k = 0; k < 4; ++k) acc[f][k].flush();
-#pragma unroll
-      for (int c = 0; c < (SHAK ? TS : 1); ++c) {
-        qa[c][0].flush();
-        qa[c][1].flush();
-      }
-    }
-  }
-  };
-  bool fast = g.interp == 2 && p0 >= 2 && p0 + TS <= n - 2 && nf == TS;
-#pragma unroll
-  for (int f = 0; f < TS; ++f) fast = fast && act[f];
-  if (fast) run(std::true_type{});
-  else run(std::false_type{});
-#pragma unroll
-  for (int f = 0; f < TS + 1; ++f) {
-    if (!act[f]) continue;
-    double S0 = acc[f][0].total(), S1 = acc[f][1].total();
-    double S2 = D == 2 ? acc[f][2].total() : 0.0;
-    double S3 = acc[f][3].total();
-    if (lane == 0) {
-      const FaceParam& P = s.fp[fidx[f]];
-      double fl[4];
-      fl[0] = P.fwa[0] + S0;
-      fl[1] = P.fwa[1] + S1;
-      if (D == 1) {
-        fl[2] = P.fwa[2] + 0.5 * S3;
-        fl[3] = 0.0;
-      } else {
-        fl[2] = P.fwa[2] + S2;
-        fl[3] = P.fwa[3] + 0.5 * S3;
-      }
-      double* out = s.fw + (long)fidx[f] * 4;
-      if (DIR == 1) {  // global_frame with n = (0, 1)
-        out[0] = fl[0];
-        out[1] = -fl[2];
-        out[2] = fl[1];
-        out[3] = fl[3];
-      } else {
-        out[0] = fl[0];
-        out[1] = fl[1];
-        out[2] = fl[2];
-        out[3] = fl[3];
-      }
-    }
-  }
-  if (SHAK) {
-#pragma unroll
-    for (int c = 0; c < TS; ++c) {
-      double q0 = qa[c][0].total();
-      double q1 = D == 2 ? qa[c][1].total() : 0.0;
-      if (lane == 0 && c < ncell) {
-        long cc = base[c + 2] / vs;
-        s.q[cc * 2 + 0] = 0.5 * q0;
-        s.q[cc * 2 + 1] = 0.5 * q1;
-      }
-    }
-  }
-}
-
-// ------------------------------------------------------------------ pass B
-
-// Per-face evaluation state of one thread (one velocity, static upwind side).
-template <typename R>
-struct FEv;
-
-// FP32: monomial form of FaceCoef32.
-constexpr bool FLUX_NEEDS_G = true;
-template <>
-struct FEv<float> {
-  float4 E, T, G, C, Dd;
-  int kind;
-  template <bool FAST>
-  __device__ __forceinline__ void load_interior(const DevState& s, int f, bool pos) {
-    kind = 1;
-    const FaceCoef32& c = s.fc[f];
-    E = c.E;
-    T = c.T;
-    if (FLUX_NEEDS_G) {
-      G = c.G;
-      const float4* cd = pos ? &c.Cp : &c.Cm;
-      C = cd[0];
-      Dd = cd[1];
-    }
-  }
-  __device__ __forceinline__ void load(const DevState& s, int f, bool pos) {
-    kind = s.kind[f];
-    if (kind == 0) return;
-    const FaceCoef32& c = s.fc[f];
-    E = c.E;
-    T = c.T;
-    if (kind == 1) {
-      G = c.G;
-      C = pos ? c.Cp : c.Cm;
-      Dd = pos ? c.Dp : c.Dm;
-    }
-  }
-};
-
-// FP64: direct formulas of the reference with the interface prim.
-template <>
-struct FEv<double> {
-  FP<double> P;
-  double dd;  // cell size along the face normal
-  double wU, wV, wlam, wrn, wcB, wsc, rot;
-  int kind;
-  template <bool FAST>
-  __device__ __forceinline__ void load_interior(const DevState& s, int f, bool pos) {
-    load(s, f, pos);
-  }
-  __device__ __forceinline__ void load(const DevState& s, int f, bool pos) {
-    (void)pos;
-    kind = s.kind[f];
-    if (kind == 0) return;
-    const Geo& g = s.g;
-    FaceGeo r = face_geo(g, f);
-    dd = r.d == 0 ? g.dx : g.dy;
-    if (kind == 1) {
-      P = load_fp<double>(s, f);
-    } else {
-      const double* wp = s.wall + (long)f * 4;
-      double lw = g.D == 1 ? wp[2] : wp[3];
-      double rho = s.rhow[f];
-      wU = r.d == 0 ? wp[1] : wp[2];
-      wV = g.D == 1 ? 0.0 : (r.d == 0 ? wp[2] : -wp[1]);
-      wlam = lw;
-      wrn = g.D == 1 ? rho * sqrt(lw / PI) : rho * (lw / PI);
-      wcB = g.K / (2.0 * lw);
-      wsc = g.D == 2 ? (r.d == 0 ? g.dy : g.dx) : 1.0;
-      int p0 = r.d == 0 ? r.fi : r.fj;
-      rot = p0 == 0 ? 1.0 : -1.0;
-    }
-  }
-};
-
-// Velocity monomials of one face direction.
-template <typename R>
-struct Mono {
-  R un, ut, c2, m[7];
-  __device__ __forceinline__ void set(R a, R b) {
-    un = a;
-    ut = b;
-    c2 = a * a + b * b;
-    m[0] = a;
-    m[1] = a * a;
-    m[2] = m[1] * a;
-    m[3] = m[1] * b;
-    m[4] = m[1] * c2;
-    m[5] = a * b;
-    m[6] = a * c2;
-  }
-};
-
-// Interface flux of one face at this thread's velocity.  hu, bu: upwind cell
-// values; su, sb: upwind slopes times dx; side = +0.5 when the upwind cell is
-// on the left, -0.5 on the right; hc, bc: the interior cell of a wall face.
-template <int D, int FLUX, bool FAST = false>
-__device__ __forceinline__ void eval_face(const FEv<float>& e, const Mono<float>& M, float side,
-                                          float hu, float bu, float su, float sb, float hc,
-                                          float bc, double dt, float& fh, float& fb) {
-  (void)dt;
-  if (!FAST && e.kind == 0) {
-    fh = 0.f;
-    fb = 0.f;
-    return;
-  }
-  const float un = M.un;
-  if (!FAST && e.kind == 2) {
-    // u h_wall len dt, h_wall the wall Maxwellian on incoming velocities
-    // (src/Flux/flux_boundary.jl:39-61, :190-220)
-    bool in = un * e.T.w >= 0.f;
-    float hw, bw;
-    if (in) {
-      hw = ex2(e.E.x + e.E.y * un + e.E.z * M.ut + e.E.w * M.c2);
-      bw = hw * e.T.z;
-    } else {
-      hw = hc;
-      bw = bc;
-    }
-    fh = un * hw * e.T.x;
-    fb = un * bw * e.T.x;
-    return;
-  }
-  const float hf = hu + side * su;
-  const float bf = bu + side * sb;
-  const float a = e.T.x * un;
-  const float c = e.T.y * M.m[1];
-  fh = a * hf - c * su;
-  fb = a * bf - c * sb;
-  if (FLUX == FLUX_KFVS) return;
-  const float Hm = ex2(e.E.x + e.E.y * un + e.E.z * M.ut + e.E.w * M.c2);
-  float ph = e.T.z * M.m[0];
-  float pb = e.T.w * M.m[0];
-  if (FLUX == FLUX_UGKS) {
-    ph += e.C.x * M.m[1] + e.C.y * M.m[2] + e.C.w * M.m[4] + e.G.x * M.m[5] + e.G.y * M.m[6];
-    pb += e.Dd.x * M.m[1] + e.Dd.y * M.m[2] + e.Dd.w * M.m[4] + e.G.z * M.m[5] + e.G.w * M.m[6];
-    if (D == 2) {
-      ph += e.C.z * M.m[3];
-      pb += e.Dd.z * M.m[3];
-    }
-  }
-  fh += Hm * ph;
-  fb += Hm * pb;
-}
-
-template <int D, int FLUX, bool FAST = false>
-__device__ __forceinline__ void eval_face(const FEv<double>& e, const Mono<double>& M,
-                                          double side, double hu, double bu, double su,
-                                          double sb, double hc, double bc, double dt,
-                                          double& fh, double& fb) {
-  if (!FAST && e.kind == 0) {
-    fh = 0.0;
-    fb = 0.0;
-    return;
-  }
-  const double un = M.un, ut = M.ut;
-  if (!FAST && e.kind == 2) {
-    bool in = un * e.rot >= 0.0;
-    double hw, bw;
-    if (in) {
-      double du = un - e.wU, ee = du * du;
-      if (D == 2) {
-        double dv = ut - e.wV;
-        ee += dv * dv;
-      }
-      hw = e.wrn * exp(-e.wlam * ee);
-      bw = hw * e.wcB;
-    } else {
-      hw = hc;
-      bw = bc;
-    }
-    fh = un * hw * e.wsc * dt;
-    fb = un * bw * e.wsc * dt;
-    return;
-  }
-  const double hf = hu + side * su;
-  const double bf = bu + side * sb;
-  double Th, Tb;
-  face_flux<double, FLUX, D>(e.P, dt, un, ut, side > 0.0, hf, bf, su / e.dd, sb / e.dd, fh, fb,
-                             Th, Tb);
-}
-
-// Pointwise relaxation of one cell value (step!, src/Solver/step_2f.jl:32-63, :210-248).
-__device__ __forceinline__ void relax(const CellCoef32& k, bool shak, float u, float vv,
-                                      float c2, float h0, float b0, float dh, float db,
-                                      float& hn, float& bn) {
-  float M = ex2(k.EM.x + k.EM.y * u + k.EM.z * vv + k.EM.w * c2);
-  float MH = M, MB = M * k.A.x;
-  if (shak) {
-    float OH = ex2(k.EO.x + k.EO.y * u + k.EO.z * vv + k.EO.w * c2);
-    float cq = (k.Q.x + k.Q.y * u + k.Q.z * vv) * OH;
-    float tl = k.TL.x + k.TL.y * u + k.TL.z * vv + k.TL.w * c2;
-    MH += cq * (tl - 5.f);
-    MB += cq * (tl - 3.f) * k.Q.w;
-  }
-  hn = (h0 + dh * k.A.w + k.A.y * MH) * k.A.z;
-  bn = (b0 + db * k.A.w + k.A.y * MB) * k.A.z;
-}
-
-__device__ __forceinline__ void relax(const CP<double>& C, double ds, double u, double vv,
-                                      double Kf, int D, double h0, double b0, double dh,
-                                      double db, double& hn, double& bn) {
-  if (!C.upd) {
-    hn = h0;
-    bn = b0;
-    return;
-  }
-  double du = u - C.U, e = du * du;
-  if (D == 2) {
-    double dv = vv - C.V;
-    e += dv * dv;
-  }
-  double MH = C.rho_n * exp(-C.lam * e);
-  double MB = MH * Kf / (2.0 * C.lam);
-  if (C.coll == COLL_SHAKHOV) {
-    double ou = u - C.oU, oe = ou * ou, cq = ou * C.s0;
-    if (D == 2) {
-      double ov = vv - C.oV;
-      oe += ov * ov;
-      cq += ov * C.s1;
-    }
-    double OH = C.o_rho_n * exp(-C.olam * oe);
-    double OB = OH * Kf / (2.0 * C.olam);
-    double tl = 2.0 * C.olam * oe + Kf;
-    MH += cq * (tl - 5.0) * OH;
-    MB += cq * (tl - 3.0) * OB;
-  }
-  hn = (h0 + dh / ds + C.dtau * MH) / (1.0 + C.dtau);
-  bn = (b0 + db / ds + C.dtau * MB) / (1.0 + C.dtau);
-}
-
-// Pass B: one thread per velocity, CTA = (strip of TX columns, RY rows,
-// BS velocities).  Window rows wh[0..3] = rows j-1 .. j+2 of the strip; the
-// next window row and the next row's 4-cell x halo are loaded one iteration
-// ahead so their latency overlaps the current row's arithmetic.
-template <typename R, int D, int FLUX, int TX, int BS>
-__global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march(DevState s, double dt, int RY) {
-  const Geo& g = s.g;
-  const int v = blockIdx.z * BS + threadIdx.x;
-  if (v >= g.nvel) return;
-  const int i0 = blockIdx.x * TX;
-  const int ncol = min(TX, g.nx - i0);
-  const int j0 = D == 2 ? blockIdx.y * RY : 0;
-  const int j1 = D == 2 ? min(g.ny, j0 + RY) : 1;
-  const int vs = g.vstride;
-  const R* __restrict__ H = (const R*)s.h[s.cur];
-  const R* __restrict__ Bq = (const R*)s.b[s.cur];
-  R* __restrict__ Ho = (R*)s.h[s.cur ^ 1];
-  R* __restrict__ Bo = (R*)s.b[s.cur ^ 1];
-  const R u = vtab<R>(s, 0)[v];
-  const R vv = D == 2 ? vtab<R>(s, 1)[v] : R(0);
-  Mono<R> MX, MY;
-  MX.set(u, vv);
-  if (D == 2) MY.set(vv, -u);
-  const bool px = u >= R(0), py = vv >= R(0);
-  const R sxs = px ? R(0.5) : R(-0.5), sys = py ? R(0.5) : R(-0.5);
-  const R epsx = R(1.e-7 * g.dx), epsy = R(1.e-7 * g.dy);
-  const bool shak = s.coll == COLL_SHAKHOV;
-  const double ds = D == 1 ? g.dx : g.dx * g.dy;
-  const double Kf = g.K;
-
-  bool exx[TX + 4];
-  int rx[TX + 4];
-  int coff[TX + 4];  // offset of (column, v) inside a row
-#pragma unroll
-  for (int w = 0; w < TX + 4; ++w) {
-    int i = i0 - 2 + w;
-    exx[w] = i >= -g.ngx && i < g.nx + g.ngx;
-    rx[w] = slope_rule(g, 0, i);
-    coff[w] = exx[w] ? (i + g.ngx) * vs + v : 0;
-  }
-  const long rows = (long)g.nxt * vs;
-  auto rowok = [&](int j) { return j >= -g.ngy && j < g.ny + g.ngy; };
-  auto tile = [&](int j, R* th, R* tb) {
-    const bool rk = rowok(j);
-    const long ro = rk ? (long)(j + g.ngy) * rows : 0;
-#pragma unroll
-    for (int c = 0; c < TX; ++c) {
-      const bool e = rk && exx[c + 2];
-      th[c] = ldq(H + ro, coff[c + 2], e);
-      tb[c] = ldq(Bq + ro, coff[c + 2], e);
-    }
-  };
-  auto halo = [&](int j, R* hh, R* hb) {
-    const bool rk = rowok(j);
-    const long ro = rk ? (long)(j + g.ngy) * rows : 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int w = k < 2 ? k : TX + k;
-      hh[k] = ldq(H + ro, coff[w], rk && exx[w]);
-      hb[k] = ldq(Bq + ro, coff[w], rk && exx[w]);
-    }
-  };
-
-  R wh[4][TX], wb[4][TX];
-  R nh[TX], nb[TX];
-  R hh[4], hb[4], nhh[4], nhb[4];
-  R fyh[TX], fyb[TX];
-  if (D == 2) {
-    // prologue: rows j0-2 .. j0+2, the halo of row j0 and the y face below row j0
-    R ph[TX], pb[TX];
-    tile(j0 - 2, ph, pb);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) tile(j0 - 1 + k, wh[k], wb[k]);
-    halo(j0, hh, hb);
-    const int rlo = slope_rule(g, 1, j0 - 1), rhi = slope_rule(g, 1, j0);
-#pragma unroll
-    for (int c = 0; c < TX; ++c) {
-      FEv<R> e;
-      e.kind = 0;
-      if (c < ncol) e.load(s, s.nface_x + j0 * g.nx + i0 + c, py);
-      R hu, bu, su, sb;
-      if (py) {
-        hu = wh[0][c];
-        bu = wb[0][c];
-        su = vl_diff(rlo, ph[c], wh[0][c], wh[1][c], epsy);
-        sb = vl_diff(rlo, pb[c], wb[0][c], wb[1][c], epsy);
-      } else {
-        hu = wh[1][c];
-        bu = wb[1][c];
-        su = vl_diff(rhi, wh[0][c], wh[1][c], wh[2][c], epsy);
-        sb = vl_diff(rhi, wb[0][c], wb[1][c], wb[2][c], epsy);
-      }
-      eval_face<D, FLUX>(e, MY, sys, hu, bu, su, sb, wh[1][c], wb[1][c], dt, fyh[c], fyb[c]);
-    }
-  } else {
-    tile(0, wh[1], wb[1]);
-    halo(0, hh, hb);
-  }
-
-  auto row = [&](int j, auto fast_tag, auto sign_tag) {
-    constexpr bool FAST = decltype(fast_tag)::value;
-    constexpr int SG = decltype(sign_tag)::value;
-    // compile-time upwind sides when the warp's velocities share their signs
-    const bool qx = SG == 0 ? px : (SG == 1 || SG == 2);
-    const bool qy = SG == 0 ? py : (SG == 1 || SG == 3);
-    const R qxs = qx ? R(0.5) : R(-0.5), qys = qy ? R(0.5) : R(-0.5);
-    // prefetch the next window row and the next row's halo
-    if (D == 2 && j + 1 < j1) {
-      tile(j + 3, nh, nb);
-      halo(j + 1, nhh, nhb);
-    }
-    R xh[TX + 4], xb[TX + 4];
-#pragma unroll
-    for (int c = 0; c < TX; ++c) {
-      xh[c + 2] = wh[1][c];
-      xb[c + 2] = wb[1][c];
-    }
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      xh[k] = hh[k];
-      xb[k] = hb[k];
-      xh[TX + 2 + k] = hh[2 + k];
-      xb[TX + 2 + k] = hb[2 + k];
-    }
-    // y faces above row j
-    R fyh2[TX], fyb2[TX];
-    if (D == 2) {
-      const int rlo = slope_rule(g, 1, j), rhi = slope_rule(g, 1, j + 1);
-#pragma unroll
-      for (int c = 0; c < TX; ++c) {
-        FEv<R> e;
-        e.kind = 0;
-        if (FAST) e.template load_interior<FAST>(s, s.nface_x + (j + 1) * g.nx + i0 + c, qy);
-        else if (c < ncol) e.load(s, s.nface_x + (j + 1) * g.nx + i0 + c, qy);
-        R hu, bu, su, sb;
-        if (qy) {
-          hu = wh[1][c];
-          bu = wb[1][c];
-          su = slope<FAST>(rlo, wh[0][c], wh[1][c], wh[2][c], epsy);
-          sb = slope<FAST>(rlo, wb[0][c], wb[1][c], wb[2][c], epsy);
-        } else {
-          hu = wh[2][c];
-          bu = wb[2][c];
-          su = slope<FAST>(rhi, wh[1][c], wh[2][c], wh[3][c], epsy);
-          sb = slope<FAST>(rhi, wb[1][c], wb[2][c], wb[3][c], epsy);
-        }
-        eval_face<D, FLUX, FAST>(e, MY, qys, hu, bu, su, sb, wh[1][c], wb[1][c], dt, fyh2[c],
-                                 fyb2[c]);
-      }
-    }
-    // x slopes of cells w = 1 .. TX+2 and the x faces of row j
-    R dh[TX + 2], db[TX + 2];
-#pragma unroll
-    for (int w = 1; w <= TX + 2; ++w) {
-      dh[w - 1] = slope<FAST>(rx[w], xh[w - 1], xh[w], xh[w + 1], epsx);
-      db[w - 1] = slope<FAST>(rx[w], xb[w - 1], xb[w], xb[w + 1], epsx);
-    }
-    R fxh[TX + 1], fxb[TX + 1];
-#pragma unroll
-    for (int f = 0; f <= TX; ++f) {
-      FEv<R> e;
-      e.kind = 0;
-      const int fi = i0 + f;
-      if (FAST) e.template load_interior<FAST>(s, j * (g.nx + 1) + fi, qx);
-      else if (f <= ncol) e.load(s, j * (g.nx + 1) + fi, qx);
-      R hu = qx ? xh[f + 1] : xh[f + 2];
-      R bu = qx ? xb[f + 1] : xb[f + 2];
-      R su = qx ? dh[f] : dh[f + 1];
-      R sb = qx ? db[f] : db[f + 1];
-      R hc = fi == 0 ? xh[f + 2] : xh[f + 1];
-      R bc = fi == 0 ? xb[f + 2] : xb[f + 1];
-      eval_face<D, FLUX, FAST>(e, MX, qxs, hu, bu, su, sb, hc, bc, dt, fxh[f], fxb[f]);
-    }
-    // update the cells of row j
-    const long ro = (long)(j + g.ngy) * rows;
-#pragma unroll
-    for (int c = 0; c < TX; ++c) {
-      if (!FAST && c >= ncol) continue;
-      const int cell = cell_index(g, i0 + c, j);
-      R dhh = fxh[c] - fxh[c + 1];
-      R dbb = fxb[c] - fxb[c + 1];
-      if (D == 2) {
-        dhh = dhh + fyh[c] - fyh2[c];
-        dbb = dbb + fyb[c] - fyb2[c];
-      }
-      R hn, bn;
-      if constexpr (sizeof(R) == 4) {
-        const CellCoef32 k = s.cc[cell];
-        relax(k, shak, u, vv, MX.c2, xh[c + 2], xb[c + 2], dhh, dbb, hn, bn);
-      } else {
-        const CP<double> C = load_cp<double>(s, cell);
-        relax(C, ds, u, vv, Kf, D, xh[c + 2], xb[c + 2], dhh, dbb, hn, bn);
-      }
-      Ho[ro + coff[c + 2]] = hn;
-      Bo[ro + coff[c + 2]] = bn;
-    }
-    if (D == 2) {
-#pragma unroll
-      for (int c = 0; c < TX; ++c) {
-        wh[0][c] = wh[1][c];
-        wb[0][c] = wb[1][c];
-        wh[1][c] = wh[2][c];
-        wb[1][c] = wb[2][c];
-        wh[2][c] = wh[3][c];
-        wb[2][c] = wb[3][c];
-        wh[3][c] = nh[c];
-        wb[3][c] = nb[c];
-        fyh[c] = fyh2[c];
-        fyb[c] = fyb2[c];
-      }
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        hh[k] = nhh[k];
-        hb[k] = nhb[k];
-      }
-    }
-  };
-  const bool fastx = g.interp == 2 && i0 >= 2 && i0 + TX <= g.nx - 2;
-  // warp-uniform velocity signs select a sign-specialised interior row body
-  const unsigned am = __activemask();
-  const unsigned bx = __ballot_sync(am, px), by = __ballot_sync(am, py);
-  const int sg = (bx != 0 && bx != am) || (by != 0 && by != am)
-                     ? 0 : (bx == am ? (by == am ? 1 : 2) : (by == am ? 3 : 4));
-  using T0 = std::integral_constant<int, 0>;
-  for (int j = j0; j < j1; ++j) {
-    if (fastx && (D == 1 || (j >= 1 && j <= g.ny - 3))) {
-      switch (sg) {
-        case 1: row(j, std::true_type{}, std::integral_constant<int, 1>{}); break;
-        case 2: row(j, std::true_type{}, std::integral_constant<int, 2>{}); break;
-        case 3: row(j, std::true_type{}, std::integral_constant<int, 3>{}); break;
-        case 4: row(j, std::true_type{}, std::integral_constant<int, 4>{}); break;
-        default: row(j, std::true_type{}, T0{}); break;
-      }
-    } else {
-      row(j, std::false_type{}, T0{});
-    }
-  }
-}
-
-// ------------------------------------------------------------- launchers
-
-static inline unsigned nblk2(long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
-
-constexpr int TS_MOM = 4;   // faces per warp in pass A
-constexpr int TX_MARCH = 4; // columns per strip in pass B
-constexpr int RY_MARCH = 32;
-
-template <typename R, int D, int FLUX, int TS>
-static int mom_go(DevState& s, cudaStream_t st) {
-  const Geo& g = s.g;
-  int n = 0;
-  long wx = (long)((g.nx + TS - 1) / TS) * g.ny;
-  if (s.coll == COLL_SHAKHOV)
-    k_mom<R, D, FLUX, TS, true, 0><<<nblk2(wx * 32, 128), 128, 0, st>>>(s);
-  else
-    k_mom<R, D, FLUX, TS, false, 0><<<nblk2(wx * 32, 128), 128, 0, st>>>(s);
-  ++n;
-  if (D == 2) {
-    long wy = (long)((g.ny + TS - 1) / TS) * g.nx;
-    k_mom<R, D, FLUX, TS, false, 1><<<nblk2(wy * 32, 128), 128, 0, st>>>(s);
-    ++n;
-  }
-  return n;
-}
-
-template <typename R, int D, int FLUX>
-static int mom_t(DevState& s, cudaStream_t st) {
-  if (s.tune[KB_TUNE_MOM_TS] == 2) return mom_go<R, D, FLUX, 2>(s, st);
-  return mom_go<R, D, FLUX, TS_MOM>(s, st);
-}
+#define KB_DECL(NAME)                                      \
+  int moments_##NAME(DevState& s, cudaStream_t st);        \
+  int march_##NAME(DevState& s, double dt, cudaStream_t st);
+KB_DECL(f32_kfvs)
+KB_DECL(f32_kcu)
+KB_DECL(f32_ugks)
+KB_DECL(f64_kfvs)
+KB_DECL(f64_kcu)
+KB_DECL(f64_ugks)
+#undef KB_DECL
 
 int launch_moments(DevState& s, cudaStream_t st) {
-  const int D = s.g.D;
-#define KB_MOM(R)                                                               \
-  switch (s.flux) {                                                             \
-    case FLUX_KFVS: return D == 1 ? mom_t<R, 1, FLUX_KFVS>(s, st) : mom_t<R, 2, FLUX_KFVS>(s, st); \
-    case FLUX_KCU: return D == 1 ? mom_t<R, 1, FLUX_KCU>(s, st) : mom_t<R, 2, FLUX_KCU>(s, st);    \
-    default: return D == 1 ? mom_t<R, 1, FLUX_UGKS>(s, st) : mom_t<R, 2, FLUX_UGKS>(s, st);        \
-  }
   if (s.prec == 0) {
-    KB_MOM(double)
-  } else {
-    KB_MOM(float)
+    if (s.flux == FLUX_KFVS) return moments_f64_kfvs(s, st);
+    if (s.flux == FLUX_KCU) return moments_f64_kcu(s, st);
+    return moments_f64_ugks(s, st);
   }
-#undef KB_MOM
-}
-
-template <typename R, int D, int FLUX, int TX, int BS>
-static void march_go(DevState& s, double dt, cudaStream_t st) {
-  const Geo& g = s.g;
-  const int ry = s.tune[KB_TUNE_MARCH_RY] > 0 ? s.tune[KB_TUNE_MARCH_RY] : RY_MARCH;
-  dim3 grid((g.nx + TX - 1) / TX, D == 2 ? (g.ny + ry - 1) / ry : 1, (g.nvel + BS - 1) / BS);
-  k_march<R, D, FLUX, TX, BS><<<grid, BS, 0, st>>>(s, dt, ry);
-}
-
-template <typename R, int D, int FLUX>
-static int march_t(DevState& s, double dt, cudaStream_t st) {
-  const int tx = s.tune[KB_TUNE_MARCH_TX] > 0 ? s.tune[KB_TUNE_MARCH_TX] : TX_MARCH;
-  const int bs = s.tune[KB_TUNE_MARCH_BS] > 0 ? s.tune[KB_TUNE_MARCH_BS] : 128;
-  if (tx == 2) {
-    if (bs == 64) march_go<R, D, FLUX, 2, 64>(s, dt, st);
-    else if (bs == 256) march_go<R, D, FLUX, 2, 256>(s, dt, st);
-    else march_go<R, D, FLUX, 2, 128>(s, dt, st);
-  } else if (tx == 8) {
-    if (bs == 64) march_go<R, D, FLUX, 8, 64>(s, dt, st);
-    else if (bs == 256) march_go<R, D, FLUX, 8, 256>(s, dt, st);
-    else march_go<R, D, FLUX, 8, 128>(s, dt, st);
-  } else {
-    if (bs == 64) march_go<R, D, FLUX, 4, 64>(s, dt, st);
-    else if (bs == 256) march_go<R, D, FLUX, 4, 256>(s, dt, st);
-    else march_go<R, D, FLUX, 4, 128>(s, dt, st);
-  }
-  return 1;
+  if (s.flux == FLUX_KFVS) return moments_f32_kfvs(s, st);
+  if (s.flux == FLUX_KCU) return moments_f32_kcu(s, st);
+  return moments_f32_ugks(s, st);
 }
 
 int launch_march(DevState& s, double dt, cudaStream_t st) {
-  const int D = s.g.D;
-#define KB_MARCH(R)                                                                      \
-  switch (s.flux) {                                                                      \
-    case FLUX_KFVS: return D == 1 ? march_t<R, 1, FLUX_KFVS>(s, dt, st) : march_t<R, 2, FLUX_KFVS>(s, dt, st); \
-    case FLUX_KCU: return D == 1 ? march_t<R, 1, FLUX_KCU>(s, dt, st) : march_t<R, 2, FLUX_KCU>(s, dt, st);    \
-    default: return D == 1 ? march_t<R, 1, FLUX_UGKS>(s, dt, st) : march_t<R, 2, FLUX_UGKS>(s, dt, st);        \
-  }
   if (s.prec == 0) {
-    KB_MARCH(double)
-  } else {
-    KB_MARCH(float)
+    if (s.flux == FLUX_KFVS) return march_f64_kfvs(s, dt, st);
+    if (s.flux == FLUX_KCU) return march_f64_kcu(s, dt, st);
+    return march_f64_ugks(s, dt, st);
   }
-#undef KB_MARCH
+  if (s.flux == FLUX_KFVS) return march_f32_kfvs(s, dt, st);
+  if (s.flux == FLUX_KCU) return march_f32_kcu(s, dt, st);
+  return march_f32_ugks(s, dt, st);
 }
 
 }  // namespace kb

@@ -19,7 +19,7 @@ from . import _native as N
 CACHE = os.environ.get("KITGPU_TUNE_CACHE",
                        os.path.join(os.path.expanduser("~"), ".cache", "kitgpu_tune.json"))
 
-MARCH_TX = (2, 4, 8)
+MARCH_TX = (2, 4)
 MARCH_BS = (64, 128)
 MARCH_RY = (16, 32)
 MOM_TS = (2, 4)

@@ -158,4 +158,4 @@ def test_unsupported_paths_raise():
 
 def test_tune_signature_and_options():
     from kitgpu import tune
-    assert set(tune.MARCH_TX) <= {2, 4, 8} and set(tune.MOM_TS) <= {2, 4}
+    assert set(tune.MARCH_TX) <= {2, 4} and set(tune.MOM_TS) <= {2, 4}
