@@ -121,6 +121,26 @@ int kb_download_state(kb_handle_t* h, double* w, double* prim, double* hdist,
 int kb_timestep(kb_handle_t* h, double cfl, double sim_time, double max_time,
                 double* dt_out);
 
+/* CFL rate of a state held in the CALLER's device memory, for callers that
+ * cannot allocate device memory (a host whose device memory belongs to its
+ * own pool, or a service that has already accounted every byte): the call
+ * makes no allocation of any kind.  No counterpart in the reference.
+ *   d_prim  device array [cells incl. ghosts][dim+2], same order as
+ *           kb_upload_state's prim; only physical cells are read;
+ *   d_tmax  device double receiving max over cells of
+ *           (max(umax,|U|) + c)/dx (+ (max(vmax,|V|) + c)/dy in 2D), so that
+ *           dt = cfl / tmax as in kb_timestep;
+ *   stream  cudaStream_t (NULL: default stream); the call only enqueues.
+ * Per-block partial maxima live in one fixed device array compiled into the
+ * library (8 KB, held by every GPU that loads it until exit); grids above
+ * KB_NOALLOC_MAX_CELLS physical cells are rejected with KB_ERR_ARG.  Every
+ * call reuses that array: calls that overlap on the GPU race.  The first call
+ * on a device looks up the array's device address; make that first call
+ * before any stream capture. */
+#define KB_NOALLOC_MAX_CELLS 2097152
+int kb_timestep_noalloc(const kb_config_t* cfg, const double* d_prim, double* d_tmax,
+                        void* stream);
+
 /* reconstruct!: van Leer slopes of w for every cell.  The slopes of h and b
  * are formed on the fly inside kb_evolve / kb_update, so this stage only
  * refreshes the w slopes that KCU / UGKS read. */

@@ -75,6 +75,8 @@ SIGNATURES = {
     "kb_get_stream": [_H, ctypes.POINTER(ctypes.c_void_p)],
     "kb_set_tuning": [_H, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32],
     "kb_step_async": [_H, ctypes.c_double, ctypes.c_int32],
+    "kb_timestep_noalloc": [ctypes.POINTER(KbConfig), ctypes.c_void_p, ctypes.c_void_p,
+                            ctypes.c_void_p],
     "kb_query": [_H, _D, ctypes.POINTER(ctypes.c_int32)],
     "kb_get_tuning": [_H, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32],
 }
