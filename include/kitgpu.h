@@ -182,8 +182,9 @@ int kb_download_faces(kb_handle_t* h, double dt, double* fw, double* fh, double*
  * for the direction, src/Data/data_array.jl:15-50).  Any pointer may be NULL. */
 int kb_download_slopes(kb_handle_t* h, double* sw, double* sh, double* sb);
 
-/* Status word of the handle: KB_OK, or KB_ERR_NUMERIC once a step produced a
- * non-finite or non-positive density / lambda. */
+/* Status word of the handle: KB_OK, KB_ERR_NUMERIC once a step produced a
+ * non-finite or non-positive density / lambda, or KB_ERR_TIMEOUT once a
+ * bounded device wait (coefficient staging of the update pass) gave up. */
 int kb_status(kb_handle_t* h);
 
 /* Device bytes held by the handle. */

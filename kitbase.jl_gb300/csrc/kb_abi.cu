@@ -413,6 +413,14 @@ int kb_evolve(kb_handle_t* h, double dt) {
   return KB_OK;
 }
 
+// Status word of the device state: bit 0 a non-physical state after a step,
+// bit 1 a bounded device wait (bulk-copy staging) that gave up.
+static int status_error(int st) {
+  if (st & 2) return fail(KB_ERR_TIMEOUT, "a device wait for staged coefficients timed out");
+  if (st) return fail(KB_ERR_NUMERIC, "non-finite or non-positive density / lambda after a step");
+  return KB_OK;
+}
+
 static int read_residual(kb_handle* h, double* residual) {
   double r[4];
   int st = 0;
@@ -421,8 +429,7 @@ static int read_residual(kb_handle* h, double* residual) {
   KB_TRY(sync(h));
   if (residual)
     for (int k = 0; k < h->s.g.NW; ++k) residual[k] = r[k];
-  if (st) return fail(KB_ERR_NUMERIC, "non-finite or non-positive density / lambda after a step");
-  return KB_OK;
+  return status_error(st);
 }
 
 int kb_update(kb_handle_t* h, double dt, double* residual) {
@@ -533,8 +540,7 @@ int kb_query(kb_handle_t* h, double* residual, int32_t* ready) {
     for (int k = 0; k < h->s.g.NW; ++k) residual[k] = h->h_res[k];
   int st = 0;
   std::memcpy(&st, h->h_res + 4, sizeof(int));
-  if (st) return fail(KB_ERR_NUMERIC, "non-finite or non-positive density / lambda after a step");
-  return KB_OK;
+  return status_error(st);
 }
 
 int kb_set_timing(kb_handle_t* h, int enable) {
@@ -654,7 +660,7 @@ int kb_status(kb_handle_t* h) {
   int st = 0;
   KB_CUDA(cudaMemcpyAsync(&st, h->s.status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   KB_TRY(sync(h));
-  return st ? KB_ERR_NUMERIC : KB_OK;
+  return (st & 2) ? KB_ERR_TIMEOUT : st ? KB_ERR_NUMERIC : KB_OK;
 }
 
 int kb_device_bytes(kb_handle_t* h, int64_t* bytes) {

@@ -52,6 +52,58 @@ __device__ __forceinline__ float ex2(float x) {
   return y;
 }
 
+// ---- bulk async copies (TMA engine) into shared memory, completed on an mbarrier.
+// Every wait is bounded by the global timer: after KB_WAIT_NS the waiter
+// gives up, and the caller records KB status bit 2 (timeout).
+constexpr unsigned long long KB_WAIT_NS = 1000000000ull;  // 1 s
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// true once the phase with this parity completed; false after KB_WAIT_NS.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  while (!mbar_try(bar, parity))
+    if (gtimer() - t0 > KB_WAIT_NS) return false;
+  return true;
+}
+// global -> shared bulk copy; dst, src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // Rule-dispatching slope; FAST = interior cell (van Leer only).
 template <bool FAST, typename R>
 __device__ __forceinline__ R slope(int rule, R qm, R q0, R qp, R epsd) {
@@ -292,10 +344,9 @@ template <>
 struct FEv<float> {
   float4 E, T, G, C, Dd;
   int kind;
-  template <bool FAST>
-  __device__ __forceinline__ void load_interior(const DevState& s, int f, bool pos) {
+  // c: this face's coefficient block (global or staged in shared memory)
+  __device__ __forceinline__ void load_interior(const FaceCoef32& c, bool pos) {
     kind = 1;
-    const FaceCoef32& c = s.fc[f];
     E = c.E;
     T = c.T;
     if (FLUX_NEEDS_G) {
@@ -305,10 +356,9 @@ struct FEv<float> {
       Dd = cd[1];
     }
   }
-  __device__ __forceinline__ void load(const DevState& s, int f, bool pos) {
-    kind = s.kind[f];
+  __device__ __forceinline__ void load(const FaceCoef32& c, int kd, bool pos) {
+    kind = kd;
     if (kind == 0) return;
-    const FaceCoef32& c = s.fc[f];
     E = c.E;
     T = c.T;
     if (kind == 1) {
@@ -326,10 +376,6 @@ struct FEv<double> {
   double dd;  // cell size along the face normal
   double wU, wV, wlam, wrn, wcB, wsc, rot;
   int kind;
-  template <bool FAST>
-  __device__ __forceinline__ void load_interior(const DevState& s, int f, bool pos) {
-    load(s, f, pos);
-  }
   __device__ __forceinline__ void load(const DevState& s, int f, bool pos) {
     (void)pos;
     kind = s.kind[f];
@@ -511,31 +557,122 @@ __device__ __forceinline__ void relax(const CP<double>& C, double ds, double u, 
   bn = (b0 + db / ds + C.dtau * MB) / (1.0 + C.dtau);
 }
 
+// Load face f's evaluation state: FP32 from its coefficient block c (global
+// memory or staged in shared memory), FP64 from the FaceParam table.
+template <bool FAST>
+__device__ __forceinline__ void face_load(FEv<float>& e, const DevState& s, int f,
+                                          const FaceCoef32& c, bool pos) {
+  if (FAST) e.load_interior(c, pos);
+  else e.load(c, s.kind[f], pos);
+}
+template <bool FAST>
+__device__ __forceinline__ void face_load(FEv<double>& e, const DevState& s, int f,
+                                          const FaceCoef32& c, bool pos) {
+  (void)c;
+  e.load(s, f, pos);
+}
+
+// Shared-memory staging of the FP32 coefficient blocks of a pass-B strip:
+// rows are staged CH at a time into two buffers (double buffering) by bulk
+// async copies issued from warp 0, each buffer completing on its own mbarrier.
+// Per row of a buffer: x faces [TX+1], y faces above the row [TX], cells [TX].
+constexpr int MARCH_CH = 8;
+template <int TX>
+struct MarchStage {
+  static constexpr int XF = 0;
+  static constexpr int YF = (TX + 1) * (int)sizeof(FaceCoef32);
+  static constexpr int CC = YF + TX * (int)sizeof(FaceCoef32);
+  static constexpr int ROW = CC + TX * (int)sizeof(CellCoef32);
+  static constexpr int BUF = MARCH_CH * ROW;
+  static constexpr int Y0 = TX * (int)sizeof(FaceCoef32);  // y faces below the first row
+  // [y faces below the first row][buffer 0][buffer 1][2 mbarriers]
+  static constexpr int BYTES = Y0 + 2 * BUF + 16;
+};
+static_assert(sizeof(FaceCoef32) % 16 == 0 && sizeof(CellCoef32) % 16 == 0,
+              "bulk copies need 16-byte multiples");
+
 // Pass B: one thread per velocity, CTA = (strip of TX columns, RY rows,
 // BS velocities).  Window rows wh[0..3] = rows j-1 .. j+2 of the strip; the
 // next window row and the next row's 4-cell x halo are loaded one iteration
-// ahead so their latency overlaps the current row's arithmetic.
+// ahead so their latency overlaps the current row's arithmetic.  In the 2D
+// FP32 form the per-face / per-cell coefficient blocks of the strip arrive in
+// shared memory by bulk async copies, a chunk of rows ahead of their use, so
+// the row body waits on no global load but the distributions.  Threads past
+// the last velocity compute on a clamped velocity and store nothing, so every
+// thread reaches every barrier.
 template <typename R, int D, int FLUX, int TX, int BS>
 __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march(DevState s, double dt, int RY) {
+  constexpr bool STAGE = sizeof(R) == 4 && D == 2;
+  using SL = MarchStage<TX>;
+  extern __shared__ __align__(16) unsigned char smem[];
   const Geo& g = s.g;
-  const int v = blockIdx.z * BS + threadIdx.x;
-  if (v >= g.nvel) return;
+  const int vraw = blockIdx.z * BS + threadIdx.x;
+  const bool vok = vraw < g.nvel;
+  const int v = vok ? vraw : g.nvel - 1;
   const int i0 = blockIdx.x * TX;
   const int ncol = min(TX, g.nx - i0);
   const int j0 = D == 2 ? blockIdx.y * RY : 0;
-  const int j1 = D == 2 ? min(g.ny, j0 + RY) : 1;
+  int j1 = D == 2 ? min(g.ny, j0 + RY) : 1;
   const int vs = g.vstride;
   const R* __restrict__ H = (const R*)s.h[s.cur];
   const R* __restrict__ Bq = (const R*)s.b[s.cur];
   R* __restrict__ Ho = (R*)s.h[s.cur ^ 1];
   R* __restrict__ Bo = (R*)s.b[s.cur ^ 1];
+
+  // ---- coefficient staging (2D FP32)
+  const int nchunk = (j1 - j0 + MARCH_CH - 1) / MARCH_CH;
+  unsigned long long* bars = (unsigned long long*)(smem + SL::BYTES - 16);
+  int failed = -1;  // chunk whose copies missed the deadline
+  auto issue = [&](int ch) {  // warp 0: copy chunk ch into buffer ch & 1
+    unsigned char* buf = smem + SL::Y0 + (ch & 1) * SL::BUF;
+    const int r0 = j0 + ch * MARCH_CH;
+    const int nr = min(MARCH_CH, j1 - r0);
+    const unsigned xb = (ncol + 1) * sizeof(FaceCoef32), yb = ncol * sizeof(FaceCoef32),
+                   cb = ncol * sizeof(CellCoef32);
+    unsigned bytes = nr * (xb + yb + cb);
+    if (ch == 0) bytes += yb;
+    const int lane = threadIdx.x;
+    if (lane == 0) mbar_expect(&bars[ch & 1], bytes);
+    __syncwarp();
+    if (lane < nr) {
+      const int j = r0 + lane;
+      unsigned char* row = buf + lane * SL::ROW;
+      bulk_g2s(row + SL::XF, s.fc + (long)j * (g.nx + 1) + i0, xb, &bars[ch & 1]);
+      bulk_g2s(row + SL::YF, s.fc + s.nface_x + (long)(j + 1) * g.nx + i0, yb, &bars[ch & 1]);
+      bulk_g2s(row + SL::CC, s.cc + cell_index(g, i0, j), cb, &bars[ch & 1]);
+    }
+    if (ch == 0 && lane == 0)
+      bulk_g2s(smem, s.fc + s.nface_x + (long)j0 * g.nx + i0, yb, &bars[0]);
+  };
+  // wait for chunk ch; the outcome is made CTA-uniform, and after a timeout
+  // the CTA stops issuing copies and leaves the row loop
+  auto await = [&](int ch) {
+    const bool ok = mbar_wait(&bars[ch & 1], (ch >> 1) & 1);
+    if (__syncthreads_or(!ok)) {
+      failed = ch;
+      if (threadIdx.x == 0) atomicOr(s.status, 2);
+    }
+  };
+  if (STAGE) {
+    if (threadIdx.x == 0) {
+      mbar_init(&bars[0], 1);
+      mbar_init(&bars[1], 1);
+      fence_async_smem();
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      issue(0);
+      if (nchunk > 1) issue(1);
+    }
+  }
+
   const R u = vtab<R>(s, 0)[v];
   const R vv = D == 2 ? vtab<R>(s, 1)[v] : R(0);
   Mono<R> MX, MY;
   MX.set(u, vv);
   if (D == 2) MY.set(vv, -u);
   const bool px = u >= R(0), py = vv >= R(0);
-  const R sxs = px ? R(0.5) : R(-0.5), sys = py ? R(0.5) : R(-0.5);
+  const R sys = py ? R(0.5) : R(-0.5);
   const R epsx = R(1.e-7 * g.dx), epsy = R(1.e-7 * g.dy);
   const bool shak = s.coll == COLL_SHAKHOV;
   const double ds = D == 1 ? g.dx : g.dx * g.dy;
@@ -573,6 +710,23 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
       hb[k] = ldq(Bq + ro, coff[w], rk && exx[w]);
     }
   };
+  // coefficient blocks of row j: the staged copies, or the global tables
+  auto stage_row = [&](int j) -> const unsigned char* {
+    const int r = j - j0;
+    return smem + SL::Y0 + ((r / MARCH_CH) & 1) * SL::BUF + (r % MARCH_CH) * SL::ROW;
+  };
+  auto xcoef = [&](int j) -> const FaceCoef32* {
+    if (STAGE) return (const FaceCoef32*)(stage_row(j) + SL::XF);
+    return s.fc + (long)j * (g.nx + 1) + i0;
+  };
+  auto ycoef = [&](int j) -> const FaceCoef32* {  // y faces above row j
+    if (STAGE) return (const FaceCoef32*)(stage_row(j) + SL::YF);
+    return s.fc + s.nface_x + (long)(j + 1) * g.nx + i0;
+  };
+  auto ccoef = [&](int j) -> const CellCoef32* {
+    if (STAGE) return (const CellCoef32*)(stage_row(j) + SL::CC);
+    return s.cc + cell_index(g, i0, j);
+  };
 
   R wh[4][TX], wb[4][TX];
   R nh[TX], nb[TX];
@@ -585,12 +739,18 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
 #pragma unroll
     for (int k = 0; k < 4; ++k) tile(j0 - 1 + k, wh[k], wb[k]);
     halo(j0, hh, hb);
+    if (STAGE) {
+      await(0);
+      if (failed >= 0) j1 = j0;  // no rows: straight to the bounded clean-up
+    }
+    const FaceCoef32* y0c =
+        STAGE ? (const FaceCoef32*)smem : s.fc + s.nface_x + (long)j0 * g.nx + i0;
     const int rlo = slope_rule(g, 1, j0 - 1), rhi = slope_rule(g, 1, j0);
 #pragma unroll
     for (int c = 0; c < TX; ++c) {
       FEv<R> e;
       e.kind = 0;
-      if (c < ncol) e.load(s, s.nface_x + j0 * g.nx + i0 + c, py);
+      if (c < ncol) face_load<false>(e, s, s.nface_x + j0 * g.nx + i0 + c, y0c[c], py);
       R hu, bu, su, sb;
       if (py) {
         hu = wh[0][c];
@@ -617,6 +777,9 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
     const bool qx = SG == 0 ? px : (SG == 1 || SG == 2);
     const bool qy = SG == 0 ? py : (SG == 1 || SG == 3);
     const R qxs = qx ? R(0.5) : R(-0.5), qys = qy ? R(0.5) : R(-0.5);
+    const FaceCoef32* xc = xcoef(j);
+    const FaceCoef32* yc = ycoef(j);
+    const CellCoef32* cc = ccoef(j);
     // prefetch the next window row and the next row's halo
     if (D == 2 && j + 1 < j1) {
       tile(j + 3, nh, nb);
@@ -643,8 +806,8 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
       for (int c = 0; c < TX; ++c) {
         FEv<R> e;
         e.kind = 0;
-        if (FAST) e.template load_interior<FAST>(s, s.nface_x + (j + 1) * g.nx + i0 + c, qy);
-        else if (c < ncol) e.load(s, s.nface_x + (j + 1) * g.nx + i0 + c, qy);
+        if (FAST || c < ncol)
+          face_load<FAST>(e, s, s.nface_x + (j + 1) * g.nx + i0 + c, yc[c], qy);
         R hu, bu, su, sb;
         if (qy) {
           hu = wh[1][c];
@@ -674,8 +837,7 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
       FEv<R> e;
       e.kind = 0;
       const int fi = i0 + f;
-      if (FAST) e.template load_interior<FAST>(s, j * (g.nx + 1) + fi, qx);
-      else if (f <= ncol) e.load(s, j * (g.nx + 1) + fi, qx);
+      if (FAST || f <= ncol) face_load<FAST>(e, s, j * (g.nx + 1) + fi, xc[f], qx);
       R hu = qx ? xh[f + 1] : xh[f + 2];
       R bu = qx ? xb[f + 1] : xb[f + 2];
       R su = qx ? dh[f] : dh[f + 1];
@@ -689,7 +851,6 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
 #pragma unroll
     for (int c = 0; c < TX; ++c) {
       if (!FAST && c >= ncol) continue;
-      const int cell = cell_index(g, i0 + c, j);
       R dhh = fxh[c] - fxh[c + 1];
       R dbb = fxb[c] - fxb[c + 1];
       if (D == 2) {
@@ -698,14 +859,16 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
       }
       R hn, bn;
       if constexpr (sizeof(R) == 4) {
-        const CellCoef32 k = s.cc[cell];
+        const CellCoef32 k = cc[c];
         relax(k, shak, u, vv, MX.c2, xh[c + 2], xb[c + 2], dhh, dbb, hn, bn);
       } else {
-        const CP<double> C = load_cp<double>(s, cell);
+        const CP<double> C = load_cp<double>(s, cell_index(g, i0 + c, j));
         relax(C, ds, u, vv, Kf, D, xh[c + 2], xb[c + 2], dhh, dbb, hn, bn);
       }
-      Ho[ro + coff[c + 2]] = hn;
-      Bo[ro + coff[c + 2]] = bn;
+      if (vok) {
+        Ho[ro + coff[c + 2]] = hn;
+        Bo[ro + coff[c + 2]] = bn;
+      }
     }
     if (D == 2) {
 #pragma unroll
@@ -730,12 +893,28 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
   };
   const bool fastx = g.interp == 2 && i0 >= 2 && i0 + TX <= g.nx - 2;
   // warp-uniform velocity signs select a sign-specialised interior row body
-  const unsigned am = __activemask();
-  const unsigned bx = __ballot_sync(am, px), by = __ballot_sync(am, py);
-  const int sg = (bx != 0 && bx != am) || (by != 0 && by != am)
-                     ? 0 : (bx == am ? (by == am ? 1 : 2) : (by == am ? 3 : 4));
+  const unsigned bx = __ballot_sync(0xffffffffu, px), by = __ballot_sync(0xffffffffu, py);
+  const int sg = (bx != 0 && bx != 0xffffffffu) || (by != 0 && by != 0xffffffffu)
+                     ? 0 : (bx != 0 ? (by != 0 ? 1 : 2) : (by != 0 ? 3 : 4));
   using T0 = std::integral_constant<int, 0>;
   for (int j = j0; j < j1; ++j) {
+    if (STAGE) {
+      const int r = j - j0;
+      if (r > 0 && r % MARCH_CH == 0) {
+        const int ch = r / MARCH_CH;
+        // buffer (ch + 1) & 1 is free once every thread finished chunk ch - 1
+        if (ch + 1 < nchunk) {
+          __syncthreads();
+          if (threadIdx.x < 32) {
+            if (threadIdx.x == 0) fence_async_smem();
+            __syncwarp();
+            issue(ch + 1);
+          }
+        }
+        await(ch);
+        if (failed >= 0) break;
+      }
+    }
     if (fastx && (D == 1 || (j >= 1 && j <= g.ny - 3))) {
       // sign-specialised rows only in the FP32 path (the FP64 path is
       // bound by the FP64 pipe, not by selects)
@@ -753,6 +932,12 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
     } else {
       row(j, std::false_type{}, T0{});
     }
+  }
+  if (STAGE && failed >= 0) {
+    // copies of the failed chunk and of the one issued after it may still
+    // land: wait (bounded) for them before the shared memory is released
+    mbar_wait(&bars[failed & 1], (failed >> 1) & 1);
+    if (failed + 1 < nchunk) mbar_wait(&bars[(failed + 1) & 1], ((failed + 1) >> 1) & 1);
   }
 }
 
@@ -793,7 +978,8 @@ static void march_go(DevState& s, double dt, cudaStream_t st) {
   const Geo& g = s.g;
   const int ry = s.tune[KB_TUNE_MARCH_RY] > 0 ? s.tune[KB_TUNE_MARCH_RY] : RY_MARCH;
   dim3 grid((g.nx + TX - 1) / TX, D == 2 ? (g.ny + ry - 1) / ry : 1, (g.nvel + BS - 1) / BS);
-  k_march<R, D, FLUX, TX, BS><<<grid, BS, 0, st>>>(s, dt, ry);
+  const int smem = sizeof(R) == 4 && D == 2 ? MarchStage<TX>::BYTES : 0;
+  k_march<R, D, FLUX, TX, BS><<<grid, BS, smem, st>>>(s, dt, ry);
 }
 
 // FP32: the autotuned shapes (TX 2 or 4 columns, 64 or 128 threads);
