@@ -332,6 +332,338 @@ __global__ void __launch_bounds__(128) k_mom(DevState s) {
   }
 }
 
+// Pass A, FP32 form: the stencil window of a CTA segment (4 warps x TS faces
+// along one line) is streamed through shared memory in chunks of MOM_VC
+// velocities by bulk async copies, MOM_P chunks in flight, so the DRAM
+// latency is covered by the copies already issued instead of by registers.
+// Each warp then reads its TS+4 window cells from shared memory, lanes over
+// velocities, exactly as the register form does.
+constexpr int MOM_VC = 128;  // velocities per staged chunk
+constexpr int MOM_P = 3;     // chunks in flight
+template <int TS>
+struct MomStage {
+  static constexpr int NF = 4 * TS;     // faces per CTA segment
+  static constexpr int NWIN = NF + 4;   // window cells p0-2 .. p0+NF+1
+  static constexpr int FLOATS = (2 * NWIN + 3) * MOM_VC;  // [cell][h|b][v], then u, v, w
+  static constexpr int BYTES = MOM_P * FLOATS * 4 + 8 * MOM_P;
+};
+
+template <int D, int FLUX, int TS, bool SHAK, int DIR>
+__global__ void __launch_bounds__(128) k_mom_st(DevState s) {
+  using R = float;
+  using SL = MomStage<TS>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* stg = (float*)smem;
+  unsigned long long* bars = (unsigned long long*)(smem + MOM_P * SL::FLOATS * 4);
+  const Geo& g = s.g;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int n = DIR == 0 ? g.nx : g.ny;  // cells along the line
+  const int ng = DIR == 0 ? g.ngx : g.ngy;
+  const int nseg = (n + SL::NF - 1) / SL::NF;
+  const int line = blockIdx.x / nseg, sgi = blockIdx.x - line * nseg;
+  const int p0 = sgi * SL::NF;      // first face of the CTA segment
+  const int p0w = p0 + wid * TS;    // first face of this warp
+  const int ncell = max(0, min(TS, n - p0w));
+  const int nf = ncell > 0 ? ncell + (p0w + ncell == n ? 1 : 0) : 0;  // faces p0w .. p0w+nf-1
+  const int vs = g.vstride;
+  const double dd = DIR == 0 ? g.dx : g.dy;
+  const R epsd = R(1.e-7 * dd);
+  const int nchunk = (g.nvel + MOM_VC - 1) / MOM_VC;
+
+  // window cell w of the CTA (p = p0 - 2 + w): existence and cell index
+  auto win_cell = [&](int w, bool& e) {
+    const int p = p0 - 2 + w;
+    e = p >= -ng && p < n + ng;
+    return DIR == 0 ? cell_index(g, p, line) : cell_index(g, line, p);
+  };
+  int nexist = 0;
+  for (int w = 0; w < SL::NWIN; ++w) {
+    bool e;
+    win_cell(w, e);
+    nexist += e;
+  }
+  // cells outside the grid (incl. ghosts) read as zero: clear their slots once
+  if (nexist < SL::NWIN) {
+    for (int i = threadIdx.x; i < MOM_P * 2 * SL::NWIN; i += blockDim.x) {
+      const int st = i / (2 * SL::NWIN), r = i - st * 2 * SL::NWIN;
+      bool e;
+      win_cell(r >> 1, e);
+      if (!e)
+        for (int k = 0; k < MOM_VC; ++k) stg[st * SL::FLOATS + r * MOM_VC + k] = 0.f;
+    }
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < MOM_P; ++k) mbar_init(&bars[k], 1);
+  }
+  fence_async_smem();
+  __syncthreads();
+
+  const R* __restrict__ H = (const R*)s.h[s.cur];
+  const R* __restrict__ Bq = (const R*)s.b[s.cur];
+  auto issue = [&](int k) {  // warp 0: chunk k into stage k % MOM_P
+    float* S = stg + (k % MOM_P) * SL::FLOATS;
+    unsigned long long* bar = &bars[k % MOM_P];
+    const int v0 = k * MOM_VC;
+    const unsigned cb = (unsigned)min(MOM_VC, vs - v0) * 4u;  // a multiple of 16
+    if (lane == 0) mbar_expect(bar, cb * (2 * nexist + 3));
+    __syncwarp();
+    for (int i = lane; i < 2 * SL::NWIN + 3; i += 32) {
+      if (i < 2 * SL::NWIN) {
+        bool e;
+        const int c = win_cell(i >> 1, e);
+        if (!e) continue;
+        const R* src = ((i & 1) ? Bq : H) + (long)c * vs + v0;
+        bulk_g2s(S + i * MOM_VC, src, cb, bar);
+      } else {
+        const int t = i - 2 * SL::NWIN;
+        bulk_g2s(S + i * MOM_VC, vtab<R>(s, t) + v0, cb, bar);
+      }
+    }
+  };
+  if (wid == 0)
+    for (int k = 0; k < MOM_P && k < nchunk; ++k) issue(k);
+
+  // this warp's faces and window (wl = 0 .. TS+3 <-> CTA window cell wid*TS + wl)
+  int rule[TS + 4];
+#pragma unroll
+  for (int w = 0; w < TS + 4; ++w) rule[w] = slope_rule(g, DIR, p0w - 2 + w);
+  int fidx[TS + 1];
+  bool act[TS + 1];
+  R t3[TS + 1], t4[TS + 1];
+#pragma unroll
+  for (int f = 0; f < TS + 1; ++f) {
+    int p = p0w + f;
+    fidx[f] = DIR == 0 ? line * (g.nx + 1) + p : s.nface_x + p * g.nx + line;
+    act[f] = f < nf && s.kind[fidx[f]] == 1;
+    t3[f] = R(0);
+    t4[f] = R(0);
+    if (act[f]) {
+      const FaceParam& P = s.fp[fidx[f]];
+      t3[f] = R(P.tr[0]);
+      t4[f] = R(P.tr[1] / dd);
+    }
+  }
+  R oU[TS], oV[TS];
+  if (SHAK) {
+#pragma unroll
+    for (int c = 0; c < TS; ++c) {
+      bool e;
+      const int cc = win_cell(wid * TS + c + 2, e);
+      oU[c] = e ? R(s.prim[(long)cc * 4 + 1]) : R(0);
+      oV[c] = (e && D == 2) ? R(s.prim[(long)cc * 4 + 2]) : R(0);
+    }
+  }
+  BAcc<R> acc[TS + 1][4];
+  BAcc<R> qa[SHAK ? TS : 1][2];
+#pragma unroll
+  for (int f = 0; f < TS + 1; ++f)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[f][k].init();
+#pragma unroll
+  for (int c = 0; c < (SHAK ? TS : 1); ++c) {
+    qa[c][0].init();
+    qa[c][1].init();
+  }
+
+  bool fast = g.interp == 2 && p0w >= 2 && p0w + TS <= n - 2 && nf == TS;
+#pragma unroll
+  for (int f = 0; f < TS; ++f) fast = fast && act[f];
+  // One velocity of this warp's faces.  SG 0: upwind side per lane; SG 1 / 2:
+  // every lane of the warp has un >= 0 / un < 0, so only the upwind cells'
+  // slopes are formed and only the window cells they touch are read.
+  auto one = [&](const float* S, const float* Sw, int vl, auto fast_tag, auto sign_tag) {
+    constexpr bool FAST = decltype(fast_tag)::value;
+    constexpr int SG = decltype(sign_tag)::value;
+    const R u = S[2 * SL::NWIN * MOM_VC + vl];
+    const R vv = D == 2 ? S[(2 * SL::NWIN + 1) * MOM_VC + vl] : R(0);
+    const R om = S[(2 * SL::NWIN + 2) * MOM_VC + vl];
+    const R un = DIR == 0 ? u : vv;
+    const R ut = DIR == 0 ? vv : -u;
+    constexpr int WLO = SG == 2 ? 1 : 0, WHI = SG == 1 ? TS + 1 : (SG == 2 ? TS + 2 : TS + 3);
+    R hx[TS + 4], bx[TS + 4];
+#pragma unroll
+    for (int w = WLO; w <= WHI; ++w) {
+      hx[w] = Sw[(2 * w) * MOM_VC + vl];
+      bx[w] = Sw[(2 * w + 1) * MOM_VC + vl];
+    }
+    const bool pos = SG == 0 ? un >= R(0) : SG == 1;
+    const R c2 = un * un + ut * ut;
+    const R un2 = un * un;
+#pragma unroll
+    for (int f = 0; f < TS + 1; ++f) {
+      if (FAST ? f == TS : !act[f]) continue;
+      R hu, bu, su, sb;
+      if (SG == 1 || (SG == 0 && FAST)) {
+        // upwind cell w = f + 1 (pos) or f + 2 (neg), its slope from three values
+        const int w = SG == 1 ? f + 1 : f + 2;
+        if (SG == 1) {
+          hu = hx[w];
+          bu = bx[w];
+          su = slope<FAST>(rule[w], hx[w - 1], hx[w], hx[w + 1], epsd);
+          sb = slope<FAST>(rule[w], bx[w - 1], bx[w], bx[w + 1], epsd);
+        } else {
+          const R hm = pos ? hx[f] : hx[f + 1], h0 = pos ? hx[f + 1] : hx[f + 2],
+                  hp = pos ? hx[f + 2] : hx[f + 3];
+          const R bm = pos ? bx[f] : bx[f + 1], b0 = pos ? bx[f + 1] : bx[f + 2],
+                  bp = pos ? bx[f + 2] : bx[f + 3];
+          hu = h0;
+          bu = b0;
+          su = slope<FAST>(1, hm, h0, hp, epsd);
+          sb = slope<FAST>(1, bm, b0, bp, epsd);
+        }
+      } else if (SG == 2) {
+        const int w = f + 2;
+        hu = hx[w];
+        bu = bx[w];
+        su = slope<FAST>(rule[w], hx[w - 1], hx[w], hx[w + 1], epsd);
+        sb = slope<FAST>(rule[w], bx[w - 1], bx[w], bx[w + 1], epsd);
+      } else {
+        // boundary segment, mixed signs: both candidate cells' rules apply
+        const int wl = f + 1, wr = f + 2;
+        const R sl = slope<FAST>(rule[wl], hx[wl - 1], hx[wl], hx[wl + 1], epsd);
+        const R sr = slope<FAST>(rule[wr], hx[wr - 1], hx[wr], hx[wr + 1], epsd);
+        const R tl = slope<FAST>(rule[wl], bx[wl - 1], bx[wl], bx[wl + 1], epsd);
+        const R tr = slope<FAST>(rule[wr], bx[wr - 1], bx[wr], bx[wr + 1], epsd);
+        hu = pos ? hx[wl] : hx[wr];
+        bu = pos ? bx[wl] : bx[wr];
+        su = pos ? sl : sr;
+        sb = pos ? tl : tr;
+      }
+      R hf = hu + (pos ? R(0.5) : R(-0.5)) * su;
+      R bf = bu + (pos ? R(0.5) : R(-0.5)) * sb;
+      R Th = t3[f] * un * hf - t4[f] * un2 * su;
+      R Tb = t3[f] * un * bf - t4[f] * un2 * sb;
+      R wT = om * Th;
+      acc[f][0].add(wT);
+      acc[f][1].add(wT * un);
+      if (D == 2) acc[f][2].add(wT * ut);
+      acc[f][3].add(wT * c2 + om * Tb);
+    }
+    if (SHAK) {
+#pragma unroll
+      for (int c = 0; c < TS; ++c) {
+        R cu = u - oU[c];
+        R cv = vv - oV[c];
+        R c2o = cu * cu + cv * cv;
+        R hc = hx[c + 2], bc = bx[c + 2];
+        qa[c][0].add(om * cu * c2o * hc + om * cu * bc);
+        if (D == 2) qa[c][1].add(om * cv * c2o * hc + om * cv * bc);
+      }
+    }
+  };
+  // one staged chunk of this warp's faces (FAST: interior van Leer window)
+  auto body = [&](const float* S, int k, auto fast_tag) {
+    constexpr bool FAST = decltype(fast_tag)::value;
+    using I0 = std::integral_constant<int, 0>;
+    const float* Sw = S + wid * TS * 2 * MOM_VC;  // this warp's window cell 0
+    // iterations holding at least one velocity: the same count on every lane,
+    // so the whole warp reaches each ballot
+    const int mmax = min(MOM_VC / 32, (g.nvel - k * MOM_VC + 31) / 32);
+#pragma unroll
+    for (int m = 0; m < MOM_VC / 32; ++m) {
+      if (m >= mmax) break;
+      const int vl = m * 32 + lane;
+      const bool valid = k * MOM_VC + vl < g.nvel;
+      if (FAST) {
+        const R un = S[(2 * SL::NWIN + (DIR == 0 ? 0 : 1)) * MOM_VC + vl];
+        const unsigned ap = __ballot_sync(0xffffffffu, !valid || un >= R(0));
+        const unsigned an = __ballot_sync(0xffffffffu, !valid || un < R(0));
+        if (valid) {
+          if (ap == 0xffffffffu) one(S, Sw, vl, fast_tag, std::integral_constant<int, 1>{});
+          else if (an == 0xffffffffu) one(S, Sw, vl, fast_tag, std::integral_constant<int, 2>{});
+          else one(S, Sw, vl, fast_tag, I0{});
+        }
+      } else if (valid) {
+        one(S, Sw, vl, fast_tag, I0{});
+      }
+    }
+    // flush the FP32 partials (8 velocities per lane) into the compensated sums
+    if (k & 1) {
+#pragma unroll
+      for (int f = 0; f < TS + 1; ++f)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[f][q].flush();
+#pragma unroll
+      for (int c = 0; c < (SHAK ? TS : 1); ++c) {
+        qa[c][0].flush();
+        qa[c][1].flush();
+      }
+    }
+  };
+  int failed = -1;
+  for (int k = 0; k < nchunk; ++k) {
+    const bool ok = mbar_wait(&bars[k % MOM_P], (k / MOM_P) & 1);
+    if (__syncthreads_or(!ok)) {  // CTA-uniform
+      failed = k;
+      if (threadIdx.x == 0) atomicOr(s.status, 2);
+      break;
+    }
+    const float* S = stg + (k % MOM_P) * SL::FLOATS;
+    if (nf > 0) {
+      if (fast) body(S, k, std::true_type{});
+      else body(S, k, std::false_type{});
+    }
+    // stage k % MOM_P is free once every warp is done with it
+    __syncthreads();
+    if (wid == 0 && k + MOM_P < nchunk) {
+      if (lane == 0) fence_async_smem();
+      __syncwarp();
+      issue(k + MOM_P);
+    }
+  }
+  if (failed >= 0) {
+    // copies issued for chunks failed .. failed + MOM_P - 1 may still land
+    for (int k = failed; k < nchunk && k < failed + MOM_P; ++k)
+      mbar_wait(&bars[k % MOM_P], (k / MOM_P) & 1);
+    return;
+  }
+#pragma unroll
+  for (int f = 0; f < TS + 1; ++f) {
+    if (!act[f]) continue;
+    double S0 = acc[f][0].total(), S1 = acc[f][1].total();
+    double S2 = D == 2 ? acc[f][2].total() : 0.0;
+    double S3 = acc[f][3].total();
+    if (lane == 0) {
+      const FaceParam& P = s.fp[fidx[f]];
+      double fl[4];
+      fl[0] = P.fwa[0] + S0;
+      fl[1] = P.fwa[1] + S1;
+      if (D == 1) {
+        fl[2] = P.fwa[2] + 0.5 * S3;
+        fl[3] = 0.0;
+      } else {
+        fl[2] = P.fwa[2] + S2;
+        fl[3] = P.fwa[3] + 0.5 * S3;
+      }
+      double* out = s.fw + (long)fidx[f] * 4;
+      if (DIR == 1) {  // global_frame with n = (0, 1)
+        out[0] = fl[0];
+        out[1] = -fl[2];
+        out[2] = fl[1];
+        out[3] = fl[3];
+      } else {
+        out[0] = fl[0];
+        out[1] = fl[1];
+        out[2] = fl[2];
+        out[3] = fl[3];
+      }
+    }
+  }
+  if (SHAK) {
+#pragma unroll
+    for (int c = 0; c < TS; ++c) {
+      double q0 = qa[c][0].total();
+      double q1 = D == 2 ? qa[c][1].total() : 0.0;
+      if (lane == 0 && c < ncell) {
+        bool e;
+        const long cc = win_cell(wid * TS + c + 2, e);
+        s.q[cc * 2 + 0] = 0.5 * q0;
+        s.q[cc * 2 + 1] = 0.5 * q1;
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------------ pass B
 
 // Per-face evaluation state of one thread (one velocity, static upwind side).
@@ -949,9 +1281,35 @@ constexpr int RY_MARCH = 32;
 
 static inline unsigned nblk2(long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// FP32 pass A: one CTA (4 warps) per segment of 4 TS faces along a line;
+// its dynamic shared memory exceeds the default 48 KB for TS = 4, so the
+// limit is raised once per device.
+template <int D, int FLUX, int TS, bool SHAK, int DIR>
+static void mom_st_go(DevState& s, cudaStream_t st) {
+  const Geo& g = s.g;
+  using SL = MomStage<TS>;
+  const int n = DIR == 0 ? g.nx : g.ny, nlines = DIR == 0 ? g.ny : g.nx;
+  const long nblk = (long)nlines * ((n + SL::NF - 1) / SL::NF);
+  auto kern = k_mom_st<D, FLUX, TS, SHAK, DIR>;
+  static bool raised[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (SL::BYTES > 48 * 1024 && dev >= 0 && dev < 64 && !raised[dev]) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SL::BYTES);
+    raised[dev] = true;
+  }
+  kern<<<(unsigned)nblk, 128, SL::BYTES, st>>>(s);
+}
+
 template <typename R, int D, int FLUX, int TS>
 static int mom_go(DevState& s, cudaStream_t st) {
   const Geo& g = s.g;
+  if constexpr (sizeof(R) == 4) {
+    if (s.coll == COLL_SHAKHOV) mom_st_go<D, FLUX, TS, true, 0>(s, st);
+    else mom_st_go<D, FLUX, TS, false, 0>(s, st);
+    if (D == 2) mom_st_go<D, FLUX, TS, false, 1>(s, st);
+    return D == 2 ? 2 : 1;
+  }
   int n = 0;
   long wx = (long)((g.nx + TS - 1) / TS) * g.ny;
   if (s.coll == COLL_SHAKHOV)
