@@ -18,6 +18,7 @@
 // and written once.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <type_traits>
@@ -30,9 +31,16 @@ namespace kb {
 // van Leer slope times dx, from raw differences: dx * vanleer(a/dx, b/dx)
 // = (a|b| + b|a|) / (|a| + |b| + 1e-7 dx) (src/Reconstruction/recon_limiter.jl:17-19);
 // rules 2 / 3 are the one-sided reconstruct2! differences.
+// x / y as one reciprocal and one multiply, subnormal inputs and results
+// flushed to zero (the non-flushing form adds range fix-ups to every call).
+__device__ __forceinline__ float fdiv_ftz(float x, float y) {
+  float r;
+  asm("div.approx.ftz.f32 %0, %1, %2;" : "=f"(r) : "f"(x), "f"(y));
+  return r;
+}
 __device__ __forceinline__ float vl_diff(int rule, float qm, float q0, float qp, float epsd) {
   float a = q0 - qm, b = qp - q0;
-  if (rule == 1) return __fdividef(a * fabsf(b) + b * fabsf(a), fabsf(a) + fabsf(b) + epsd);
+  if (rule == 1) return fdiv_ftz(a * fabsf(b) + b * fabsf(a), fabsf(a) + fabsf(b) + epsd);
   if (rule == 2) return b;
   if (rule == 3) return a;
   return 0.f;
@@ -85,6 +93,9 @@ __device__ __forceinline__ bool mbar_try(unsigned long long* bar, unsigned parit
       : "r"(smem_u32(bar)), "r"(parity)
       : "memory");
   return ok != 0;
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 // true once the phase with this parity completed; false after KB_WAIT_NS.
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
@@ -336,8 +347,10 @@ __global__ void __launch_bounds__(128) k_mom(DevState s) {
 // along one line) is streamed through shared memory in chunks of MOM_VC
 // velocities by bulk async copies, MOM_P chunks in flight, so the DRAM
 // latency is covered by the copies already issued instead of by registers.
-// Each warp then reads its TS+4 window cells from shared memory, lanes over
-// velocities, exactly as the register form does.
+// A fifth (producer) warp issues the copies; each consumer warp reads its
+// TS+4 window cells from shared memory, lanes over velocities, and releases a
+// stage through its own mbarrier arrival, so consumer warps never wait on
+// one another.
 constexpr int MOM_VC = 128;  // velocities per staged chunk
 constexpr int MOM_P = 3;     // chunks in flight
 template <int TS>
@@ -345,16 +358,21 @@ struct MomStage {
   static constexpr int NF = 4 * TS;     // faces per CTA segment
   static constexpr int NWIN = NF + 4;   // window cells p0-2 .. p0+NF+1
   static constexpr int FLOATS = (2 * NWIN + 3) * MOM_VC;  // [cell][h|b][v], then u, v, w
-  static constexpr int BYTES = MOM_P * FLOATS * 4 + 8 * MOM_P;
+  // stages, then full[MOM_P], empty[MOM_P] mbarriers and a failure flag
+  static constexpr int BYTES = MOM_P * FLOATS * 4 + 16 * MOM_P + 16;
 };
+constexpr int MOM_THREADS = 160;  // 4 consumer warps + 1 producer warp
 
 template <int D, int FLUX, int TS, bool SHAK, int DIR>
-__global__ void __launch_bounds__(128) k_mom_st(DevState s) {
+__global__ void __launch_bounds__(MOM_THREADS) k_mom_st(DevState s) {
   using R = float;
   using SL = MomStage<TS>;
   extern __shared__ __align__(16) unsigned char smem[];
   float* stg = (float*)smem;
-  unsigned long long* bars = (unsigned long long*)(smem + MOM_P * SL::FLOATS * 4);
+  unsigned long long* full = (unsigned long long*)(smem + MOM_P * SL::FLOATS * 4);
+  unsigned long long* empty = full + MOM_P;
+  int* bad = (int*)(empty + MOM_P);
+  constexpr int PRODUCER = 4;
   const Geo& g = s.g;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int n = DIR == 0 ? g.nx : g.ny;  // cells along the line
@@ -363,7 +381,7 @@ __global__ void __launch_bounds__(128) k_mom_st(DevState s) {
   const int line = blockIdx.x / nseg, sgi = blockIdx.x - line * nseg;
   const int p0 = sgi * SL::NF;      // first face of the CTA segment
   const int p0w = p0 + wid * TS;    // first face of this warp
-  const int ncell = max(0, min(TS, n - p0w));
+  const int ncell = wid == PRODUCER ? 0 : max(0, min(TS, n - p0w));
   const int nf = ncell > 0 ? ncell + (p0w + ncell == n ? 1 : 0) : 0;  // faces p0w .. p0w+nf-1
   const int vs = g.vstride;
   const double dd = DIR == 0 ? g.dx : g.dy;
@@ -393,16 +411,20 @@ __global__ void __launch_bounds__(128) k_mom_st(DevState s) {
     }
   }
   if (threadIdx.x == 0) {
-    for (int k = 0; k < MOM_P; ++k) mbar_init(&bars[k], 1);
+    for (int k = 0; k < MOM_P; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], PRODUCER);
+    }
+    *bad = 0;
   }
   fence_async_smem();
   __syncthreads();
 
   const R* __restrict__ H = (const R*)s.h[s.cur];
   const R* __restrict__ Bq = (const R*)s.b[s.cur];
-  auto issue = [&](int k) {  // warp 0: chunk k into stage k % MOM_P
+  auto issue = [&](int k) {  // producer warp: chunk k into stage k % MOM_P
     float* S = stg + (k % MOM_P) * SL::FLOATS;
-    unsigned long long* bar = &bars[k % MOM_P];
+    unsigned long long* bar = &full[k % MOM_P];
     const int v0 = k * MOM_VC;
     const unsigned cb = (unsigned)min(MOM_VC, vs - v0) * 4u;  // a multiple of 16
     if (lane == 0) mbar_expect(bar, cb * (2 * nexist + 3));
@@ -420,8 +442,6 @@ __global__ void __launch_bounds__(128) k_mom_st(DevState s) {
       }
     }
   };
-  if (wid == 0)
-    for (int k = 0; k < MOM_P && k < nchunk; ++k) issue(k);
 
   // this warp's faces and window (wl = 0 .. TS+3 <-> CTA window cell wid*TS + wl)
   int rule[TS + 4];
@@ -590,31 +610,57 @@ __global__ void __launch_bounds__(128) k_mom_st(DevState s) {
       }
     }
   };
-  int failed = -1;
-  for (int k = 0; k < nchunk; ++k) {
-    const bool ok = mbar_wait(&bars[k % MOM_P], (k / MOM_P) & 1);
-    if (__syncthreads_or(!ok)) {  // CTA-uniform
-      failed = k;
-      if (threadIdx.x == 0) atomicOr(s.status, 2);
-      break;
+  volatile int* vbad = bad;
+  if (wid == PRODUCER) {
+    for (int k = 0; k < nchunk; ++k) {
+      if (k >= MOM_P) {
+        // stage k % MOM_P is free once all consumer warps released chunk k - MOM_P
+        int ok = 1, stop = 0;
+        if (lane == 0) {
+          ok = mbar_wait(&empty[k % MOM_P], ((k / MOM_P) - 1) & 1);
+          stop = *vbad;
+        }
+        ok = __shfl_sync(0xffffffffu, ok, 0);  // one decision for the whole warp
+        stop = __shfl_sync(0xffffffffu, stop, 0);
+        if (!ok || stop) {  // stop issuing: consumers then skip their waits
+          if (lane == 0 && !ok) {
+            atomicOr(bad, 1);
+            atomicOr(s.status, 2);
+          }
+          break;
+        }
+        if (lane == 0) fence_async_smem();
+        __syncwarp();
+      }
+      issue(k);
     }
-    const float* S = stg + (k % MOM_P) * SL::FLOATS;
-    if (nf > 0) {
-      if (fast) body(S, k, std::true_type{});
-      else body(S, k, std::false_type{});
-    }
-    // stage k % MOM_P is free once every warp is done with it
-    __syncthreads();
-    if (wid == 0 && k + MOM_P < nchunk) {
-      if (lane == 0) fence_async_smem();
+  } else {
+    for (int k = 0; k < nchunk; ++k) {
+      bool ok = *vbad == 0;
+      if (ok) {
+        ok = mbar_wait(&full[k % MOM_P], (k / MOM_P) & 1);
+        if (!ok) {
+          atomicOr(bad, 1);
+          atomicOr(s.status, 2);
+        }
+      }
+      ok = __all_sync(0xffffffffu, ok);
+      const float* S = stg + (k % MOM_P) * SL::FLOATS;
+      if (ok && nf > 0) {
+        if (fast) body(S, k, std::true_type{});
+        else body(S, k, std::false_type{});
+      }
       __syncwarp();
-      issue(k + MOM_P);
+      if (lane == 0) mbar_arrive(&empty[k % MOM_P]);
     }
   }
-  if (failed >= 0) {
-    // copies issued for chunks failed .. failed + MOM_P - 1 may still land
-    for (int k = failed; k < nchunk && k < failed + MOM_P; ++k)
-      mbar_wait(&bars[k % MOM_P], (k / MOM_P) & 1);
+  __syncthreads();
+  if (*vbad) {
+    // copies of the last chunks issued may still land: wait (bounded) for
+    // each stage's latest phase before the shared memory is released
+    if (threadIdx.x == 0)
+      for (int k = max(0, nchunk - MOM_P); k < nchunk; ++k)
+        mbar_wait(&full[k % MOM_P], (k / MOM_P) & 1);
     return;
   }
 #pragma unroll
@@ -933,7 +979,7 @@ static_assert(sizeof(FaceCoef32) % 16 == 0 && sizeof(CellCoef32) % 16 == 0,
 // the last velocity compute on a clamped velocity and store nothing, so every
 // thread reaches every barrier.
 template <typename R, int D, int FLUX, int TX, int BS>
-__global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march(DevState s, double dt, int RY) {
+__global__ void __launch_bounds__(BS, (sizeof(R) == 4 && TX < 4 ? 384 : 256) / BS) k_march(DevState s, double dt, int RY) {
   constexpr bool STAGE = sizeof(R) == 4 && D == 2;
   using SL = MarchStage<TX>;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1273,6 +1319,264 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 ? 384 : 256) / BS) k_march
   }
 }
 
+// ------------------------------------------------- pass B, FP32 2D (TMA rows)
+
+// 3D tiled tensor load (TMA) of one box into shared memory, completed on an
+// mbarrier.  Coordinates outside the tensor read as zero.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1,
+                                            int c2, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2),
+      "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory ring of the 2D FP32 update: one slot per grid row of the
+// strip, holding the row's h and b boxes (TX+4 columns incl. the 2-cell x
+// halo on each side, M3_BS velocities; [column][velocity]) and the row's
+// coefficient blocks (x faces [TX+1], y faces above the row [TX], cells [TX]).
+constexpr int M3_BS = 128;  // velocities (threads) per CTA
+template <int TX, int NS>
+struct M3Layout {
+  static constexpr int W = TX + 4;
+  static constexpr int BOX = W * M3_BS * 4;
+  static constexpr int XF = 2 * BOX;
+  static constexpr int YF = XF + (TX + 1) * (int)sizeof(FaceCoef32);
+  static constexpr int CC = YF + TX * (int)sizeof(FaceCoef32);
+  static constexpr int SLOT = (CC + TX * (int)sizeof(CellCoef32) + 127) / 128 * 128;
+  // slots, full[NS], empty[NS], failure flag
+  static constexpr int BYTES = NS * SLOT + 16 * NS + 16;
+};
+
+// Pass B in the 2D FP32 form.  Thread = one velocity; CTA = 128 velocities x
+// a strip of TX columns x RY rows, marching up the rows.  Rows arrive by TMA
+// (h and b boxes) plus bulk copies (coefficients) into a ring of NS slots,
+// NS - 5 rows ahead of the 4-row stencil window; thread 0 refills a slot once
+// every warp has released the row it held (per-slot "empty" mbarriers), so
+// warps never wait on one another and the window costs no registers.  Each
+// x face and y face is evaluated once per velocity and feeds both neighbours.
+template <int FLUX, int TX, int NS>
+__global__ void __launch_bounds__(M3_BS) k_march3(const __grid_constant__ CUtensorMap tmh,
+                                                  const __grid_constant__ CUtensorMap tmb,
+                                                  DevState s, int RY) {
+  static_assert(NS >= 6, "the ring holds the 4-row window plus at least one row ahead");
+  using L = M3Layout<TX, NS>;
+  constexpr int D = 2;
+  extern __shared__ __align__(1024) unsigned char smem3[];
+  unsigned long long* full = (unsigned long long*)(smem3 + NS * L::SLOT);
+  unsigned long long* empty = full + NS;
+  int* bad = (int*)(empty + NS);
+  volatile int* vbad = bad;
+  const Geo& g = s.g;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int v0 = blockIdx.x * M3_BS;
+  const int vraw = v0 + tid;
+  const bool vok = vraw < g.nvel;
+  const int v = vok ? vraw : g.nvel - 1;
+  const int i0 = blockIdx.y * TX;
+  const int ncol = min(TX, g.nx - i0);
+  const int j0 = blockIdx.z * RY;
+  const int j1 = min(g.ny, j0 + RY);
+  const int q0 = j0 - 2;    // first staged row
+  const int qend = j1 + 1;  // last staged row
+  const int vs = g.vstride;
+  float* __restrict__ Ho = (float*)s.h[s.cur ^ 1];
+  float* __restrict__ Bo = (float*)s.b[s.cur ^ 1];
+
+  auto slot = [&](int q) -> const unsigned char* { return smem3 + ((q - q0) % NS) * L::SLOT; };
+  auto issue = [&](int q) {  // thread 0: grid row q and its coefficient blocks
+    const int r = q - q0;
+    unsigned char* S = smem3 + (r % NS) * L::SLOT;
+    unsigned long long* bar = &full[r % NS];
+    const bool hy = q >= j0 - 1 && q <= j1 - 1, hx = q >= j0 && q <= j1 - 1;
+    const unsigned xb = (ncol + 1) * sizeof(FaceCoef32), yb = ncol * sizeof(FaceCoef32),
+                   cb = ncol * sizeof(CellCoef32);
+    mbar_expect(bar, 2 * L::BOX + (hy ? yb : 0u) + (hx ? xb + cb : 0u));
+    tma_load_3d(S, &tmh, v0, i0 - 2 + g.ngx, q + g.ngy, bar);
+    tma_load_3d(S + L::BOX, &tmb, v0, i0 - 2 + g.ngx, q + g.ngy, bar);
+    if (hx) {
+      bulk_g2s(S + L::XF, s.fc + (long)q * (g.nx + 1) + i0, xb, bar);
+      bulk_g2s(S + L::CC, s.cc + cell_index(g, i0, q), cb, bar);
+    }
+    if (hy) bulk_g2s(S + L::YF, s.fc + s.nface_x + (long)(q + 1) * g.nx + i0, yb, bar);
+  };
+  // every thread waits for row q itself; after any timeout the copies stop
+  // and the remaining waits are skipped (the status word reports it)
+  auto await_row = [&](int q) {
+    if (*vbad) return;
+    const int r = q - q0;
+    if (!mbar_wait(&full[r % NS], (r / NS) & 1)) {
+      atomicOr(bad, 1);
+      atomicOr(s.status, 2);
+    }
+  };
+  auto release_row = [&](int q) {  // this warp no longer reads row q
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[(q - q0) % NS]);
+  };
+
+  int issued = 0;  // rows issued so far (thread 0)
+  if (tid == 0) {
+    for (int k = 0; k < NS; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], M3_BS / 32);
+    }
+    *bad = 0;
+    fence_async_smem();
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int q = q0; q <= qend && q < q0 + NS; ++q, ++issued) issue(q);
+
+  const float u = s.uf[v], vv = s.vf[v];
+  Mono<float> MX, MY;
+  MX.set(u, vv);
+  MY.set(vv, -u);
+  const bool px = u >= 0.f, py = vv >= 0.f;
+  const float sx = px ? 0.5f : -0.5f, sy = py ? 0.5f : -0.5f;
+  const float epsx = float(1.e-7 * g.dx), epsy = float(1.e-7 * g.dy);
+  const bool shak = s.coll == COLL_SHAKHOV;
+  const int shx = px ? 0 : 1;  // x window shift: face f's upwind cell is window k = f + 1
+  int rxs[TX + 3];             // x slope rule of window k (column k + shx)
+#pragma unroll
+  for (int k = 0; k < TX + 3; ++k) rxs[k] = slope_rule(g, 0, i0 - 2 + k + shx);
+  const long rowstride = (long)g.nxt * vs;
+
+  auto Hv = [&](const unsigned char* S, int w) { return ((const float*)S)[w * M3_BS + tid]; };
+  auto Bv = [&](const unsigned char* S, int w) {
+    return ((const float*)(S + L::BOX))[w * M3_BS + tid];
+  };
+  // flux through the y face of column c between rows ql and ql + 1
+  auto yface = [&](int ql, int c, auto fast_tag, float& fh, float& fb) {
+    constexpr bool FAST = decltype(fast_tag)::value;
+    fh = 0.f;
+    fb = 0.f;
+    if (!FAST && c >= ncol) return;
+    const int qa = py ? ql - 1 : ql;  // stencil rows qa .. qa + 2, upwind cell qa + 1
+    const unsigned char* S0 = slot(qa);
+    const unsigned char* S1 = slot(qa + 1);
+    const unsigned char* S2 = slot(qa + 2);
+    const int w = c + 2;
+    const float h0 = Hv(S1, w), b0 = Bv(S1, w);
+    const int rule = FAST ? 1 : slope_rule(g, 1, qa + 1);
+    const float su = vl_diff(rule, Hv(S0, w), h0, Hv(S2, w), epsy);
+    const float sb = vl_diff(rule, Bv(S0, w), b0, Bv(S2, w), epsy);
+    FEv<float> e;
+    const FaceCoef32* yc = (const FaceCoef32*)(slot(ql) + L::YF);
+    face_load<FAST>(e, s, s.nface_x + (ql + 1) * g.nx + i0 + c, yc[c], py);
+    float hc = 0.f, bc = 0.f;
+    if (!FAST) {  // interior cell of a wall face
+      const unsigned char* Si = slot(ql + 1 == 0 ? ql + 1 : ql);
+      hc = Hv(Si, w);
+      bc = Bv(Si, w);
+    }
+    eval_face<D, FLUX, FAST>(e, MY, sy, h0, b0, su, sb, hc, bc, 0.0, fh, fb);
+  };
+
+  float fyh[TX], fyb[TX];  // flux through the y faces below the current row
+  await_row(q0);
+  await_row(q0 + 1);
+  await_row(q0 + 2);
+  await_row(q0 + 3);
+  {
+    const bool fast = g.interp == 2 && i0 >= 2 && i0 + TX <= g.nx - 2 && j0 >= 2 && j0 <= g.ny - 2;
+#pragma unroll
+    for (int c = 0; c < TX; ++c) {
+      if (fast) yface(j0 - 1, c, std::true_type{}, fyh[c], fyb[c]);
+      else yface(j0 - 1, c, std::false_type{}, fyh[c], fyb[c]);
+    }
+  }
+  release_row(q0);
+
+  auto row = [&](int j, auto fast_tag) {
+    constexpr bool FAST = decltype(fast_tag)::value;
+    const unsigned char* Sj = slot(j);
+    // y faces above row j
+    float fyh2[TX], fyb2[TX];
+#pragma unroll
+    for (int c = 0; c < TX; ++c) yface(j, c, fast_tag, fyh2[c], fyb2[c]);
+    // x window of row j, shifted to the upwind side, and the x faces
+    float xs[TX + 3], xt[TX + 3];
+#pragma unroll
+    for (int k = 0; k < TX + 3; ++k) {
+      xs[k] = Hv(Sj, k + shx);
+      xt[k] = Bv(Sj, k + shx);
+    }
+    const FaceCoef32* xc = (const FaceCoef32*)(Sj + L::XF);
+    float fxh[TX + 1], fxb[TX + 1];
+#pragma unroll
+    for (int f = 0; f <= TX; ++f) {
+      fxh[f] = 0.f;
+      fxb[f] = 0.f;
+      if (!FAST && f > ncol) continue;
+      const float su = slope<FAST>(rxs[f + 1], xs[f], xs[f + 1], xs[f + 2], epsx);
+      const float sb = slope<FAST>(rxs[f + 1], xt[f], xt[f + 1], xt[f + 2], epsx);
+      FEv<float> e;
+      const int fi = i0 + f;
+      face_load<FAST>(e, s, j * (g.nx + 1) + fi, xc[f], px);
+      float hc = 0.f, bc = 0.f;
+      if (!FAST) {  // interior cell of a wall face
+        hc = Hv(Sj, fi == 0 ? f + 2 : f + 1);
+        bc = Bv(Sj, fi == 0 ? f + 2 : f + 1);
+      }
+      eval_face<D, FLUX, FAST>(e, MX, sx, xs[f + 1], xt[f + 1], su, sb, hc, bc, 0.0, fxh[f],
+                               fxb[f]);
+    }
+    // relax and store the cells of row j
+    const CellCoef32* cc = (const CellCoef32*)(Sj + L::CC);
+    const long ro = (long)(j + g.ngy) * rowstride + (long)(i0 + g.ngx) * vs + v;
+#pragma unroll
+    for (int c = 0; c < TX; ++c) {
+      if (!FAST && c >= ncol) continue;
+      const float dhh = fxh[c] - fxh[c + 1] + fyh[c] - fyh2[c];
+      const float dbb = fxb[c] - fxb[c + 1] + fyb[c] - fyb2[c];
+      float hn, bn;
+      const CellCoef32 k = cc[c];
+      relax(k, shak, u, vv, MX.c2, Hv(Sj, c + 2), Bv(Sj, c + 2), dhh, dbb, hn, bn);
+      if (vok) {
+        Ho[ro + (long)c * vs] = hn;
+        Bo[ro + (long)c * vs] = bn;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < TX; ++c) {
+      fyh[c] = fyh2[c];
+      fyb[c] = fyb2[c];
+    }
+  };
+
+  const bool fastx = g.interp == 2 && i0 >= 2 && i0 + TX <= g.nx - 2;
+  for (int j = j0; j < j1; ++j) {
+    if (tid == 0 && *vbad == 0) {
+      // refill the slot of row q - NS (released after row q - NS + 1)
+      const int q = j + NS - 3;
+      if (j > j0 && q <= qend) {
+        const int r = q - q0;
+        if (mbar_wait(&empty[r % NS], ((r - NS) / NS) & 1)) {
+          fence_async_smem();
+          issue(q);
+          ++issued;
+        } else {
+          atomicOr(bad, 1);
+          atomicOr(s.status, 2);
+        }
+      }
+    }
+    await_row(j + 2);
+    if (fastx && j >= 1 && j <= g.ny - 3) row(j, std::true_type{});
+    else row(j, std::false_type{});
+    release_row(j - 1);
+  }
+  __syncthreads();
+  if (*vbad && tid == 0) {
+    // copies of the last rows issued may still land: wait (bounded) for each
+    // slot's latest row before the shared memory is released
+    for (int r = max(0, issued - NS); r < issued; ++r) mbar_wait(&full[r % NS], (r / NS) & 1);
+  }
+}
+
 // ----------------------------------------------------------- launch helpers
 
 constexpr int TS_MOM = 4;    // faces per warp in pass A
@@ -1298,7 +1602,7 @@ static void mom_st_go(DevState& s, cudaStream_t st) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SL::BYTES);
     raised[dev] = true;
   }
-  kern<<<(unsigned)nblk, 128, SL::BYTES, st>>>(s);
+  kern<<<(unsigned)nblk, MOM_THREADS, SL::BYTES, st>>>(s);
 }
 
 template <typename R, int D, int FLUX, int TS>
@@ -1340,6 +1644,27 @@ static void march_go(DevState& s, double dt, cudaStream_t st) {
   k_march<R, D, FLUX, TX, BS><<<grid, BS, smem, st>>>(s, dt, ry);
 }
 
+// FP32 2D pass B (k_march3): the tensor maps of the current h / b buffers for
+// this strip width; the ring needs more than the default 48 KB of shared
+// memory, so the limit is raised once per device.
+template <int FLUX, int TX, int NS>
+static void march3_go(DevState& s, cudaStream_t st) {
+  const Geo& g = s.g;
+  using L = M3Layout<TX, NS>;
+  const int ry = s.tune[KB_TUNE_MARCH_RY] > 0 ? s.tune[KB_TUNE_MARCH_RY] : RY_MARCH;
+  const CUtensorMap* tm = (const CUtensorMap*)s.tmaps + ((TX == 4 ? 1 : 0) * 2 + s.cur) * 2;
+  auto kern = k_march3<FLUX, TX, NS>;
+  static bool raised[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !raised[dev]) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
+    raised[dev] = true;
+  }
+  dim3 grid((g.nvel + M3_BS - 1) / M3_BS, (g.nx + TX - 1) / TX, (g.ny + ry - 1) / ry);
+  kern<<<grid, M3_BS, L::BYTES, st>>>(tm[0], tm[1], s, ry);
+}
+
 // FP32: the autotuned shapes (TX 2 or 4 columns, 64 or 128 threads);
 // FP64: one shape (two columns keep the FP64 update free of spills).
 template <typename R, int D, int FLUX>
@@ -1349,12 +1674,18 @@ static int march_t(DevState& s, double dt, cudaStream_t st) {
   } else {
     const int tx = s.tune[KB_TUNE_MARCH_TX] > 0 ? s.tune[KB_TUNE_MARCH_TX] : TX_MARCH;
     const int bs = s.tune[KB_TUNE_MARCH_BS] > 0 ? s.tune[KB_TUNE_MARCH_BS] : 128;
-    if (tx == 2) {
-      if (bs == 64) march_go<R, D, FLUX, 2, 64>(s, dt, st);
-      else march_go<R, D, FLUX, 2, 128>(s, dt, st);
+    if constexpr (D == 2) {
+      (void)bs;
+      if (tx == 2) march3_go<FLUX, 2, 8>(s, st);
+      else march3_go<FLUX, 4, 7>(s, st);
     } else {
-      if (bs == 64) march_go<R, D, FLUX, 4, 64>(s, dt, st);
-      else march_go<R, D, FLUX, 4, 128>(s, dt, st);
+      if (tx == 2) {
+        if (bs == 64) march_go<R, D, FLUX, 2, 64>(s, dt, st);
+        else march_go<R, D, FLUX, 2, 128>(s, dt, st);
+      } else {
+        if (bs == 64) march_go<R, D, FLUX, 4, 64>(s, dt, st);
+        else march_go<R, D, FLUX, 4, 128>(s, dt, st);
+      }
     }
   }
   return 1;
