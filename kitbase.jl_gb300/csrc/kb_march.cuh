@@ -1577,6 +1577,433 @@ __global__ void __launch_bounds__(M3_BS) k_march3(const __grid_constant__ CUtens
   }
 }
 
+// ------------------------------------ pass B, FP32 2D, two velocities per thread
+
+// Packed FP32 pair arithmetic (one instruction for both lanes of a float2).
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
+  unsigned long long A = *reinterpret_cast<unsigned long long*>(&a);
+  unsigned long long B = *reinterpret_cast<unsigned long long*>(&b), C;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(C) : "l"(A), "l"(B));
+  return *reinterpret_cast<float2*>(&C);
+}
+__device__ __forceinline__ float2 f2s(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 f2ex2(float2 a) { return make_float2(ex2(a.x), ex2(a.y)); }
+
+// van Leer slope (times dx) of a pair, interior cells (rule 1)
+__device__ __forceinline__ float2 vl2(float2 qm, float2 q0, float2 qp, float epsd) {
+  const float2 a = f2sub(q0, qm), b = f2sub(qp, q0);
+  const float2 A = make_float2(fabsf(a.x), fabsf(a.y)), B = make_float2(fabsf(b.x), fabsf(b.y));
+  const float2 num = f2fma(b, A, f2mul(a, B));
+  const float2 den = f2add(f2add(A, B), f2s(epsd));
+  return make_float2(fdiv_ftz(num.x, den.x), fdiv_ftz(num.y, den.y));
+}
+// general slope of a pair: per-lane rules (boundary cells)
+__device__ __forceinline__ float2 slope2(int r0, int r1, float2 qm, float2 q0, float2 qp,
+                                         float epsd) {
+  if (r0 == 1 && r1 == 1) return vl2(qm, q0, qp, epsd);
+  return make_float2(vl_diff(r0, qm.x, q0.x, qp.x, epsd), vl_diff(r1, qm.y, q0.y, qp.y, epsd));
+}
+
+struct Mono2 {
+  float2 un, ut, c2, m[7];
+  __device__ __forceinline__ void set(float2 a, float2 b) {
+    un = a;
+    ut = b;
+    c2 = f2fma(a, a, f2mul(b, b));
+    m[0] = a;
+    m[1] = f2mul(a, a);
+    m[2] = f2mul(m[1], a);
+    m[3] = f2mul(m[1], b);
+    m[4] = f2mul(m[1], c2);
+    m[5] = f2mul(a, b);
+    m[6] = f2mul(a, c2);
+  }
+  __device__ __forceinline__ Mono<float> lane(int k) const {
+    Mono<float> M;
+    M.un = k ? un.y : un.x;
+    M.ut = k ? ut.y : ut.x;
+    M.c2 = k ? c2.y : c2.x;
+#pragma unroll
+    for (int i = 0; i < 7; ++i) M.m[i] = k ? m[i].y : m[i].x;
+    return M;
+  }
+};
+
+// interface flux of an interior face for a velocity pair (same formulas as
+// eval_face); non-interior faces go lane by lane through eval_face
+template <int D, int FLUX, bool FAST>
+__device__ __forceinline__ void eval_face2(const FEv<float>& e, const Mono2& M, float2 side,
+                                           float2 hu, float2 bu, float2 su, float2 sb,
+                                           float2 hc, float2 bc, float2& fh, float2& fb) {
+  if (!FAST && e.kind != 1) {
+    eval_face<D, FLUX>(e, M.lane(0), side.x, hu.x, bu.x, su.x, sb.x, hc.x, bc.x, 0.0, fh.x, fb.x);
+    eval_face<D, FLUX>(e, M.lane(1), side.y, hu.y, bu.y, su.y, sb.y, hc.y, bc.y, 0.0, fh.y, fb.y);
+    return;
+  }
+  const float2 hf = f2fma(side, su, hu), bf = f2fma(side, sb, bu);
+  const float2 a = f2mul(f2s(e.T.x), M.un);
+  const float2 c = f2mul(f2s(-e.T.y), M.m[1]);
+  fh = f2fma(c, su, f2mul(a, hf));
+  fb = f2fma(c, sb, f2mul(a, bf));
+  if (FLUX == FLUX_KFVS) return;
+  const float2 Hm = f2ex2(
+      f2fma(f2s(e.E.w), M.c2, f2fma(f2s(e.E.z), M.ut, f2fma(f2s(e.E.y), M.un, f2s(e.E.x)))));
+  float2 ph = f2mul(f2s(e.T.z), M.m[0]);
+  float2 pb = f2mul(f2s(e.T.w), M.m[0]);
+  if (FLUX == FLUX_UGKS) {
+    ph = f2fma(f2s(e.C.x), M.m[1], ph);
+    ph = f2fma(f2s(e.C.y), M.m[2], ph);
+    ph = f2fma(f2s(e.C.w), M.m[4], ph);
+    ph = f2fma(f2s(e.G.x), M.m[5], ph);
+    ph = f2fma(f2s(e.G.y), M.m[6], ph);
+    pb = f2fma(f2s(e.Dd.x), M.m[1], pb);
+    pb = f2fma(f2s(e.Dd.y), M.m[2], pb);
+    pb = f2fma(f2s(e.Dd.w), M.m[4], pb);
+    pb = f2fma(f2s(e.G.z), M.m[5], pb);
+    pb = f2fma(f2s(e.G.w), M.m[6], pb);
+    if (D == 2) {
+      ph = f2fma(f2s(e.C.z), M.m[3], ph);
+      pb = f2fma(f2s(e.Dd.z), M.m[3], pb);
+    }
+  }
+  fh = f2fma(Hm, ph, fh);
+  fb = f2fma(Hm, pb, fb);
+}
+
+// pointwise relaxation of a velocity pair (same formulas as relax)
+__device__ __forceinline__ void relax2(const CellCoef32& k, bool shak, float2 u, float2 vv,
+                                       float2 c2, float2 h0, float2 b0, float2 dh, float2 db,
+                                       float2& hn, float2& bn) {
+  const float2 M = f2ex2(
+      f2fma(f2s(k.EM.w), c2, f2fma(f2s(k.EM.z), vv, f2fma(f2s(k.EM.y), u, f2s(k.EM.x)))));
+  float2 MH = M, MB = f2mul(M, f2s(k.A.x));
+  if (shak) {
+    const float2 OH = f2ex2(
+        f2fma(f2s(k.EO.w), c2, f2fma(f2s(k.EO.z), vv, f2fma(f2s(k.EO.y), u, f2s(k.EO.x)))));
+    const float2 cq = f2mul(f2fma(f2s(k.Q.z), vv, f2fma(f2s(k.Q.y), u, f2s(k.Q.x))), OH);
+    const float2 tl =
+        f2fma(f2s(k.TL.w), c2, f2fma(f2s(k.TL.z), vv, f2fma(f2s(k.TL.y), u, f2s(k.TL.x))));
+    MH = f2fma(cq, f2add(tl, f2s(-5.f)), MH);
+    MB = f2fma(f2mul(cq, f2add(tl, f2s(-3.f))), f2s(k.Q.w), MB);
+  }
+  hn = f2mul(f2fma(f2s(k.A.y), MH, f2fma(dh, f2s(k.A.w), h0)), f2s(k.A.z));
+  bn = f2mul(f2fma(f2s(k.A.y), MB, f2fma(db, f2s(k.A.w), b0)), f2s(k.A.z));
+}
+
+// Pass B in the 2D FP32 form with two adjacent velocities per thread: the
+// same ring, rows and faces as k_march3, with packed FP32-pair arithmetic, so
+// each face's coefficients, each slot lookup and each barrier operation serve
+// two velocities.  A CTA of 64 threads covers the 128 velocities of a box.
+constexpr int M4_THREADS = M3_BS / 2;
+template <int FLUX, int TX, int NS, int G>
+__global__ void __launch_bounds__(M4_THREADS * G) k_march4(const __grid_constant__ CUtensorMap tmh,
+                                                       const __grid_constant__ CUtensorMap tmb,
+                                                       DevState s, int RY) {
+  static_assert(NS >= 6, "the ring holds the 4-row window plus at least one row ahead");
+  using L = M3Layout<TX, NS>;
+  constexpr int D = 2;
+  extern __shared__ __align__(1024) unsigned char smem4[];
+  unsigned long long* full = (unsigned long long*)(smem4 + NS * L::SLOT);
+  unsigned long long* empty = full + NS;
+  int* bad = (int*)(empty + NS);
+  volatile int* vbad = bad;
+  const Geo& g = s.g;
+  const int tid = threadIdx.x, lane = tid & 31;
+  // G groups of 64 threads split the strip's columns: group tid / 64 owns
+  // columns cg .. cg + TXG - 1; every group covers all 128 velocities
+  constexpr int TXG = TX / G;
+  const int lt = tid % M4_THREADS, cg = (tid / M4_THREADS) * TXG;
+  const int v0 = blockIdx.x * M3_BS;
+  const int va = v0 + 2 * lt, vb = va + 1;  // this thread's velocities
+  const bool oka = va < g.nvel, okb = vb < g.nvel;
+  const int ia = oka ? va : g.nvel - 1, ib = okb ? vb : g.nvel - 1;
+  const int i0 = blockIdx.y * TX;
+  const int ncol = min(TX, g.nx - i0);
+  const int j0 = blockIdx.z * RY;
+  const int j1 = min(g.ny, j0 + RY);
+  const int q0 = j0 - 2;
+  const int qend = j1 + 1;
+  const int vs = g.vstride;
+  float* __restrict__ Ho = (float*)s.h[s.cur ^ 1];
+  float* __restrict__ Bo = (float*)s.b[s.cur ^ 1];
+
+  auto slot = [&](int q) -> const unsigned char* { return smem4 + ((q - q0) % NS) * L::SLOT; };
+  auto issue = [&](int q) {
+    const int r = q - q0;
+    unsigned char* S = smem4 + (r % NS) * L::SLOT;
+    unsigned long long* bar = &full[r % NS];
+    const bool hy = q >= j0 - 1 && q <= j1 - 1, hx = q >= j0 && q <= j1 - 1;
+    const unsigned xb = (ncol + 1) * sizeof(FaceCoef32), yb = ncol * sizeof(FaceCoef32),
+                   cb = ncol * sizeof(CellCoef32);
+    mbar_expect(bar, 2 * L::BOX + (hy ? yb : 0u) + (hx ? xb + cb : 0u));
+    tma_load_3d(S, &tmh, v0, i0 - 2 + g.ngx, q + g.ngy, bar);
+    tma_load_3d(S + L::BOX, &tmb, v0, i0 - 2 + g.ngx, q + g.ngy, bar);
+    if (hx) {
+      bulk_g2s(S + L::XF, s.fc + (long)q * (g.nx + 1) + i0, xb, bar);
+      bulk_g2s(S + L::CC, s.cc + cell_index(g, i0, q), cb, bar);
+    }
+    if (hy) bulk_g2s(S + L::YF, s.fc + s.nface_x + (long)(q + 1) * g.nx + i0, yb, bar);
+  };
+  auto await_row = [&](int q) {
+    if (*vbad) return;
+    const int r = q - q0;
+    if (!mbar_wait(&full[r % NS], (r / NS) & 1)) {
+      atomicOr(bad, 1);
+      atomicOr(s.status, 2);
+    }
+  };
+  auto release_row = [&](int q) {
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[(q - q0) % NS]);
+  };
+
+  int issued = 0;
+  if (tid == 0) {
+    for (int k = 0; k < NS; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], M4_THREADS * G / 32);
+    }
+    *bad = 0;
+    fence_async_smem();
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int q = q0; q <= qend && q < q0 + NS; ++q, ++issued) issue(q);
+
+  const float2 u = make_float2(s.uf[ia], s.uf[ib]), vv = make_float2(s.vf[ia], s.vf[ib]);
+  Mono2 MX, MY;
+  MX.set(u, vv);
+  MY.set(vv, make_float2(-u.x, -u.y));
+  const bool pxa = u.x >= 0.f, pxb = u.y >= 0.f, pya = vv.x >= 0.f, pyb = vv.y >= 0.f;
+  const float2 sx = make_float2(pxa ? 0.5f : -0.5f, pxb ? 0.5f : -0.5f);
+  const float2 sy = make_float2(pya ? 0.5f : -0.5f, pyb ? 0.5f : -0.5f);
+  const float epsx = float(1.e-7 * g.dx), epsy = float(1.e-7 * g.dy);
+  const bool shak = s.coll == COLL_SHAKHOV;
+  const int sha = pxa ? 0 : 1, shb = pxb ? 0 : 1;  // x window shift per lane
+  const bool samex = sha == shb, samey = pya == pyb;
+  int rxa[TXG + 3], rxb[TXG + 3];
+#pragma unroll
+  for (int k = 0; k < TXG + 3; ++k) {
+    rxa[k] = slope_rule(g, 0, i0 - 2 + cg + k + sha);
+    rxb[k] = slope_rule(g, 0, i0 - 2 + cg + k + shb);
+  }
+  const long rowstride = (long)g.nxt * vs;
+
+  // values of this thread's pair in column w of a slot: both lanes from the
+  // same column (one 64-bit load) or each lane from its own column
+  auto Hp = [&](const unsigned char* S, int w) {
+    return *(const float2*)((const float*)S + w * M3_BS + 2 * lt);
+  };
+  auto Bp = [&](const unsigned char* S, int w) {
+    return *(const float2*)((const float*)(S + L::BOX) + w * M3_BS + 2 * lt);
+  };
+  auto H2 = [&](const unsigned char* Sa, int wa, const unsigned char* Sb, int wb) {
+    return make_float2(((const float*)Sa)[wa * M3_BS + 2 * lt],
+                       ((const float*)Sb)[wb * M3_BS + 2 * lt + 1]);
+  };
+  auto B2 = [&](const unsigned char* Sa, int wa, const unsigned char* Sb, int wb) {
+    return make_float2(((const float*)(Sa + L::BOX))[wa * M3_BS + 2 * lt],
+                       ((const float*)(Sb + L::BOX))[wb * M3_BS + 2 * lt + 1]);
+  };
+
+  auto yface = [&](int ql, int c, auto fast_tag, auto same_tag, float2& fh, float2& fb) {
+    constexpr bool FAST = decltype(fast_tag)::value;
+    constexpr bool SAME = decltype(same_tag)::value;  // both lanes share their upwind sides
+    fh = f2s(0.f);
+    fb = f2s(0.f);
+    if (!FAST && cg + c >= ncol) return;
+    const int w = cg + c + 2;
+    const int qa = pya ? ql - 1 : ql, qb = pyb ? ql - 1 : ql;  // stencil rows start
+    float2 hm, h0, hp, bm, b0, bp;
+    if (SAME) {
+      const unsigned char* S0 = slot(qa);
+      const unsigned char* S1 = slot(qa + 1);
+      const unsigned char* S2 = slot(qa + 2);
+      hm = Hp(S0, w); h0 = Hp(S1, w); hp = Hp(S2, w);
+      bm = Bp(S0, w); b0 = Bp(S1, w); bp = Bp(S2, w);
+    } else {
+      hm = H2(slot(qa), w, slot(qb), w); h0 = H2(slot(qa + 1), w, slot(qb + 1), w);
+      hp = H2(slot(qa + 2), w, slot(qb + 2), w);
+      bm = B2(slot(qa), w, slot(qb), w); b0 = B2(slot(qa + 1), w, slot(qb + 1), w);
+      bp = B2(slot(qa + 2), w, slot(qb + 2), w);
+    }
+    float2 su, sb;
+    if (FAST) {
+      su = vl2(hm, h0, hp, epsy);
+      sb = vl2(bm, b0, bp, epsy);
+    } else {
+      const int ra = slope_rule(g, 1, qa + 1), rb = slope_rule(g, 1, qb + 1);
+      su = slope2(ra, rb, hm, h0, hp, epsy);
+      sb = slope2(ra, rb, bm, b0, bp, epsy);
+    }
+    FEv<float> e;
+    const FaceCoef32* yc = (const FaceCoef32*)(slot(ql) + L::YF);
+    if (FAST) e.load_interior(yc[cg + c], true);
+    else e.load(yc[cg + c], s.kind[s.nface_x + (ql + 1) * g.nx + i0 + cg + c], true);
+    if (FLUX != FLUX_KFVS && (FAST || e.kind == 1)) {
+      // the upwind-dependent coefficients of each lane
+      const float4* cpa = pya ? &yc[cg + c].Cp : &yc[cg + c].Cm;
+      if (!SAME) {  // mixed pair: evaluate lane by lane
+        FEv<float> ea = e, eb = e;
+        ea.C = (pya ? yc[cg + c].Cp : yc[cg + c].Cm);
+        ea.Dd = (pya ? yc[cg + c].Dp : yc[cg + c].Dm);
+        eb.C = (pyb ? yc[cg + c].Cp : yc[cg + c].Cm);
+        eb.Dd = (pyb ? yc[cg + c].Dp : yc[cg + c].Dm);
+        eval_face<D, FLUX>(ea, MY.lane(0), sy.x, h0.x, b0.x, su.x, sb.x, 0.f, 0.f, 0.0, fh.x, fb.x);
+        eval_face<D, FLUX>(eb, MY.lane(1), sy.y, h0.y, b0.y, su.y, sb.y, 0.f, 0.f, 0.0, fh.y, fb.y);
+        return;
+      }
+      e.C = cpa[0];
+      e.Dd = cpa[1];
+    }
+    float2 hc = f2s(0.f), bc = f2s(0.f);
+    if (!FAST) {
+      const unsigned char* Si = slot(ql + 1 == 0 ? ql + 1 : ql);
+      hc = Hp(Si, w);
+      bc = Bp(Si, w);
+    }
+    eval_face2<D, FLUX, FAST>(e, MY, sy, h0, b0, su, sb, hc, bc, fh, fb);
+  };
+
+  float2 fyh[TXG], fyb[TXG];
+  await_row(q0);
+  await_row(q0 + 1);
+  await_row(q0 + 2);
+  await_row(q0 + 3);
+  const bool same = samex && samey;
+  {
+    const bool fast = g.interp == 2 && i0 >= 2 && i0 + TX <= g.nx - 2 && j0 >= 2 && j0 <= g.ny - 2;
+#pragma unroll
+    for (int c = 0; c < TXG; ++c) {
+      if (fast && same) yface(j0 - 1, c, std::true_type{}, std::true_type{}, fyh[c], fyb[c]);
+      else yface(j0 - 1, c, std::false_type{}, std::false_type{}, fyh[c], fyb[c]);
+    }
+  }
+  release_row(q0);
+
+  auto row = [&](int j, auto fast_tag, auto same_tag) {
+    constexpr bool FAST = decltype(fast_tag)::value;
+    constexpr bool SAME = decltype(same_tag)::value;
+    const unsigned char* Sj = slot(j);
+    float2 fyh2[TXG], fyb2[TXG];
+#pragma unroll
+    for (int c = 0; c < TXG; ++c) yface(j, c, fast_tag, same_tag, fyh2[c], fyb2[c]);
+    // x window of row j shifted to each lane's upwind side
+    float2 xs[TXG + 3], xt[TXG + 3];
+    if (SAME) {
+#pragma unroll
+      for (int k = 0; k < TXG + 3; ++k) {
+        xs[k] = Hp(Sj, cg + k + sha);
+        xt[k] = Bp(Sj, cg + k + sha);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < TXG + 3; ++k) {
+        xs[k] = H2(Sj, cg + k + sha, Sj, cg + k + shb);
+        xt[k] = B2(Sj, cg + k + sha, Sj, cg + k + shb);
+      }
+    }
+    const FaceCoef32* xc = (const FaceCoef32*)(Sj + L::XF);
+    float2 fxh[TXG + 1], fxb[TXG + 1];
+#pragma unroll
+    for (int f = 0; f <= TXG; ++f) {
+      fxh[f] = f2s(0.f);
+      fxb[f] = f2s(0.f);
+      if (!FAST && cg + f > ncol) continue;
+      float2 su, sb;
+      if (FAST) {
+        su = vl2(xs[f], xs[f + 1], xs[f + 2], epsx);
+        sb = vl2(xt[f], xt[f + 1], xt[f + 2], epsx);
+      } else {
+        su = slope2(rxa[f + 1], rxb[f + 1], xs[f], xs[f + 1], xs[f + 2], epsx);
+        sb = slope2(rxa[f + 1], rxb[f + 1], xt[f], xt[f + 1], xt[f + 2], epsx);
+      }
+      const int fi = i0 + cg + f;
+      FEv<float> e;
+      if (FAST) e.load_interior(xc[cg + f], true);
+      else e.load(xc[cg + f], s.kind[j * (g.nx + 1) + fi], true);
+      if (FLUX != FLUX_KFVS && (FAST || e.kind == 1)) {
+        if (!SAME) {  // mixed pair: evaluate lane by lane
+          FEv<float> ea = e, eb = e;
+          ea.C = (pxa ? xc[cg + f].Cp : xc[cg + f].Cm);
+          ea.Dd = (pxa ? xc[cg + f].Dp : xc[cg + f].Dm);
+          eb.C = (pxb ? xc[cg + f].Cp : xc[cg + f].Cm);
+          eb.Dd = (pxb ? xc[cg + f].Dp : xc[cg + f].Dm);
+          eval_face<D, FLUX>(ea, MX.lane(0), sx.x, xs[f + 1].x, xt[f + 1].x, su.x, sb.x, 0.f,
+                             0.f, 0.0, fxh[f].x, fxb[f].x);
+          eval_face<D, FLUX>(eb, MX.lane(1), sx.y, xs[f + 1].y, xt[f + 1].y, su.y, sb.y, 0.f,
+                             0.f, 0.0, fxh[f].y, fxb[f].y);
+          continue;
+        }
+        const float4* cp = pxa ? &xc[cg + f].Cp : &xc[cg + f].Cm;
+        e.C = cp[0];
+        e.Dd = cp[1];
+      }
+      float2 hc = f2s(0.f), bc = f2s(0.f);
+      if (!FAST) {
+        hc = Hp(Sj, cg + (fi == 0 ? f + 2 : f + 1));
+        bc = Bp(Sj, cg + (fi == 0 ? f + 2 : f + 1));
+      }
+      eval_face2<D, FLUX, FAST>(e, MX, sx, xs[f + 1], xt[f + 1], su, sb, hc, bc, fxh[f], fxb[f]);
+    }
+    const CellCoef32* cc = (const CellCoef32*)(Sj + L::CC);
+    const long ro = (long)(j + g.ngy) * rowstride + (long)(i0 + g.ngx) * vs + va;
+#pragma unroll
+    for (int c = 0; c < TXG; ++c) {
+      if (!FAST && cg + c >= ncol) continue;
+      const float2 dhh = f2sub(f2add(f2sub(fxh[c], fxh[c + 1]), fyh[c]), fyh2[c]);
+      const float2 dbb = f2sub(f2add(f2sub(fxb[c], fxb[c + 1]), fyb[c]), fyb2[c]);
+      float2 hn, bn;
+      relax2(cc[cg + c], shak, u, vv, MX.c2, Hp(Sj, cg + c + 2), Bp(Sj, cg + c + 2), dhh, dbb,
+             hn, bn);
+      float* ph = Ho + ro + (long)(cg + c) * vs;
+      float* pb = Bo + ro + (long)(cg + c) * vs;
+      if (okb) {
+        *(float2*)ph = hn;
+        *(float2*)pb = bn;
+      } else if (oka) {
+        ph[0] = hn.x;
+        pb[0] = bn.x;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < TXG; ++c) {
+      fyh[c] = fyh2[c];
+      fyb[c] = fyb2[c];
+    }
+  };
+
+  const bool fastx = g.interp == 2 && i0 >= 2 && i0 + TX <= g.nx - 2;
+  for (int j = j0; j < j1; ++j) {
+    if (tid == 0 && *vbad == 0) {
+      const int q = j + NS - 3;
+      if (j > j0 && q <= qend) {
+        const int r = q - q0;
+        if (mbar_wait(&empty[r % NS], ((r - NS) / NS) & 1)) {
+          fence_async_smem();
+          issue(q);
+          ++issued;
+        } else {
+          atomicOr(bad, 1);
+          atomicOr(s.status, 2);
+        }
+      }
+    }
+    await_row(j + 2);
+    // warps whose pairs all share their upwind sides run only the packed body
+    if (fastx && j >= 1 && j <= g.ny - 3 && same) row(j, std::true_type{}, std::true_type{});
+    else row(j, std::false_type{}, std::false_type{});
+    release_row(j - 1);
+  }
+  __syncthreads();
+  if (*vbad && tid == 0) {
+    for (int r = max(0, issued - NS); r < issued; ++r) mbar_wait(&full[r % NS], (r / NS) & 1);
+  }
+}
+
 // ----------------------------------------------------------- launch helpers
 
 constexpr int TS_MOM = 4;    // faces per warp in pass A
@@ -1647,13 +2074,16 @@ static void march_go(DevState& s, double dt, cudaStream_t st) {
 // FP32 2D pass B (k_march3): the tensor maps of the current h / b buffers for
 // this strip width; the ring needs more than the default 48 KB of shared
 // memory, so the limit is raised once per device.
-template <int FLUX, int TX, int NS>
+template <int FLUX, int TX, int NS, int G>
 static void march3_go(DevState& s, cudaStream_t st) {
+  constexpr bool PAIR = G > 0;  // G groups of 64 threads, two velocities each
   const Geo& g = s.g;
   using L = M3Layout<TX, NS>;
   const int ry = s.tune[KB_TUNE_MARCH_RY] > 0 ? s.tune[KB_TUNE_MARCH_RY] : RY_MARCH;
   const CUtensorMap* tm = (const CUtensorMap*)s.tmaps + ((TX == 4 ? 1 : 0) * 2 + s.cur) * 2;
-  auto kern = k_march3<FLUX, TX, NS>;
+  decltype(&k_march3<FLUX, TX, NS>) kern;
+  if constexpr (PAIR) kern = k_march4<FLUX, TX, NS, G>;
+  else kern = k_march3<FLUX, TX, NS>;
   static bool raised[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -1662,7 +2092,7 @@ static void march3_go(DevState& s, cudaStream_t st) {
     raised[dev] = true;
   }
   dim3 grid((g.nvel + M3_BS - 1) / M3_BS, (g.nx + TX - 1) / TX, (g.ny + ry - 1) / ry);
-  kern<<<grid, M3_BS, L::BYTES, st>>>(tm[0], tm[1], s, ry);
+  kern<<<grid, PAIR ? M4_THREADS * G : M3_BS, L::BYTES, st>>>(tm[0], tm[1], s, ry);
 }
 
 // FP32: the autotuned shapes (TX 2 or 4 columns, 64 or 128 threads);
@@ -1675,9 +2105,16 @@ static int march_t(DevState& s, double dt, cudaStream_t st) {
     const int tx = s.tune[KB_TUNE_MARCH_TX] > 0 ? s.tune[KB_TUNE_MARCH_TX] : TX_MARCH;
     const int bs = s.tune[KB_TUNE_MARCH_BS] > 0 ? s.tune[KB_TUNE_MARCH_BS] : 128;
     if constexpr (D == 2) {
-      (void)bs;
-      if (tx == 2) march3_go<FLUX, 2, 8>(s, st);
-      else march3_go<FLUX, 4, 7>(s, st);
+      // bs 64: two velocities per thread, one 64-thread group per strip
+      // (k_march4); tx 4 + bs 64 splits the strip between two groups; bs 128:
+      // one velocity per thread (k_march3)
+      if (bs == 64) {
+        if (tx == 2) march3_go<FLUX, 2, 8, 1>(s, st);
+        else march3_go<FLUX, 4, 7, 2>(s, st);
+      } else {
+        if (tx == 2) march3_go<FLUX, 2, 8, 0>(s, st);
+        else march3_go<FLUX, 4, 7, 0>(s, st);
+      }
     } else {
       if (tx == 2) {
         if (bs == 64) march_go<R, D, FLUX, 2, 64>(s, dt, st);

@@ -128,3 +128,28 @@ def test_fp32_split_error(gpu_lib, name, cfg, n):
     w, p, h, b = orc.get_state()
     e = rho_u_t_error(g["prim"], p)
     assert max(e) < 1e-5, e
+
+
+FP32_SHAPES = [(tx, bs) for tx in (2, 4) for bs in (64, 128)]
+
+
+@pytest.mark.parametrize("tx,bs", FP32_SHAPES, ids=["tx%d-bs%d" % s for s in FP32_SHAPES])
+@pytest.mark.parametrize("name,cfg", [
+    ("cavity-kcu-shakhov", cavity(nx=13, ny=11, nu=14, nv=16)),
+    ("quadrant-ugks-bgk-extra", quadrant(nx=18, ny=17, nu=15, nv=12)),
+    ("quadrant-kfvs-shakhov-extra", quadrant(nx=17, ny=19, nu=16, nv=13, flux="kfvs", coll="shakhov")),
+], ids=lambda x: x if isinstance(x, str) else "")
+def test_fp32_update_shapes(gpu_lib, name, cfg, tx, bs):
+    """Every launch shape of the FP32 2D update (one or two velocities per
+    thread, two or four columns per strip), incl. partial strips and velocity
+    pairs whose upwind sides differ, stays within 1e-5 of the FP64 oracle."""
+    KS, ctr, *faces, t = kitgpu.initialize(cfg, precision="fp32")
+    ctr.handle.set_tuning(march_tx=tx, march_ry=8, march_bs=bs)
+    orc = oracle_for(KS)
+    dt = kitgpu.timestep(KS, ctr, 0.0)
+    kitgpu.step(KS, ctr, dt, 30)
+    orc.step(dt, 30)
+    g = ctr.handle.download()
+    w, p, h, b = orc.get_state()
+    e = rho_u_t_error(g["prim"], p)
+    assert max(e) < 1e-5, e
