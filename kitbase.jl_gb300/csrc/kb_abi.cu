@@ -44,8 +44,10 @@ struct kb_handle {
   std::vector<cudaEvent_t> events;
   double stage_ms[KB_NSTAGE] = {0};
   int64_t stage_n[KB_NSTAGE] = {0};
-  // TMA descriptors of the FP32 2D update: [strip width 2, 4][buffer][h, b]
-  CUtensorMap tmaps[2][2][2];
+  // TMA descriptors of the FP32 form: [0, 8) the 2D update, [strip width 2, 4]
+  // [buffer][h, b]; [8, 24) the moment pass, [direction][faces per warp 2, 4]
+  // [buffer][h, b]
+  CUtensorMap tmaps[24];
 };
 
 
@@ -58,10 +60,12 @@ static int fail(int code, const std::string& msg) {
 
 void kb::set_error(const std::string& msg) { g_err = msg; }
 
-// Encode the TMA descriptors of the FP32 2D update pass: each distribution
-// buffer is a 3D tensor (velocity, column, row) incl. ghosts; one box is
-// 128 velocities x (strip width + 4) columns x 1 row.  Coordinates outside
-// the tensor read as zero, which is what the update expects beyond the grid.
+// Encode the TMA descriptors of the FP32 form: each distribution buffer is a
+// 3D tensor (velocity, column, row) incl. ghosts.  Update-pass boxes are 128
+// velocities x (strip width + 4) columns x 1 row; moment-pass boxes are 128
+// velocities x (4 x faces per warp + 4) cells along x or along y.  Coordinates
+// outside the tensor read as zero, which is what both passes expect beyond the
+// grid.
 static int make_tmaps(kb_handle* h) {
   void* fn = nullptr;
   cudaDriverEntryPointQueryResult q;
@@ -74,19 +78,28 @@ static int make_tmaps(kb_handle* h) {
   const cuuint64_t dims[3] = {(cuuint64_t)g.vstride, (cuuint64_t)g.nxt, (cuuint64_t)g.nyt};
   const cuuint64_t strides[2] = {(cuuint64_t)g.vstride * 4, (cuuint64_t)g.vstride * 4 * g.nxt};
   const cuuint32_t estr[3] = {1, 1, 1};
-  for (int t = 0; t < 2; ++t) {
+  auto make = [&](int idx, const cuuint32_t* box, int k, int d) {
+    CUresult r = encode(&h->tmaps[idx], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                        d == 0 ? h->s.h[k] : h->s.b[k], dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+  };
+  bool ok = true;
+  for (int t = 0; t < 2 && g.D == 2; ++t) {
     const cuuint32_t box[3] = {128, (cuuint32_t)(t == 0 ? 2 + 4 : 4 + 4), 1};
     for (int k = 0; k < 2; ++k)
-      for (int d = 0; d < 2; ++d) {
-        CUresult r = encode(&h->tmaps[t][k][d], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
-                            d == 0 ? h->s.h[k] : h->s.b[k], dims, strides, box, estr,
-                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (r != CUDA_SUCCESS)
-          return fail(KB_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
-      }
+      for (int d = 0; d < 2; ++d) ok = ok && make((t * 2 + k) * 2 + d, box, k, d);
   }
-  h->s.tmaps = &h->tmaps[0][0][0];
+  for (int dir = 0; dir < g.D; ++dir)
+    for (int t = 0; t < 2; ++t) {
+      const cuuint32_t nwin = 4 * (t == 0 ? 2 : 4) + 4;
+      const cuuint32_t box[3] = {128, dir == 0 ? nwin : 1u, dir == 0 ? 1u : nwin};
+      for (int k = 0; k < 2; ++k)
+        for (int d = 0; d < 2; ++d) ok = ok && make(8 + ((dir * 2 + t) * 2 + k) * 2 + d, box, k, d);
+    }
+  if (!ok) return fail(KB_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  h->s.tmaps = &h->tmaps[0];
   return KB_OK;
 }
 
@@ -278,7 +291,7 @@ int kb_create(const kb_config_t* cfg, const double* u, const double* v, const do
   ALLOC(h->d_stage, double, h->stage_elems);
 #undef ALLOC
   h->s.tmaps = nullptr;
-  if (c.precision == KB_PREC_FP32 && c.dim == 2 && (rc = make_tmaps(h)) != KB_OK) return bail(rc);
+  if (c.precision == KB_PREC_FP32 && (rc = make_tmaps(h)) != KB_OK) return bail(rc);
   cudaMemset(h->s.sw, 0, sizeof(double) * h->ncell * 8);
   cudaMemset(h->s.q, 0, sizeof(double) * h->ncell * 2);
   cudaMemset(h->s.w, 0, sizeof(double) * h->ncell * 4);

@@ -47,8 +47,8 @@ struct DevState {
   double* blockres; // [nblocks][16] residual partials
   double* residual; // [4]
   int* status;      // [1]
-  // host pointer to the TMA descriptors (CUtensorMap) of the FP32 2D form:
-  // [strip width 2, 4][buffer 0, 1][h, b]; unused by device code
+  // host pointer to the TMA descriptors (CUtensorMap) of the FP32 form (the
+  // layout is documented at kb_handle::tmaps); unused by device code
   const void* tmaps;
   int nface_x, nface_y;
   int ncell;

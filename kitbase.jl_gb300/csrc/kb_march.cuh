@@ -115,6 +115,18 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
       : "memory");
 }
 
+// 3D tiled tensor load (TMA) of one box into shared memory, completed on an
+// mbarrier.  Coordinates outside the tensor read as zero.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1,
+                                            int c2, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2),
+      "r"(smem_u32(bar))
+      : "memory");
+}
+
 // Rule-dispatching slope; FAST = interior cell (van Leer only).
 template <bool FAST, typename R>
 __device__ __forceinline__ R slope(int rule, R qm, R q0, R qp, R epsd) {
@@ -345,7 +357,9 @@ __global__ void __launch_bounds__(128) k_mom(DevState s) {
 
 // Pass A, FP32 form: the stencil window of a CTA segment (4 warps x TS faces
 // along one line) is streamed through shared memory in chunks of MOM_VC
-// velocities by bulk async copies, MOM_P chunks in flight, so the DRAM
+// velocities, MOM_P chunks in flight: one TMA tensor box per distribution
+// (velocities x window cells of the line; cells outside the grid read as
+// zero) plus three bulk copies of the velocity tables per chunk, so the DRAM
 // latency is covered by the copies already issued instead of by registers.
 // A fifth (producer) warp issues the copies; each consumer warp reads its
 // TS+4 window cells from shared memory, lanes over velocities, and releases a
@@ -357,19 +371,22 @@ template <int TS>
 struct MomStage {
   static constexpr int NF = 4 * TS;     // faces per CTA segment
   static constexpr int NWIN = NF + 4;   // window cells p0-2 .. p0+NF+1
-  static constexpr int FLOATS = (2 * NWIN + 3) * MOM_VC;  // [cell][h|b][v], then u, v, w
+  static constexpr int BOX = NWIN * MOM_VC;                // one distribution: [cell][v]
+  static constexpr int FLOATS = 2 * BOX + 3 * MOM_VC;      // h box, b box, then u, v, w
   // stages, then full[MOM_P], empty[MOM_P] mbarriers and a failure flag
   static constexpr int BYTES = MOM_P * FLOATS * 4 + 16 * MOM_P + 16;
 };
 constexpr int MOM_THREADS = 160;  // 4 consumer warps + 1 producer warp
 
 template <int D, int FLUX, int TS, bool SHAK, int DIR>
-__global__ void __launch_bounds__(MOM_THREADS) k_mom_st(DevState s) {
+__global__ void __launch_bounds__(MOM_THREADS) k_mom_st(const __grid_constant__ CUtensorMap tmh,
+                                                        const __grid_constant__ CUtensorMap tmb,
+                                                        DevState s) {
   using R = float;
   using SL = MomStage<TS>;
-  extern __shared__ __align__(16) unsigned char smem[];
-  float* stg = (float*)smem;
-  unsigned long long* full = (unsigned long long*)(smem + MOM_P * SL::FLOATS * 4);
+  extern __shared__ __align__(1024) unsigned char smemA[];
+  float* stg = (float*)smemA;
+  unsigned long long* full = (unsigned long long*)(smemA + MOM_P * SL::FLOATS * 4);
   unsigned long long* empty = full + MOM_P;
   int* bad = (int*)(empty + MOM_P);
   constexpr int PRODUCER = 4;
@@ -394,22 +411,6 @@ __global__ void __launch_bounds__(MOM_THREADS) k_mom_st(DevState s) {
     e = p >= -ng && p < n + ng;
     return DIR == 0 ? cell_index(g, p, line) : cell_index(g, line, p);
   };
-  int nexist = 0;
-  for (int w = 0; w < SL::NWIN; ++w) {
-    bool e;
-    win_cell(w, e);
-    nexist += e;
-  }
-  // cells outside the grid (incl. ghosts) read as zero: clear their slots once
-  if (nexist < SL::NWIN) {
-    for (int i = threadIdx.x; i < MOM_P * 2 * SL::NWIN; i += blockDim.x) {
-      const int st = i / (2 * SL::NWIN), r = i - st * 2 * SL::NWIN;
-      bool e;
-      win_cell(r >> 1, e);
-      if (!e)
-        for (int k = 0; k < MOM_VC; ++k) stg[st * SL::FLOATS + r * MOM_VC + k] = 0.f;
-    }
-  }
   if (threadIdx.x == 0) {
     for (int k = 0; k < MOM_P; ++k) {
       mbar_init(&full[k], 1);
@@ -420,27 +421,21 @@ __global__ void __launch_bounds__(MOM_THREADS) k_mom_st(DevState s) {
   fence_async_smem();
   __syncthreads();
 
-  const R* __restrict__ H = (const R*)s.h[s.cur];
-  const R* __restrict__ Bq = (const R*)s.b[s.cur];
-  auto issue = [&](int k) {  // producer warp: chunk k into stage k % MOM_P
+  // tensor coordinates (velocity, column, row) of the window's first cell
+  const int cx = DIR == 0 ? p0 - 2 + g.ngx : line + g.ngx;
+  const int cy = DIR == 0 ? line + g.ngy : p0 - 2 + g.ngy;
+  auto issue = [&](int k) {  // producer lane 0: chunk k into stage k % MOM_P
     float* S = stg + (k % MOM_P) * SL::FLOATS;
     unsigned long long* bar = &full[k % MOM_P];
     const int v0 = k * MOM_VC;
     const unsigned cb = (unsigned)min(MOM_VC, vs - v0) * 4u;  // a multiple of 16
-    if (lane == 0) mbar_expect(bar, cb * (2 * nexist + 3));
-    __syncwarp();
-    for (int i = lane; i < 2 * SL::NWIN + 3; i += 32) {
-      if (i < 2 * SL::NWIN) {
-        bool e;
-        const int c = win_cell(i >> 1, e);
-        if (!e) continue;
-        const R* src = ((i & 1) ? Bq : H) + (long)c * vs + v0;
-        bulk_g2s(S + i * MOM_VC, src, cb, bar);
-      } else {
-        const int t = i - 2 * SL::NWIN;
-        bulk_g2s(S + i * MOM_VC, vtab<R>(s, t) + v0, cb, bar);
-      }
+    if (lane == 0) {
+      mbar_expect(bar, 2u * SL::BOX * 4u + 3u * cb);
+      tma_load_3d(S, &tmh, v0, cx, cy, bar);
+      tma_load_3d(S + SL::BOX, &tmb, v0, cx, cy, bar);
+      for (int t = 0; t < 3; ++t) bulk_g2s(S + 2 * SL::BOX + t * MOM_VC, vtab<R>(s, t) + v0, cb, bar);
     }
+    __syncwarp();
   };
 
   // this warp's faces and window (wl = 0 .. TS+3 <-> CTA window cell wid*TS + wl)
@@ -494,17 +489,17 @@ __global__ void __launch_bounds__(MOM_THREADS) k_mom_st(DevState s) {
   auto one = [&](const float* S, const float* Sw, int vl, auto fast_tag, auto sign_tag) {
     constexpr bool FAST = decltype(fast_tag)::value;
     constexpr int SG = decltype(sign_tag)::value;
-    const R u = S[2 * SL::NWIN * MOM_VC + vl];
-    const R vv = D == 2 ? S[(2 * SL::NWIN + 1) * MOM_VC + vl] : R(0);
-    const R om = S[(2 * SL::NWIN + 2) * MOM_VC + vl];
+    const R u = S[2 * SL::BOX + vl];
+    const R vv = D == 2 ? S[2 * SL::BOX + MOM_VC + vl] : R(0);
+    const R om = S[2 * SL::BOX + 2 * MOM_VC + vl];
     const R un = DIR == 0 ? u : vv;
     const R ut = DIR == 0 ? vv : -u;
     constexpr int WLO = SG == 2 ? 1 : 0, WHI = SG == 1 ? TS + 1 : (SG == 2 ? TS + 2 : TS + 3);
     R hx[TS + 4], bx[TS + 4];
 #pragma unroll
     for (int w = WLO; w <= WHI; ++w) {
-      hx[w] = Sw[(2 * w) * MOM_VC + vl];
-      bx[w] = Sw[(2 * w + 1) * MOM_VC + vl];
+      hx[w] = Sw[w * MOM_VC + vl];
+      bx[w] = Sw[SL::BOX + w * MOM_VC + vl];
     }
     const bool pos = SG == 0 ? un >= R(0) : SG == 1;
     const R c2 = un * un + ut * ut;
@@ -575,7 +570,7 @@ __global__ void __launch_bounds__(MOM_THREADS) k_mom_st(DevState s) {
   auto body = [&](const float* S, int k, auto fast_tag) {
     constexpr bool FAST = decltype(fast_tag)::value;
     using I0 = std::integral_constant<int, 0>;
-    const float* Sw = S + wid * TS * 2 * MOM_VC;  // this warp's window cell 0
+    const float* Sw = S + wid * TS * MOM_VC;  // this warp's window cell 0 (h; b at + BOX)
     // iterations holding at least one velocity: the same count on every lane,
     // so the whole warp reaches each ballot
     const int mmax = min(MOM_VC / 32, (g.nvel - k * MOM_VC + 31) / 32);
@@ -585,7 +580,7 @@ __global__ void __launch_bounds__(MOM_THREADS) k_mom_st(DevState s) {
       const int vl = m * 32 + lane;
       const bool valid = k * MOM_VC + vl < g.nvel;
       if (FAST) {
-        const R un = S[(2 * SL::NWIN + (DIR == 0 ? 0 : 1)) * MOM_VC + vl];
+        const R un = S[2 * SL::BOX + (DIR == 0 ? 0 : MOM_VC) + vl];
         const unsigned ap = __ballot_sync(0xffffffffu, !valid || un >= R(0));
         const unsigned an = __ballot_sync(0xffffffffu, !valid || un < R(0));
         if (valid) {
@@ -1321,18 +1316,6 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 && TX < 4 ? 384 : 256) / B
 
 // ------------------------------------------------- pass B, FP32 2D (TMA rows)
 
-// 3D tiled tensor load (TMA) of one box into shared memory, completed on an
-// mbarrier.  Coordinates outside the tensor read as zero.
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1,
-                                            int c2, unsigned long long* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2),
-      "r"(smem_u32(bar))
-      : "memory");
-}
-
 // Shared-memory ring of the 2D FP32 update: one slot per grid row of the
 // strip, holding the row's h and b boxes (TX+4 columns incl. the 2-cell x
 // halo on each side, M3_BS velocities; [column][velocity]) and the row's
@@ -2022,6 +2005,8 @@ static void mom_st_go(DevState& s, cudaStream_t st) {
   const int n = DIR == 0 ? g.nx : g.ny, nlines = DIR == 0 ? g.ny : g.nx;
   const long nblk = (long)nlines * ((n + SL::NF - 1) / SL::NF);
   auto kern = k_mom_st<D, FLUX, TS, SHAK, DIR>;
+  const CUtensorMap* tm =
+      (const CUtensorMap*)s.tmaps + 8 + ((DIR * 2 + (TS == 4 ? 1 : 0)) * 2 + s.cur) * 2;
   static bool raised[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -2029,7 +2014,7 @@ static void mom_st_go(DevState& s, cudaStream_t st) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SL::BYTES);
     raised[dev] = true;
   }
-  kern<<<(unsigned)nblk, MOM_THREADS, SL::BYTES, st>>>(s);
+  kern<<<(unsigned)nblk, MOM_THREADS, SL::BYTES, st>>>(tm[0], tm[1], s);
 }
 
 template <typename R, int D, int FLUX, int TS>
