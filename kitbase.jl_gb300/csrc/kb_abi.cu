@@ -87,14 +87,14 @@ static int make_tmaps(kb_handle* h) {
   };
   bool ok = true;
   for (int t = 0; t < 2 && g.D == 2; ++t) {
-    const cuuint32_t box[3] = {128, (cuuint32_t)(t == 0 ? 2 + 4 : 4 + 4), 1};
+    const cuuint32_t box[3] = {kb::KB_TMA_VBOX, (cuuint32_t)(t == 0 ? 2 + 4 : 4 + 4), 1};
     for (int k = 0; k < 2; ++k)
       for (int d = 0; d < 2; ++d) ok = ok && make((t * 2 + k) * 2 + d, box, k, d);
   }
   for (int dir = 0; dir < g.D; ++dir)
     for (int t = 0; t < 2; ++t) {
       const cuuint32_t nwin = 4 * (t == 0 ? 2 : 4) + 4;
-      const cuuint32_t box[3] = {128, dir == 0 ? nwin : 1u, dir == 0 ? 1u : nwin};
+      const cuuint32_t box[3] = {kb::KB_TMA_VBOX, dir == 0 ? nwin : 1u, dir == 0 ? 1u : nwin};
       for (int k = 0; k < 2; ++k)
         for (int d = 0; d < 2; ++d) ok = ok && make(8 + ((dir * 2 + t) * 2 + k) * 2 + d, box, k, d);
     }

@@ -8,6 +8,10 @@
 
 namespace kb {
 
+// Velocities per TMA box of the FP32 passes: the tensor maps (kb_abi.cu) and
+// the shared-memory stages of both passes (kb_march.cuh) are sized by it.
+constexpr int KB_TMA_VBOX = 128;
+
 // Record the message returned by kb_last_error() for this host thread.
 void set_error(const std::string& msg);
 

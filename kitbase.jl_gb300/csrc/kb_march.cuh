@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(128) k_mom(DevState s) {
 // TS+4 window cells from shared memory, lanes over velocities, and releases a
 // stage through its own mbarrier arrival, so consumer warps never wait on
 // one another.
-constexpr int MOM_VC = 128;  // velocities per staged chunk
+constexpr int MOM_VC = KB_TMA_VBOX;  // velocities per staged chunk (one TMA box)
 constexpr int MOM_P = 3;     // chunks in flight
 template <int TS>
 struct MomStage {
@@ -1320,7 +1320,7 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 && TX < 4 ? 384 : 256) / B
 // strip, holding the row's h and b boxes (TX+4 columns incl. the 2-cell x
 // halo on each side, M3_BS velocities; [column][velocity]) and the row's
 // coefficient blocks (x faces [TX+1], y faces above the row [TX], cells [TX]).
-constexpr int M3_BS = 128;  // velocities (threads) per CTA
+constexpr int M3_BS = KB_TMA_VBOX;  // velocities (threads) per CTA, one TMA box
 template <int TX, int NS>
 struct M3Layout {
   static constexpr int W = TX + 4;
