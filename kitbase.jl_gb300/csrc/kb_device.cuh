@@ -199,25 +199,31 @@ struct GM {
   double Mu[7], MuL[7], MuR[7], Mv[7], Mxi[3];
 };
 
-__device__ inline void gauss_moments(const double* p, int nw, double inK, GM& m) {
+// half: 1 the left half range only (MuL, Mv, Mxi), 2 the right half only,
+// 3 everything.  1 / (2 lambda) is formed once and multiplied in.
+__device__ inline void gauss_moments(const double* p, int nw, double inK, GM& m, int half = 3) {
   double l = p[nw - 1], U = p[1];
+  const double hl = 0.5 / l;
   double e = 0.5 * exp(-l * (U * U)) / sqrt(PI * l);
-  m.MuL[0] = 0.5 * erfc(-sqrt(l) * U);
-  m.MuL[1] = U * m.MuL[0] + e;
-  m.MuR[0] = 0.5 * erfc(sqrt(l) * U);
-  m.MuR[1] = U * m.MuR[0] - e;
-  for (int i = 2; i <= 6; ++i) {
-    m.MuL[i] = U * m.MuL[i - 1] + 0.5 * (i - 1) * m.MuL[i - 2] / l;
-    m.MuR[i] = U * m.MuR[i - 1] + 0.5 * (i - 1) * m.MuR[i - 2] / l;
+  if (half & 1) {
+    m.MuL[0] = 0.5 * erfc(-sqrt(l) * U);
+    m.MuL[1] = U * m.MuL[0] + e;
+    for (int i = 2; i <= 6; ++i) m.MuL[i] = U * m.MuL[i - 1] + (i - 1) * hl * m.MuL[i - 2];
   }
-  for (int i = 0; i <= 6; ++i) m.Mu[i] = m.MuL[i] + m.MuR[i];
+  if (half & 2) {
+    m.MuR[0] = 0.5 * erfc(sqrt(l) * U);
+    m.MuR[1] = U * m.MuR[0] - e;
+    for (int i = 2; i <= 6; ++i) m.MuR[i] = U * m.MuR[i - 1] + (i - 1) * hl * m.MuR[i - 2];
+  }
+  if (half == 3)
+    for (int i = 0; i <= 6; ++i) m.Mu[i] = m.MuL[i] + m.MuR[i];
   double V = nw == 4 ? p[2] : 0.0;
   m.Mv[0] = 1.0;
   m.Mv[1] = V;
-  for (int i = 2; i <= 6; ++i) m.Mv[i] = V * m.Mv[i - 1] + 0.5 * (i - 1) * m.Mv[i - 2] / l;
+  for (int i = 2; i <= 6; ++i) m.Mv[i] = V * m.Mv[i - 1] + (i - 1) * hl * m.Mv[i - 2];
   m.Mxi[0] = 1.0;
-  m.Mxi[1] = 0.5 * inK / l;
-  m.Mxi[2] = (inK * inK + 2.0 * inK) / (4.0 * (l * l));
+  m.Mxi[1] = inK * hl;
+  m.Mxi[2] = (inK * inK + 2.0 * inK) * (hl * hl);
 }
 
 // moments_conserve(Mu[, Mv], Mxi, alpha[, beta], delta) for the internal-energy

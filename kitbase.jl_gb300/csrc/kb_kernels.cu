@@ -71,7 +71,7 @@ __device__ inline float4 maxwell_exp2(double rho_n, double U, double V, double l
 }
 
 // FP32 monomial coefficients of the interface flux (see FaceCoef32).
-__device__ inline FaceCoef32 face_coef32(const Geo& g, const FaceParam& P, int flux, double dd) {
+__device__ __forceinline__ FaceCoef32 face_coef32(const Geo& g, const FaceParam& P, int flux, double dd) {
   FaceCoef32 c;
   float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
   c.E = c.T = c.G = c.Cp = c.Dp = c.Cm = c.Dm = z;
@@ -124,14 +124,14 @@ __device__ inline FaceCoef32 face_coef32(const Geo& g, const FaceParam& P, int f
 // Interface equilibrium from the two half Maxwellians (flux_kcu.jl:480-495,
 // flux_ugks.jl:47-56), then the KCU / UGKS time integrals, UGKS slopes and
 // the analytic part of fw.  One thread per face.
-template <int FLUX>
+template <int D, int FLUX>
 __global__ void k_face_param(DevState s, double dt) {
   const Geo& g = s.g;
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= s.nface_x + s.nface_y) return;
   if (s.kind[f] != 1) return;
   FaceGeo r = face_geo(g, f);
-  int NW = g.NW;
+  constexpr int NW = D + 2;
   double dxh = 0.5 * (r.d == 0 ? g.dx : g.dy);
   double len = face_len(g, r.d, r.fi, r.fj);
   FaceParam P;
@@ -166,9 +166,9 @@ __global__ void k_face_param(DevState s, double dt) {
     conserve_prim(wL, NW, g.gamma, pL);
     conserve_prim(wR, NW, g.gamma, pR);
     GM m;
-    gauss_moments(pL, NW, g.K, m);
+    gauss_moments(pL, NW, g.K, m, 1);
     moments_conserve(m.MuL, m.Mv, m.Mxi, NW, 0, 0, 0, M1);
-    gauss_moments(pR, NW, g.K, m);
+    gauss_moments(pR, NW, g.K, m, 2);
     moments_conserve(m.MuR, m.Mv, m.Mxi, NW, 0, 0, 0, M2);
     for (int k = 0; k < 4; ++k) wi[k] = k < NW ? pL[0] * M1[k] + pR[0] * M2[k] : 0.0;
     conserve_prim(wi, NW, g.gamma, p);
@@ -800,10 +800,20 @@ int launch_reconstruct(DevState& s, cudaStream_t st) {
 
 int launch_face_param(DevState& s, double dt, cudaStream_t st) {
   int nf = s.nface_x + s.nface_y;
+  const bool two = s.g.D == 2;
   switch (s.flux) {
-    case FLUX_KFVS: k_face_param<FLUX_KFVS><<<nblk(nf, 128), 128, 0, st>>>(s, dt); break;
-    case FLUX_KCU: k_face_param<FLUX_KCU><<<nblk(nf, 128), 128, 0, st>>>(s, dt); break;
-    default: k_face_param<FLUX_UGKS><<<nblk(nf, 128), 128, 0, st>>>(s, dt); break;
+    case FLUX_KFVS:
+      if (two) k_face_param<2, FLUX_KFVS><<<nblk(nf, 128), 128, 0, st>>>(s, dt);
+      else k_face_param<1, FLUX_KFVS><<<nblk(nf, 128), 128, 0, st>>>(s, dt);
+      break;
+    case FLUX_KCU:
+      if (two) k_face_param<2, FLUX_KCU><<<nblk(nf, 128), 128, 0, st>>>(s, dt);
+      else k_face_param<1, FLUX_KCU><<<nblk(nf, 128), 128, 0, st>>>(s, dt);
+      break;
+    default:
+      if (two) k_face_param<2, FLUX_UGKS><<<nblk(nf, 128), 128, 0, st>>>(s, dt);
+      else k_face_param<1, FLUX_UGKS><<<nblk(nf, 128), 128, 0, st>>>(s, dt);
+      break;
   }
   return 1;
 }
