@@ -315,12 +315,18 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     alg_b = 16.0 * cv  # read h, b once + write h, b once, FP32
     achieved = alg_b / (upd_ms / 1e3) / 1e9
+    # pass-B kernel of the tuned shape; DRAM traffic per launch from the
+    # committed ncu capture of that kernel, scaled by the cv of a launch
+    pair = best.get("march_bs") == 64
+    kname = ("k_march4 (pass B, two velocities per thread, TMA row ring)" if pair
+             else "k_march3 (pass B, one velocity per thread, TMA row ring)")
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "k_march_traffic.json")
+    tp = os.path.join(ROOT, "profiles", "k_march4_traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
             tt = json.load(f)
-        traffic = tt.get("bytes_per_cv", 0) * cv or None
+        if all(best.get(k) == v for k, v in tt.get("tuning", {}).items()):
+            traffic = tt.get("bytes_per_cv", 0) * cv or None
 
     # end to end through the C ABI: pinned host state in, K steps, state out
     barrier(pg)
@@ -422,7 +428,7 @@ def run_ours(args):
                    "state_bytes_fp32": 4 * 4 * ncell * nvel,
                    "l2": "inputs larger than L2 (state far above 129 MB), no flush",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "kernel": "k_march (pass B, pointwise update)",
+        "roofline": {"bound": "hbm", "kernel": kname,
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": alg_b, "launch_ms": upd_ms},

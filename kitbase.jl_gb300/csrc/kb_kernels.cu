@@ -7,6 +7,8 @@
 // them again from the neighbour cells, so h and b are read from HBM and
 // written once per step apart from stencil re-reads that hit L2.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <stdio.h>
 
 #include "kb_kernels.cuh"
@@ -764,12 +766,17 @@ __global__ void k_pack_w(double* dst4, const double* src, long ncell, int nw) {
 }
 
 // timestep: max over physical cells (src/Solver/solver_main.jl:240-342); one block.
+// Maximum over the physical cells of the CFL rate; each block reduces its
+// cells, then one atomic max per block on the bit pattern (the rates are
+// positive, so their IEEE bits order like unsigned integers and the result
+// does not depend on the order of the blocks).
 __global__ void k_timestep(DevState s, double umax, double vmax, double* out) {
   __shared__ double red[256];
   const Geo& g = s.g;
   double m = 0.0;
-  for (int t = threadIdx.x; t < g.nx * g.ny; t += blockDim.x) {
-    int i = t % g.nx, j = t / g.nx;
+  const long n = (long)g.nx * g.ny;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    int i = (int)(t % g.nx), j = (int)(t / g.nx);
     const double* p = s.prim + (long)cell_index(g, i, j) * 4;
     double sos = pow(0.5 * g.gamma / p[g.NW - 1], 0.5);
     double v;
@@ -783,7 +790,8 @@ __global__ void k_timestep(DevState s, double umax, double vmax, double* out) {
     if (threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
     __syncthreads();
   }
-  if (threadIdx.x == 0) *out = red[0];
+  if (threadIdx.x == 0)
+    atomicMax((unsigned long long*)out, (unsigned long long)__double_as_longlong(red[0]));
 }
 
 // ------------------------------------------------------------- launchers
@@ -927,7 +935,10 @@ int launch_pack_w(double* dst4, const double* src, long ncell, int nw, cudaStrea
 }
 
 int launch_timestep(const DevState& s, double umax, double vmax, double* out, cudaStream_t st) {
-  k_timestep<<<1, 256, 0, st>>>(s, umax, vmax, out);
+  cudaMemsetAsync(out, 0, sizeof(double), st);
+  const long n = (long)s.g.nx * s.g.ny;
+  const unsigned nb = (unsigned)std::min<long>(1184, std::max<long>(1, (n + 255) / 256));
+  k_timestep<<<nb, 256, 0, st>>>(s, umax, vmax, out);
   return 1;
 }
 
