@@ -4,7 +4,8 @@
 // Ragged layout: instance b owns cells [cell_off[b], cell_off[b] + nxt[b])
 // (ghosts included) and a velocity table at vel_off[b] of length nu[b]; its
 // distributions start at elem_off[b] in the flat h / b arrays and are
-// [cell][nu[b]] (velocity fastest).  A CTA takes instances from a work counter
+// [cell][nus[b]] (velocity fastest, rows padded to a multiple of 4 values so
+// every row starts 16-byte aligned for bulk copies).  A CTA takes instances from a work counter
 // (largest first) and runs the whole step of an instance:
 //   A  face moments fw (one thread per face looping over velocities, blocked
 //      compensated sums) and the old heat flux q (one thread per cell)
@@ -18,6 +19,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -25,6 +27,7 @@
 #include "../../include/kitgpu.h"
 #include "kb_device.cuh"
 #include "kb_kernels.cuh"
+#include "kb_tma.cuh"
 
 namespace kb {
 
@@ -34,6 +37,7 @@ struct BatchDev {
   const int* nx;         // physical cells
   const int* ng;         // ghost layers
   const int* nu;         // velocities
+  const int* nus;        // row stride of the distributions: nu rounded up to 4
   const long* cell_off;  // first cell (incl. ghosts)
   const long* elem_off;  // first distribution element
   const int* vel_off;    // velocity table offset
@@ -54,6 +58,15 @@ struct BatchDev {
   int* active;           // [n] 1 while not converged
   int* counter;          // work counter
   int* status;
+  // FP32 segment form: segment k covers cells [seg_i0[k], seg_i0[k] + SEG) of
+  // instance seg_b[k]; an instance's segments are consecutive from
+  // seg_first[b] (nseg[b] of them)
+  const int* seg_b;
+  const int* seg_i0;
+  const int* seg_first;
+  const int* nseg;
+  int* done;             // [n] segments of the instance finished this step
+  double* respart;       // [segments][8] residual partial sums
   double K, gamma, omega, Pr, tol;
   int coll;
 };
@@ -118,7 +131,7 @@ __global__ void __launch_bounds__(BS) k_batch_step(BatchDev B, const R* __restri
     __syncthreads();
     if (slot >= B.n) return;
     const int b = B.order[slot];
-    const int nx = B.nx[b], ng = B.ng[b], nu = B.nu[b];
+    const int nx = B.nx[b], ng = B.ng[b], nu = B.nu[b], ns = B.nus[b];
     const long c0 = B.cell_off[b], e0 = B.elem_off[b];
     const int nxt = nx + 2 * ng;
     const R* Hi = Hin + e0;
@@ -126,7 +139,7 @@ __global__ void __launch_bounds__(BS) k_batch_step(BatchDev B, const R* __restri
     R* Ho = Hout + e0;
     R* Bo = Bout + e0;
     if (!B.active[b]) {  // converged: carry the state over
-      for (long k = tid; k < (long)nxt * nu; k += BS) {
+      for (long k = tid; k < (long)nxt * ns; k += BS) {
         Ho[k] = Hi[k];
         Bo[k] = Bi[k];
       }
@@ -146,19 +159,19 @@ __global__ void __launch_bounds__(BS) k_batch_step(BatchDev B, const R* __restri
       s2.init();
       const int iL = f - 1, iR = f;
       const int rL = brule(iL, nx, ng), rR = brule(iR, nx, ng);
-      const R* hL = Hi + (long)(iL + ng) * nu;
-      const R* bL = Bi + (long)(iL + ng) * nu;
+      const R* hL = Hi + (long)(iL + ng) * ns;
+      const R* bL = Bi + (long)(iL + ng) * ns;
       for (int v = 0; v < nu; ++v) {
         R u = U[v];
         bool pos = u >= R(0);
-        const R* hc = pos ? hL : hL + nu;
-        const R* bc = pos ? bL : bL + nu;
+        const R* hc = pos ? hL : hL + ns;
+        const R* bc = pos ? bL : bL + ns;
         int r = pos ? rL : rR;
         R h0 = hc[v], b0 = bc[v];
         R sh = R(0), sb = R(0);
         if (r == 1) {
-          sh = bvl<R>(1, hc[v - nu], h0, hc[v + nu], epsd);
-          sb = bvl<R>(1, bc[v - nu], b0, bc[v + nu], epsd);
+          sh = bvl<R>(1, hc[v - ns], h0, hc[v + ns], epsd);
+          sb = bvl<R>(1, bc[v - ns], b0, bc[v + ns], epsd);
         }
         R side = pos ? R(0.5) : R(-0.5);
         R hf = h0 + side * sh, bf = b0 + side * sb;
@@ -183,8 +196,8 @@ __global__ void __launch_bounds__(BS) k_batch_step(BatchDev B, const R* __restri
       for (int i = 1 + tid; i <= nx - 2; i += BS) {
         BSum<R> s;
         s.init();
-        const R* hc = Hi + (long)(i + ng) * nu;
-        const R* bc = Bi + (long)(i + ng) * nu;
+        const R* hc = Hi + (long)(i + ng) * ns;
+        const R* bc = Bi + (long)(i + ng) * ns;
         R Uc = R(B.prim[(c0 + i + ng) * 4 + 1]);
         for (int v = 0; v < nu; ++v) {
           R cu = U[v] - Uc;
@@ -259,12 +272,12 @@ __global__ void __launch_bounds__(BS) k_batch_step(BatchDev B, const R* __restri
       const R u = U[v];
       const bool pos = u >= R(0);
       const R side = pos ? R(0.5) : R(-0.5);
-      auto at = [&](const R* q, int i) { return q[(long)(i + ng) * nu + v]; };
+      auto at = [&](const R* q, int i) { return q[(long)(i + ng) * ns + v]; };
       // fixed end cells keep their state
-      Ho[(long)ng * nu + v] = at(Hi, 0);
-      Bo[(long)ng * nu + v] = at(Bi, 0);
-      Ho[(long)(nx - 1 + ng) * nu + v] = at(Hi, nx - 1);
-      Bo[(long)(nx - 1 + ng) * nu + v] = at(Bi, nx - 1);
+      Ho[(long)ng * ns + v] = at(Hi, 0);
+      Bo[(long)ng * ns + v] = at(Bi, 0);
+      Ho[(long)(nx - 1 + ng) * ns + v] = at(Hi, nx - 1);
+      Bo[(long)(nx - 1 + ng) * ns + v] = at(Bi, nx - 1);
       // window: cells i-1, i, i+1 around the upwind cell of face i (between i-1 and i)
       auto face = [&](int f, R& fh, R& fb) {
         int up = pos ? f - 1 : f;
@@ -308,13 +321,329 @@ __global__ void __launch_bounds__(BS) k_batch_step(BatchDev B, const R* __restri
           hn = (h0 + (fhL - fhR) * idx + dtau * MH) * inv;
           bn = (b0 + (fbL - fbR) * idx + dtau * MB) * inv;
         }
-        Ho[(long)(i + ng) * nu + v] = hn;
-        Bo[(long)(i + ng) * nu + v] = bn;
+        Ho[(long)(i + ng) * ns + v] = hn;
+        Bo[(long)(i + ng) * ns + v] = bn;
         fhL = fhR;
         fbL = fbR;
       }
     }
     __syncthreads();
+  }
+}
+
+// ---- FP32 form: one CTA per segment of SEG cells, the whole step fused.
+// In 1D an instance has at most 256 velocities, so a segment's stencil window
+// (SEG + 4 cells x all velocities, h and b) fits in shared memory: the face
+// moments of the segment's faces, the new w / prim / tau of its cells and
+// the pointwise update all need only the old state inside that window, so
+// the step is one pass over HBM (each value read once, plus a 2-cell halo on
+// each side, and written once).  The window arrives by bulk async copies, one
+// per row, into rows whose stride is = 4 (mod 32) floats so that the face
+// threads read without bank conflicts.  Per-instance residuals are summed by
+// the instance's last segment in segment order (deterministic).
+constexpr int SEG = 16;
+constexpr int SEG_T = 128;
+constexpr int SEG_ROWS = SEG + 4;
+constexpr int SEG_MAXNU = 256;
+__host__ __device__ inline int seg_stride(int nus) { return (nus + 31) / 32 * 32 + 4; }
+constexpr int SEG_SMEM = 2 * SEG_ROWS * (SEG_MAXNU + 4) * 4 + 2 * SEG_MAXNU * 4 +
+                         (SEG + 1) * 3 * 8 + SEG * 8 + SEG * 12 * 4 + 8 * 8;
+
+__global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __restrict__ Hin,
+                                                     const float* __restrict__ Bin,
+                                                     float* __restrict__ Hout,
+                                                     float* __restrict__ Bout) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ unsigned long long bar;
+  __shared__ float sconst[4];  // T3, T4, 1/dx, 1e-7 dx
+  // GB300 runs FP64 at 1/64 of the FP32 rate: FP64 work below is done by as
+  // few warps as possible (the per-instance constants by one thread, the
+  // cell update and its residual by the first warp)
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int k = blockIdx.x;
+  const int b = B.seg_b[k], i0 = B.seg_i0[k];
+  const int nx = B.nx[b], ng = B.ng[b], nu = B.nu[b], ns = B.nus[b];
+  const int i1 = min(i0 + SEG, nx);
+  const long c0 = B.cell_off[b], e0 = B.elem_off[b];
+  const float* Hi = Hin + e0;
+  const float* Bi = Bin + e0;
+  float* Ho = Hout + e0;
+  float* Bo = Bout + e0;
+  if (!B.active[b]) {  // converged: carry this segment's cells over
+    for (long t = tid; t < (long)(i1 - i0) * ns; t += SEG_T) {
+      const long o = (long)(i0 + ng) * ns + t;
+      Ho[o] = Hi[o];
+      Bo[o] = Bi[o];
+    }
+    return;
+  }
+  const int sst = seg_stride(ns);
+  float* sH = (float*)sm;
+  float* sB = sH + SEG_ROWS * (SEG_MAXNU + 4);
+  float* sU = sB + SEG_ROWS * (SEG_MAXNU + 4);
+  float* sW = sU + SEG_MAXNU;
+  double* sfw = (double*)(sW + SEG_MAXNU);  // [SEG + 1][3]
+  double* sq = sfw + (SEG + 1) * 3;          // [SEG]
+  float* scc = (float*)(sq + SEG);           // [SEG][12]
+  // window rows r0 .. r1-1 (cells incl. ghosts), smem row = cell - r0
+  const int r0 = max(i0 - 2, -ng), r1 = min(i1 + 2, nx + ng), nrow = r1 - r0;
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    fence_async_smem();
+  }
+  __syncthreads();
+  if (tid < 32) {
+    if (lane == 0) mbar_expect(&bar, 2u * nrow * ns * 4u);
+    __syncwarp();
+    for (int r = lane; r < 2 * nrow; r += 32) {
+      const int row = r >> 1;
+      const float* src = ((r & 1) ? Bi : Hi) + (long)(r0 + row + ng) * ns;
+      float* dst = ((r & 1) ? sB : sH) + row * sst;
+      bulk_g2s(dst, src, (unsigned)ns * 4u, &bar);
+    }
+  }
+  for (int v = tid; v < nu; v += SEG_T) {
+    sU[v] = B.uf[B.vel_off[b] + v];
+    sW[v] = B.wtf[B.vel_off[b] + v];
+  }
+  if (tid == 0) {
+    const double dx0 = B.dx[b], dt0 = B.dt[b];
+    sconst[0] = float(dt0);
+    sconst[1] = float(0.5 * dt0 * dt0 / dx0);
+    sconst[2] = float(1.0 / dx0);
+    sconst[3] = float(1.e-7 * dx0);
+  }
+  // one thread waits for the window; the others wait at the CTA barrier
+  const bool ok = tid == 0 ? mbar_wait(&bar, 0) : true;
+  if (__syncthreads_or(!ok)) {  // CTA-uniform: bounded clean-up, then leave
+    if (tid == 0) {
+      atomicOr(B.status, 2);
+      mbar_wait(&bar, 0);
+    }
+    return;
+  }
+  const float epsd = sconst[3];
+  const float T3 = sconst[0], T4 = sconst[1];
+  auto rowH = [&](int c) { return sH + (c - r0) * sst; };
+  auto rowB = [&](int c) { return sB + (c - r0) * sst; };
+
+  // ---- face moments of faces fa .. fb (4 threads per face, velocities v = q mod 4)
+  const int fa = max(i0, 1), fb = min(i1, nx - 1);
+  const int ca = max(i0, 1), cb = min(i1, nx - 1);  // stepped cells [ca, cb)
+  {
+    const int j = tid >> 2, q = tid & 3;
+    const int f = fa + j;
+    BSum<float> s0, s1, s2;
+    s0.init();
+    s1.init();
+    s2.init();
+    if (f <= fb) {
+      const int iL = f - 1, iR = f;
+      const int rL = brule(iL, nx, ng), rR = brule(iR, nx, ng);
+      int it = 0;
+      for (int v = q; v < nu; v += 4, ++it) {
+        const float u = sU[v];
+        const bool pos = u >= 0.f;
+        const int c = pos ? iL : iR;
+        const int r = pos ? rL : rR;
+        const float* hc = rowH(c);
+        const float* bc = rowB(c);
+        const float h0 = hc[v], b0 = bc[v];
+        float sh = 0.f, sb = 0.f;
+        if (r == 1) {
+          sh = bvl<float>(1, hc[v - sst], h0, hc[v + sst], epsd);
+          sb = bvl<float>(1, bc[v - sst], b0, bc[v + sst], epsd);
+        }
+        const float side = pos ? 0.5f : -0.5f;
+        const float hf = h0 + side * sh, bf = b0 + side * sb;
+        const float fh = T3 * u * hf - T4 * (u * u) * sh;
+        const float fbb = T3 * u * bf - T4 * (u * u) * sb;
+        const float wf = sW[v] * fh;
+        s0.add(wf);
+        s1.add(wf * u);
+        s2.add(wf * u * u + sW[v] * fbb);
+        if ((it & 7) == 7) {
+          s0.flush();
+          s1.flush();
+          s2.flush();
+        }
+      }
+    }
+    // the 4 threads of a face: compensated pair sums over lanes q
+    DF d0, d1, d2;
+    s0.flush();
+    s1.flush();
+    s2.flush();
+    d0 = s0.d;
+    d1 = s1.d;
+    d2 = s2.d;
+#pragma unroll
+    for (int m = 1; m <= 2; m <<= 1) {
+      d0 = df_merge(d0, df_shfl_xor(d0, m));
+      d1 = df_merge(d1, df_shfl_xor(d1, m));
+      d2 = df_merge(d2, df_shfl_xor(d2, m));
+    }
+    if (q == 0 && f <= fb) {
+      sfw[j * 3 + 0] = (double)d0.hi + (double)d0.lo;
+      sfw[j * 3 + 1] = (double)d1.hi + (double)d1.lo;
+      sfw[j * 3 + 2] = 0.5 * ((double)d2.hi + (double)d2.lo);
+    }
+  }
+  // ---- old heat flux of the stepped cells (Shakhov), 4 threads per cell
+  if (B.coll == COLL_SHAKHOV) {
+    const int j = tid >> 2, q = tid & 3;
+    const int i = ca + j;
+    BSum<float> s;
+    s.init();
+    if (i < cb) {
+      const float Uc = float(B.prim[(c0 + i + ng) * 4 + 1]);
+      const float* hc = rowH(i);
+      const float* bc = rowB(i);
+      int it = 0;
+      for (int v = q; v < nu; v += 4, ++it) {
+        const float cu = sU[v] - Uc;
+        s.add(sW[v] * cu * (cu * cu * hc[v] + bc[v]));
+        if ((it & 7) == 7) s.flush();
+      }
+    }
+    s.flush();
+    DF d = s.d;
+#pragma unroll
+    for (int m = 1; m <= 2; m <<= 1) d = df_merge(d, df_shfl_xor(d, m));
+    if (q == 0 && i < cb) sq[j] = 0.5 * ((double)d.hi + (double)d.lo);
+  }
+  __syncthreads();
+  // ---- cell parameters of the stepped cells (one thread per cell, FP64)
+  double rr[6] = {0, 0, 0, 0, 0, 0};
+  if (tid < cb - ca) {
+    const double dx = B.dx[b], dt = B.dt[b];
+    const int i = ca + tid;
+    const long c = c0 + i + ng;
+    double* w = B.w + c * 4;
+    double* p = B.prim + c * 4;
+    const double* fL = sfw + (i - fa) * 3;
+    const double* fR = sfw + (i + 1 - fa) * 3;
+    double wo[3] = {w[0], w[1], w[2]};
+    double lo = p[2], rho_o = p[0], Uo = p[1];
+    const double idx = 1.0 / dx;
+    for (int m = 0; m < 3; ++m) w[m] += (fL[m] - fR[m]) * idx;
+    double pn[4];
+    conserve_prim(w, 3, B.gamma, pn);
+    p[0] = pn[0];
+    p[1] = pn[1];
+    p[2] = pn[2];
+    for (int m = 0; m < 3; ++m) {
+      double d = w[m] - wo[m];
+      rr[m] += d * d;
+      rr[3 + m] += fabs(w[m]);
+    }
+    double lam = pn[2];
+    if (!(pn[0] > 0.0) || !(lam > 0.0) || !isfinite(pn[0]) || !isfinite(lam)) atomicOr(B.status, 1);
+    // w, prim and q stay FP64; the coefficients below feed only the FP32
+    // pointwise update, so they are formed in FP32 (GB300's FP64 rate is
+    // 1/64 of its FP32 rate, and in 1D a cell has only ~100 velocities)
+    const float rf = float(pn[0]), lf = float(lam), rof = float(rho_o), lof = float(lo);
+    const float tau = float(B.mu[b]) * 2.f * powf(lf, float(1.0 - B.omega)) / rf;
+    const float dtt = float(dt) / tau;
+    const float Kf = float(B.K);
+    float* kc = scc + tid * 12;
+    kc[0] = rf * sqrtf(lf * float(1.0 / PI));  // new Maxwellian
+    kc[1] = float(pn[1]);
+    kc[2] = lf;
+    kc[3] = Kf / (2.f * lf);
+    kc[4] = dtt;
+    kc[5] = 1.f / (1.f + dtt);
+    kc[6] = rof * sqrtf(lof * float(1.0 / PI));  // old Maxwellian (Shakhov)
+    kc[7] = float(Uo);
+    kc[8] = lof;
+    kc[9] = Kf / (2.f * lof);
+    kc[10] = B.coll == COLL_SHAKHOV ? float(0.8 * (1.0 - B.Pr)) * (lof * lof) / rof * float(sq[tid]) : 0.f;
+  }
+  // residual partial sums of the segment: the cells are all in the first
+  // warp (SEG <= 32), reduced in a fixed shuffle order
+  static_assert(SEG <= 32, "the cell update of a segment runs in the first warp");
+  if (wid == 0) {
+    for (int m = 0; m < 6; ++m) {
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) rr[m] += __shfl_xor_sync(0xffffffffu, rr[m], o);
+    }
+  }
+  __syncthreads();  // cell coefficients ready for the pointwise update
+  // ---- pointwise KFVS flux + relaxation, one thread per velocity
+  const float idx = sconst[2];
+  for (int v = tid; v < nu; v += SEG_T) {
+    const float u = sU[v];
+    const bool pos = u >= 0.f;
+    const float side = pos ? 0.5f : -0.5f;
+    if (i0 == 0) {  // fixed end cells keep their state
+      Ho[(long)ng * ns + v] = rowH(0)[v];
+      Bo[(long)ng * ns + v] = rowB(0)[v];
+    }
+    if (i1 == nx) {
+      Ho[(long)(nx - 1 + ng) * ns + v] = rowH(nx - 1)[v];
+      Bo[(long)(nx - 1 + ng) * ns + v] = rowB(nx - 1)[v];
+    }
+    auto face = [&](int f, float& fh, float& fbv) {
+      const int up = pos ? f - 1 : f;
+      const int r = brule(up, nx, ng);
+      const float* hc = rowH(up);
+      const float* bc = rowB(up);
+      const float h0 = hc[v], b0 = bc[v];
+      float sh = 0.f, sb = 0.f;
+      if (r == 1) {
+        sh = bvl<float>(1, hc[v - sst], h0, hc[v + sst], epsd);
+        sb = bvl<float>(1, bc[v - sst], b0, bc[v + sst], epsd);
+      }
+      const float hf = h0 + side * sh, bf = b0 + side * sb;
+      fh = T3 * u * hf - T4 * (u * u) * sh;
+      fbv = T3 * u * bf - T4 * (u * u) * sb;
+    };
+    float fhL = 0.f, fbL = 0.f;
+    if (ca < cb) face(ca, fhL, fbL);
+    for (int i = ca; i < cb; ++i) {
+      float fhR, fbR;
+      face(i + 1, fhR, fbR);
+      const float* kc = scc + (i - ca) * 12;
+      const float h0 = rowH(i)[v], b0 = rowB(i)[v];
+      const float du = u - kc[1];
+      const float M = kc[0] * mexp(-kc[2] * du * du);
+      float MH = M, MB = M * kc[3];
+      if (B.coll == COLL_SHAKHOV) {
+        const float ou = u - kc[7];
+        const float OH = kc[6] * mexp(-kc[8] * ou * ou);
+        const float cq = kc[10] * ou;
+        const float tl = 2.f * kc[8] * ou * ou + float(B.K);
+        MH += cq * (tl - 5.f) * OH;
+        MB += cq * (tl - 3.f) * OH * kc[9];
+      }
+      const float dtau = kc[4], inv = kc[5];
+      Ho[(long)(i + ng) * ns + v] = (h0 + (fhL - fhR) * idx + dtau * MH) * inv;
+      Bo[(long)(i + ng) * ns + v] = (b0 + (fbL - fbR) * idx + dtau * MB) * inv;
+      fhL = fhR;
+      fbL = fbR;
+    }
+  }
+  // ---- the instance's last segment sums the partials in segment order
+  if (tid == 0) {
+    double* pr = B.respart + (long)k * 8;
+    for (int m = 0; m < 6; ++m) pr[m] = rr[m];
+    __threadfence();
+    const int prev = atomicAdd(&B.done[b], 1);
+    if (prev == B.nseg[b] - 1) {
+      __threadfence();
+      double t[6] = {0, 0, 0, 0, 0, 0};
+      const int s0 = B.seg_first[b], s1 = s0 + B.nseg[b];
+      for (int sgi = s0; sgi < s1; ++sgi)
+        for (int m = 0; m < 6; ++m) t[m] += __ldcg(B.respart + (long)sgi * 8 + m);
+      double mx = 0.0;
+      for (int m = 0; m < 3; ++m) {
+        double r = sqrt(t[m] * nx) / (t[3 + m] + 1.e-7);
+        B.residual[b * 4 + m] = r;
+        mx = fmax(mx, r);
+      }
+      if (mx < B.tol) B.active[b] = 0;
+      B.done[b] = 0;
+    }
   }
 }
 
@@ -362,8 +691,9 @@ struct kb_batch {
   int cur = 0;
   cudaStream_t stream = nullptr;
   std::vector<void*> allocs;
-  std::vector<int> nx, ng, nu;
-  std::vector<long> cell_off, elem_off;
+  std::vector<int> nx, ng, nu, nus;
+  std::vector<long> cell_off, elem_off, dense_off;  // dense_off: caller layout [cell][nu]
+  long ndense = 0, nseg = 0;
   double* d_stage = nullptr;
   double* d_umax = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -428,18 +758,33 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   B->cell_off.resize(n);
   B->elem_off.resize(n);
   long cells = 0, elems = 0, faces = 0, vels = 0;
+  B->nus.resize(n);
+  B->dense_off.resize(n);
+  std::vector<int> seg_b, seg_i0, seg_first(n), nseg(n);
+  long dense = 0;
   for (int b = 0; b < n; ++b) {
     B->cell_off[b] = cells;
     B->elem_off[b] = elems;
+    B->dense_off[b] = dense;
     face_off[b] = faces;
     vel_off[b] = (int)vels;
     long nxt = nx[b] + 2 * ngx[b];
+    B->nus[b] = (nu[b] + 3) / 4 * 4;
     cells += nxt;
-    elems += nxt * nu[b];
+    elems += nxt * B->nus[b];
+    dense += nxt * nu[b];
     faces += nx[b] + 1;
     vels += nu[b];
     dx[b] = (x1[b] - x0[b]) / nx[b];
+    seg_first[b] = (int)seg_b.size();
+    nseg[b] = (nx[b] + kb::SEG - 1) / kb::SEG;
+    for (int k = 0; k < nseg[b]; ++k) {
+      seg_b.push_back(b);
+      seg_i0.push_back(k * kb::SEG);
+    }
   }
+  B->ndense = dense;
+  B->nseg = (long)seg_b.size();
   B->ncell = cells;
   B->nelem = elems;
   B->nface = faces;
@@ -462,6 +807,8 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   if ((rc = balloc(B, &p, sizeof(T) * (size_t)(count))) != KB_OK) return fail_out(rc); \
   dst = (T*)p;
   int *d_order, *d_nx, *d_ng, *d_nu, *d_vo, *d_active, *d_counter, *d_status;
+  int *d_nus, *d_segb, *d_segi0, *d_segfirst, *d_nseg, *d_done;
+  double* d_respart;
   long *d_co, *d_eo, *d_fo;
   double *d_dx, *d_dt, *d_mu, *d_u, *d_w, *d_wv, *d_prim, *d_fw, *d_q, *d_cp, *d_res;
   float *d_uf, *d_wf;
@@ -469,6 +816,13 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   BALLOC(d_nx, int, n);
   BALLOC(d_ng, int, n);
   BALLOC(d_nu, int, n);
+  BALLOC(d_nus, int, n);
+  BALLOC(d_segb, int, B->nseg);
+  BALLOC(d_segi0, int, B->nseg);
+  BALLOC(d_segfirst, int, n);
+  BALLOC(d_nseg, int, n);
+  BALLOC(d_done, int, n);
+  BALLOC(d_respart, double, B->nseg * 8);
   BALLOC(d_vo, int, n);
   BALLOC(d_active, int, n);
   BALLOC(d_counter, int, 2);
@@ -496,6 +850,11 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
     if ((rc = balloc(B, &B->bq[k], esz * elems)) != KB_OK) return fail_out(rc);
   }
   BALLOC(B->d_stage, double, elems);
+  // padding values of the distribution rows stay zero in both buffers
+  for (int k = 0; k < 2; ++k) {
+    cudaMemset(B->h[k], 0, esz * elems);
+    cudaMemset(B->bq[k], 0, esz * elems);
+  }
 #undef BALLOC
   std::vector<float> uf(u_all, u_all + vels), wf(w_all, w_all + vels);
   std::vector<int> ones(n, 1);
@@ -504,6 +863,13 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   ok &= cudaMemcpy(d_nx, nx, sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_ng, ngx, sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_nu, nu, sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_nus, B->nus.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_segb, seg_b.data(), sizeof(int) * B->nseg, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_segi0, seg_i0.data(), sizeof(int) * B->nseg, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_segfirst, seg_first.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_nseg, nseg.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemset(d_done, 0, sizeof(int) * n) == cudaSuccess;
+  ok &= cudaMemset(d_respart, 0, sizeof(double) * B->nseg * 8) == cudaSuccess;
   ok &= cudaMemcpy(d_vo, vel_off.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_active, ones.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_co, B->cell_off.data(), sizeof(long) * n, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -528,6 +894,13 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   d.nx = d_nx;
   d.ng = d_ng;
   d.nu = d_nu;
+  d.nus = d_nus;
+  d.seg_b = d_segb;
+  d.seg_i0 = d_segi0;
+  d.seg_first = d_segfirst;
+  d.nseg = d_nseg;
+  d.done = d_done;
+  d.respart = d_respart;
   d.cell_off = d_co;
   d.elem_off = d_eo;
   d.vel_off = d_vo;
@@ -580,9 +953,16 @@ extern "C" int kb_batch_upload(kb_batch_t* B, const double* w, const double* pri
     return bfail(KB_ERR_CUDA, "kb_batch_upload: copy failed");
   const long n = B->nelem;
   const unsigned g = (unsigned)((n + 255) / 256);
+  std::vector<double> pad(n, 0.0);  // caller rows of nu values -> padded rows
   for (int which = 0; which < 2; ++which) {
     const double* src = which == 0 ? h : bq;
-    if (cudaMemcpy(B->d_stage, src, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+    for (int b = 0; b < B->n; ++b) {
+      const long nxt = B->nx[b] + 2 * B->ng[b];
+      for (long c = 0; c < nxt; ++c)
+        std::memcpy(&pad[B->elem_off[b] + c * B->nus[b]], src + B->dense_off[b] + c * B->nu[b],
+                    sizeof(double) * B->nu[b]);
+    }
+    if (cudaMemcpy(B->d_stage, pad.data(), sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess)
       return bfail(KB_ERR_CUDA, "kb_batch_upload: copy failed");
     for (int k = 0; k < 2; ++k) {
       void* dst = which == 0 ? B->h[k] : B->bq[k];
@@ -617,6 +997,7 @@ extern "C" int kb_batch_download(kb_batch_t* B, double* w, double* prim, double*
   }
   const long n = B->nelem;
   const unsigned g = (unsigned)((n + 255) / 256);
+  std::vector<double> pad(n);
   for (int which = 0; which < 2; ++which) {
     double* dst = which == 0 ? h : bq;
     if (!dst) continue;
@@ -627,7 +1008,13 @@ extern "C" int kb_batch_download(kb_batch_t* B, double* w, double* prim, double*
       kb::k_batch_back<float><<<g, 256, 0, B->stream>>>(B->d_stage, (const float*)src, n);
     B->launches++;
     cudaStreamSynchronize(B->stream);
-    cudaMemcpy(dst, B->d_stage, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaMemcpy(pad.data(), B->d_stage, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    for (int b = 0; b < B->n; ++b) {
+      const long nxt = B->nx[b] + 2 * B->ng[b];
+      for (long c = 0; c < nxt; ++c)
+        std::memcpy(dst + B->dense_off[b] + c * B->nu[b], &pad[B->elem_off[b] + c * B->nus[b]],
+                    sizeof(double) * B->nu[b]);
+    }
   }
   if (cudaGetLastError() != cudaSuccess) return bfail(KB_ERR_CUDA, "kb_batch_download failed");
   return KB_OK;
@@ -651,6 +1038,12 @@ extern "C" int kb_batch_set_dt(kb_batch_t* B, const double* dt) {
 }
 
 static void batch_launch(kb_batch* B, int cur) {
+  if (B->prec == KB_PREC_FP32) {  // fused segments (one pass over HBM)
+    kb::k_batch_seg<<<(unsigned)B->nseg, kb::SEG_T, kb::SEG_SMEM, B->stream>>>(
+        B->d, (const float*)B->h[cur], (const float*)B->bq[cur], (float*)B->h[cur ^ 1],
+        (float*)B->bq[cur ^ 1]);
+    return;
+  }
   cudaMemsetAsync(B->d.counter, 0, sizeof(int), B->stream);
   if (B->prec == KB_PREC_FP64)
     kb::k_batch_step<double, 256><<<B->grid, 256, 0, B->stream>>>(
