@@ -77,6 +77,18 @@ __device__ __forceinline__ R bvl(int rule, R qm, R q0, R qp, R epsd) {
   if (rule == 1) return (a * fabs(b) + b * fabs(a)) / (fabs(a) + fabs(b) + epsd);
   return R(0);
 }
+// FP32 form: one reciprocal and one multiply (subnormals flushed), the
+// division the FP32 passes of the 2D solver use as well
+template <>
+__device__ __forceinline__ float bvl<float>(int rule, float qm, float q0, float qp, float epsd) {
+  float a = q0 - qm, b = qp - q0;
+  if (rule != 1) return 0.f;
+  float r;
+  asm("div.approx.ftz.f32 %0, %1, %2;"
+      : "=f"(r)
+      : "f"(a * fabsf(b) + b * fabsf(a)), "f"(fabsf(a) + fabsf(b) + epsd));
+  return r;
+}
 
 // 1D slope rule: van Leer everywhere inside when ghosts exist, boundary cells
 // flat without ghosts (src/Solver/solver_reconstruction.jl:101-153).
@@ -329,6 +341,13 @@ __global__ void __launch_bounds__(BS) k_batch_step(BatchDev B, const R* __restri
     }
     __syncthreads();
   }
+}
+
+// e^x on the MUFU unit (2^(x log2 e), results below 2^-126 flushed to zero)
+__device__ __forceinline__ float fexp(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x * 1.4426950408889634f));
+  return y;
 }
 
 // ---- FP32 form: one CTA per segment of SEG cells, the whole step fused.
@@ -606,11 +625,11 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
       const float* kc = scc + (i - ca) * 12;
       const float h0 = rowH(i)[v], b0 = rowB(i)[v];
       const float du = u - kc[1];
-      const float M = kc[0] * mexp(-kc[2] * du * du);
+      const float M = kc[0] * fexp(-kc[2] * du * du);
       float MH = M, MB = M * kc[3];
       if (B.coll == COLL_SHAKHOV) {
         const float ou = u - kc[7];
-        const float OH = kc[6] * mexp(-kc[8] * ou * ou);
+        const float OH = kc[6] * fexp(-kc[8] * ou * ou);
         const float cq = kc[10] * ou;
         const float tl = 2.f * kc[8] * ou * ou + float(B.K);
         MH += cq * (tl - 5.f) * OH;
@@ -1039,6 +1058,14 @@ extern "C" int kb_batch_set_dt(kb_batch_t* B, const double* dt) {
 
 static void batch_launch(kb_batch* B, int cur) {
   if (B->prec == KB_PREC_FP32) {  // fused segments (one pass over HBM)
+    static bool raised[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (kb::SEG_SMEM > 48 * 1024 && dev >= 0 && dev < 64 && !raised[dev]) {
+      cudaFuncSetAttribute(kb::k_batch_seg, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kb::SEG_SMEM);
+      raised[dev] = true;
+    }
     kb::k_batch_seg<<<(unsigned)B->nseg, kb::SEG_T, kb::SEG_SMEM, B->stream>>>(
         B->d, (const float*)B->h[cur], (const float*)B->bq[cur], (float*)B->h[cur ^ 1],
         (float*)B->bq[cur ^ 1]);
