@@ -111,6 +111,13 @@ int kb_set_wall(kb_handle_t* h, int side, const double* host_prim);
 int kb_upload_state(kb_handle_t* h, const double* w, const double* prim,
                     const double* hdist, const double* bdist);
 
+/* Set every cell (incl. ghosts) to its equilibrium: w and prim from the host
+ * ([ncell][dim+2]), h = maxwellian(u, prim) and b = h K / (2 lambda) computed on
+ * the device, the way init_fvm builds them (src/Solver/solver_init.jl:119-141,
+ * :285-325; src/Theory/theory_equilibrium.jl:8-25).  Moves only w and prim
+ * across the bus, so a new solve starts without a host-built distribution. */
+int kb_init_equilibrium(kb_handle_t* h, const double* w, const double* prim);
+
 /* Copy the whole cell state device -> host (same layout as kb_upload_state).
  * Any pointer may be NULL to skip that field.  Feeds write_jld / extract_sol. */
 int kb_download_state(kb_handle_t* h, double* w, double* prim, double* hdist,

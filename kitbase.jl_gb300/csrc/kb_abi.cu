@@ -39,6 +39,12 @@ struct kb_handle {
   double* h_res = nullptr;    // pinned host copy of residual[4] + status
   cudaEvent_t ev_done = nullptr;
   bool pending = false;
+  // chunks of kb_step_async replayed as CUDA graphs: one executable graph per
+  // starting buffer index, valid for one (dt, nsteps) and the current tuning
+  cudaGraphExec_t agraph[2] = {nullptr, nullptr};
+  double agraph_dt = 0.0;
+  int agraph_n = 0;
+  int64_t agraph_launches = 0;
   // per-stage kernel timing (kb_set_timing): CUDA events on the handle stream
   bool timing = false;
   std::vector<cudaEvent_t> events;
@@ -327,7 +333,10 @@ int kb_create(const kb_config_t* cfg, const double* u, const double* v, const do
   kb::face_kinds_host(g, kinds.data());
   if (cudaMemcpy(h->s.kind, kinds.data(), h->nface, cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(fail(KB_ERR_CUDA, "face kind upload failed"));
-  if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(KB_ERR_CUDA, "init failed"));
+  // the set-up copies above are synchronous; wait for this handle's stream
+  // only, so that creating a handle never waits for other solves' work
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+    return bail(fail(KB_ERR_CUDA, "init failed"));
   *out = h;
   return KB_OK;
 }
@@ -337,6 +346,8 @@ int kb_destroy(kb_handle_t* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   if (h->ev_done) cudaEventDestroy(h->ev_done);
+  for (int k = 0; k < 2; ++k)
+    if (h->agraph[k]) cudaGraphExecDestroy(h->agraph[k]);
   if (h->h_res) cudaFreeHost(h->h_res);
   for (void* p : h->allocs) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -412,6 +423,32 @@ int kb_upload_state(kb_handle_t* h, const double* w, const double* prim, const d
   KB_TRY(dist_in(h, h->s.b[0], bdist));
   // both ping-pong buffers start equal: ghost cells of fix / Maxwell solves are
   // never rewritten, so the second buffer must hold them too
+  size_t dist = (size_t)h->ncell * h->vstride * (h->s.prec == KB_PREC_FP64 ? 8 : 4);
+  KB_CUDA(cudaMemcpyAsync(h->s.h[1], h->s.h[0], dist, cudaMemcpyDeviceToDevice, h->stream));
+  KB_CUDA(cudaMemcpyAsync(h->s.b[1], h->s.b[0], dist, cudaMemcpyDeviceToDevice, h->stream));
+  KB_TRY(sync(h));
+  h->evolved = false;
+  return KB_OK;
+}
+
+int kb_init_equilibrium(kb_handle_t* h, const double* w, const double* prim) {
+  if (!h || !w || !prim) return fail(KB_ERR_ARG, "kb_init_equilibrium: null argument");
+  int NW = h->s.g.NW;
+  for (long c = 0; c < h->ncell; ++c)
+    if (!(prim[c * NW] > 0.0) || !(prim[c * NW + NW - 1] > 0.0))
+      return fail(KB_ERR_ARG, "kb_init_equilibrium: density and lambda must be positive");
+  std::vector<double> w4((size_t)h->ncell * 4, 0.0), p4((size_t)h->ncell * 4, 0.0);
+  for (long c = 0; c < h->ncell; ++c)
+    for (int k = 0; k < NW; ++k) {
+      w4[c * 4 + k] = w[c * NW + k];
+      p4[c * 4 + k] = prim[c * NW + k];
+    }
+  KB_CUDA(cudaMemcpyAsync(h->s.w, w4.data(), sizeof(double) * w4.size(), cudaMemcpyHostToDevice, h->stream));
+  KB_CUDA(cudaMemcpyAsync(h->s.prim, p4.data(), sizeof(double) * p4.size(), cudaMemcpyHostToDevice, h->stream));
+  KB_CUDA(cudaMemsetAsync(h->s.sw, 0, sizeof(double) * h->ncell * 8, h->stream));
+  KB_CUDA(cudaMemsetAsync(h->s.status, 0, sizeof(int), h->stream));
+  h->s.cur = 0;
+  KB_TRY(check_launch(h, kb::launch_init_equilibrium(h->s, h->stream)));
   size_t dist = (size_t)h->ncell * h->vstride * (h->s.prec == KB_PREC_FP64 ? 8 : 4);
   KB_CUDA(cudaMemcpyAsync(h->s.h[1], h->s.h[0], dist, cudaMemcpyDeviceToDevice, h->stream));
   KB_CUDA(cudaMemcpyAsync(h->s.b[1], h->s.b[0], dist, cudaMemcpyDeviceToDevice, h->stream));
@@ -550,6 +587,26 @@ int kb_step(kb_handle_t* h, double dt, int32_t nsteps, double* residual) {
   return read_residual(h, residual);
 }
 
+// Forget the recorded step graphs of kb_step_async.
+static void drop_graphs(kb_handle* h) {
+  for (int k = 0; k < 2; ++k)
+    if (h->agraph[k]) {
+      cudaGraphExecDestroy(h->agraph[k]);
+      h->agraph[k] = nullptr;
+    }
+}
+
+// nsteps steps enqueued kernel by kernel on the handle stream.
+static int enqueue_steps(kb_handle* h, double dt, int nsteps) {
+  int n = 0;
+  for (int s = 0; s < nsteps; ++s) {
+    n += kb::launch_reconstruct(h->s, h->stream);
+    n += kb::launch_evolve(h->s, dt, h->stream);
+    n += kb::launch_update(h->s, dt, h->stream);
+  }
+  return n;
+}
+
 int kb_step_async(kb_handle_t* h, double dt, int32_t nsteps) {
   if (!h) return fail(KB_ERR_ARG, "kb_step_async: null handle");
   if (!(dt > 0.0)) return fail(KB_ERR_ARG, "kb_step_async: dt must be positive");
@@ -558,11 +615,44 @@ int kb_step_async(kb_handle_t* h, double dt, int32_t nsteps) {
     KB_CUDA(cudaMallocHost((void**)&h->h_res, sizeof(double) * 5));
     KB_CUDA(cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming));
   }
-  for (int s = 0; s < nsteps; ++s) {
-    int n = kb::launch_reconstruct(h->s, h->stream);
-    n += kb::launch_evolve(h->s, dt, h->stream);
-    n += kb::launch_update(h->s, dt, h->stream);
-    KB_TRY(check_launch(h, n));
+  // A served request advances in equal chunks with one dt, so the chunk's
+  // ~8 kernels per step are recorded once per starting buffer as a CUDA graph
+  // and replayed: one launch per chunk instead of hundreds keeps the host
+  // from becoming the bottleneck when many small solves share the GPU.  The
+  // first chunk of a shape runs eagerly (module loading and function
+  // attributes happen outside a capture) and is recorded for the next one.
+  const int c = h->s.cur;
+  if (nsteps > 0 && h->agraph[c] && h->agraph_dt == dt && h->agraph_n == nsteps) {
+    KB_CUDA(cudaGraphLaunch(h->agraph[c], h->stream));
+    h->launches += h->agraph_launches;
+    h->s.cur = c ^ (nsteps & 1);
+  } else {
+    // record only a chunk shape seen twice in a row (a request's last, shorter
+    // chunk is not worth a recording)
+    const bool again = h->agraph_dt == dt && h->agraph_n == nsteps;
+    if (!again) {
+      drop_graphs(h);
+      h->agraph_dt = dt;
+      h->agraph_n = nsteps;
+    }
+    KB_TRY(check_launch(h, enqueue_steps(h, dt, nsteps)));
+    if (again && nsteps > 0 && !h->agraph[c]) {
+      // record the same chunk from buffer c for the next calls
+      const int after = h->s.cur;
+      h->s.cur = c;
+      cudaGraph_t gr = nullptr;
+      bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      int n = ok ? enqueue_steps(h, dt, nsteps) : 0;
+      ok = cudaStreamEndCapture(h->stream, &gr) == cudaSuccess && ok;
+      if (ok && cudaGraphInstantiate(&h->agraph[c], gr, 0) == cudaSuccess) {
+        h->agraph_launches = n;
+      } else {
+        h->agraph[c] = nullptr;
+      }
+      if (gr) cudaGraphDestroy(gr);
+      cudaGetLastError();  // a failed recording only means no replay
+      h->s.cur = after;
+    }
   }
   KB_CUDA(cudaMemcpyAsync(h->h_res, h->s.residual, sizeof(double) * 4, cudaMemcpyDeviceToHost,
                           h->stream));
@@ -627,6 +717,7 @@ int kb_set_tuning(kb_handle_t* h, const int32_t* params, int32_t n) {
     if (!ok) return fail(KB_ERR_ARG, "kb_set_tuning: value out of range for parameter " + std::to_string(k));
   }
   for (int k = 0; k < n; ++k) h->s.tune[k] = params[k];
+  drop_graphs(h);  // recorded launch shapes are stale
   return KB_OK;
 }
 

@@ -794,6 +794,31 @@ __global__ void k_timestep(DevState s, double umax, double vmax, double* out) {
     atomicMax((unsigned long long*)out, (unsigned long long)__double_as_longlong(red[0]));
 }
 
+// Equilibrium initial distributions of init_fvm (src/Solver/solver_init.jl:
+// 119-141, :285-325): h = maxwellian(u, prim) (src/Theory/theory_equilibrium.jl:
+// 8-25), b = h K / (2 lambda), for every cell incl. ghosts.  One block per cell.
+template <typename R>
+__global__ void k_init_eq(DevState s, R* __restrict__ H, R* __restrict__ Bq) {
+  const Geo& g = s.g;
+  const long c = blockIdx.x;
+  const double* p = s.prim + c * 4;
+  const double rho = p[0], U = p[1], V = g.D == 2 ? p[2] : 0.0, lam = p[g.NW - 1];
+  const double rn = g.D == 1 ? rho * sqrt(lam / PI) : rho * (lam / PI);
+  const double cB = g.K / (2.0 * lam);
+  const long vs = g.vstride;
+  for (int v = threadIdx.x; v < g.nvel; v += blockDim.x) {
+    const double du = s.u[v] - U;
+    double e = du * du;
+    if (g.D == 2) {
+      const double dv = s.v[v] - V;
+      e += dv * dv;
+    }
+    const double M = rn * exp(-lam * e);
+    H[c * vs + v] = (R)M;
+    Bq[c * vs + v] = (R)(M * cB);
+  }
+}
+
 // ------------------------------------------------------------- launchers
 
 static inline unsigned nblk(long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -939,6 +964,12 @@ int launch_timestep(const DevState& s, double umax, double vmax, double* out, cu
   const long n = (long)s.g.nx * s.g.ny;
   const unsigned nb = (unsigned)std::min<long>(1184, std::max<long>(1, (n + 255) / 256));
   k_timestep<<<nb, 256, 0, st>>>(s, umax, vmax, out);
+  return 1;
+}
+
+int launch_init_equilibrium(DevState& s, cudaStream_t st) {
+  if (s.prec == 0) k_init_eq<double><<<s.ncell, 128, 0, st>>>(s, (double*)s.h[0], (double*)s.b[0]);
+  else k_init_eq<float><<<s.ncell, 128, 0, st>>>(s, (float*)s.h[0], (float*)s.b[0]);
   return 1;
 }
 

@@ -90,6 +90,9 @@ int launch_convert_out(double* dst, int prec, const void* src, long ncell, int n
                        int vstride, cudaStream_t st);
 int launch_pack_w(double* dst4, const double* src, long ncell, int nw, cudaStream_t st);
 
+// Equilibrium h, b of every cell from its prim into buffer 0.
+int launch_init_equilibrium(DevState& s, cudaStream_t st);
+
 // CFL time step (timestep, src/Solver/solver_main.jl:240-342): tmax into out.
 int launch_timestep(const DevState& s, double umax, double vmax, double* out, cudaStream_t st);
 

@@ -59,6 +59,7 @@ SIGNATURES = {
     "kb_destroy": [_H],
     "kb_set_wall": [_H, ctypes.c_int, _D],
     "kb_upload_state": [_H, _D, _D, _D, _D],
+    "kb_init_equilibrium": [_H, _D, _D],
     "kb_download_state": [_H, _D, _D, _D, _D],
     "kb_timestep": [_H, ctypes.c_double, ctypes.c_double, ctypes.c_double, _D],
     "kb_reconstruct": [_H],

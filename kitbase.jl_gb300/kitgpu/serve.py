@@ -21,7 +21,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .setup import solver_set
-from .solver import Handle, initial_state, kb_config, wall_states
+from .solver import Handle, initial_cells, kb_config, wall_states
 
 
 def sod_request(nx, nu, Kn=1e-3):
@@ -131,8 +131,10 @@ class Server:
                 else:
                     h = Handle(kb_config(KS, self.precision), vs.flat(vs.u), vs.flat(vs.v),
                                vs.flat(vs.weights))
-                w, p, hd, bd = initial_state(KS)
-                h.upload(w, p, hd, bd)
+                # the Sod and cavity presets start in equilibrium: only w and
+                # prim cross the bus, h and b are built on the device
+                w, p = initial_cells(KS)
+                h.init_equilibrium(w, p)
                 for side, prim in enumerate(wall_states(KS)):
                     if KS.set.boundary[side] == "maxwell":
                         h.set_wall(side, prim)

@@ -93,6 +93,11 @@ class Handle:
         a = [np.ascontiguousarray(x, dtype=np.float64) for x in (w, prim, h, b)]
         self.call("kb_upload_state", *[N.ptr(x) for x in a])
 
+    def init_equilibrium(self, w, prim):
+        """w, prim per cell; h, b set to the equilibrium on the device."""
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (w, prim)]
+        self.call("kb_init_equilibrium", *[N.ptr(x) for x in a])
+
     def download(self, want=("w", "prim", "h", "b")):
         out = {}
         w = np.zeros((self.ncell, self.nw)) if "w" in want else None
@@ -236,6 +241,26 @@ class Faces:
         nfx = (self.handle.cfg.nx + 1) * (self.handle.cfg.ny if self.handle.dim == 2 else 1)
         sl = slice(0, nfx) if self.direction == 0 else slice(nfx, None)
         return fw[sl], fh[sl], fb[sl]
+
+
+def initial_cells(KS):
+    """Per-cell (w, prim) of init_fvm, all cells incl. ghosts, x fastest."""
+    ps, ib, gas = KS.ps, KS.ib, KS.gas
+    if KS.dim == 1:
+        pts = [(x,) for x in ps.x]
+    else:
+        nxt, nyt = ps.x.shape
+        pts = [(ps.x[i, j], ps.y[i, j]) for j in range(nyt) for i in range(nxt)]
+    ws, ps_ = [], []
+    cache = {}
+    for pt in pts:
+        w = np.asarray(ib.fw(*pt), dtype=np.float64)
+        key = w.tobytes()
+        if key not in cache:
+            cache[key] = conserve_prim(w, gas.gamma)
+        ws.append(w)
+        ps_.append(cache[key])
+    return np.array(ws), np.array(ps_)
 
 
 def initial_state(KS):

@@ -153,3 +153,21 @@ def test_fp32_update_shapes(gpu_lib, name, cfg, tx, bs):
     w, p, h, b = orc.get_state()
     e = rho_u_t_error(g["prim"], p)
     assert max(e) < 1e-5, e
+
+
+@pytest.mark.parametrize("name,cfg,prec", [
+    ("sod", sod(), "fp64"), ("cavity", cavity(nx=9, ny=7), "fp64"),
+    ("quadrant-ghosts", quadrant(nx=6, ny=5), "fp64"), ("cavity-fp32", cavity(nx=9, ny=7), "fp32"),
+], ids=lambda x: x if isinstance(x, str) else "")
+def test_init_equilibrium_matches_host_state(gpu_lib, name, cfg, prec):
+    """kb_init_equilibrium builds on the device the h, b that init_fvm builds
+    on the host (equal to 1e-14 in FP64, to FP32 rounding in FP32)."""
+    KS, ctr, *faces, t = kitgpu.initialize(cfg, precision=prec)
+    ref = ctr.handle.download()
+    w, p = kitgpu.solver.initial_cells(KS)
+    ctr.handle.init_equilibrium(w, p)
+    got = ctr.handle.download()
+    tol = 1e-14 if prec == "fp64" else 0.0
+    for k in ("w", "prim", "h", "b"):
+        scale = np.max(np.abs(ref[k]))
+        assert np.max(np.abs(got[k] - ref[k])) <= tol * scale + (6e-8 * np.abs(ref[k]).max() if prec == "fp32" else 0.0), k
