@@ -376,8 +376,25 @@ int kb_set_wall(kb_handle_t* h, int side, const double* host_prim) {
   return KB_OK;
 }
 
-// distributions host (double, [ncell][nvel]) <-> device (padded, precision)
+// Device address of page-locked host memory (the host pointer's mapping under
+// unified addressing), or null for pageable memory.
+static void* device_view(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// distributions host (double, [ncell][nvel]) <-> device (padded, precision).
+// Page-locked host arrays are converted in place by one kernel that reads
+// (or writes) them over the host link directly; pageable ones go through the
+// device staging buffer in chunks.
 static int dist_in(kb_handle* h, void* dst, const double* src) {
+  if (const void* dv = device_view(src))
+    return check_launch(h, kb::launch_convert_in(dst, h->s.prec, (const double*)dv, h->ncell,
+                                                 h->nvel, h->vstride, h->stream));
   long per = std::max<long>(1, h->stage_elems / h->nvel);
   size_t esz = h->s.prec == KB_PREC_FP64 ? 8 : 4;
   for (long c0 = 0; c0 < h->ncell; c0 += per) {
@@ -391,6 +408,11 @@ static int dist_in(kb_handle* h, void* dst, const double* src) {
 }
 
 static int dist_out(kb_handle* h, double* dst, const void* src) {
+  if (void* dv = device_view(dst)) {
+    KB_TRY(check_launch(h, kb::launch_convert_out((double*)dv, h->s.prec, src, h->ncell, h->nvel,
+                                                  h->vstride, h->stream)));
+    return sync(h);
+  }
   long per = std::max<long>(1, h->stage_elems / h->nvel);
   size_t esz = h->s.prec == KB_PREC_FP64 ? 8 : 4;
   for (long c0 = 0; c0 < h->ncell; c0 += per) {

@@ -731,33 +731,18 @@ __global__ void k_slopes_dump(DevState s, double* sh, double* sb) {
 
 // --------------------------------------------------------- conversions
 
-__global__ void k_conv_in_d(double* dst, const double* src, long ncell, int nvel, int vs) {
-  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncell * nvel) return;
-  long c = t / nvel;
-  int v = (int)(t % nvel);
-  dst[c * vs + v] = src[t];
-}
-__global__ void k_conv_in_f(float* dst, const double* src, long ncell, int nvel, int vs) {
-  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncell * nvel) return;
-  long c = t / nvel;
-  int v = (int)(t % nvel);
-  dst[c * vs + v] = (float)src[t];
-}
-__global__ void k_conv_out_d(double* dst, const double* src, long ncell, int nvel, int vs) {
-  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncell * nvel) return;
-  long c = t / nvel;
-  int v = (int)(t % nvel);
-  dst[t] = src[c * vs + v];
-}
-__global__ void k_conv_out_f(double* dst, const float* src, long ncell, int nvel, int vs) {
-  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncell * nvel) return;
-  long c = t / nvel;
-  int v = (int)(t % nvel);
-  dst[t] = (double)src[c * vs + v];
+// Row copy with conversion between the host layout ([cell][nvel], FP64) and
+// the device layout ([cell][vstride], storage precision); a block converts cpb
+// consecutive cells, threads striding over velocities (no index division).
+template <typename DT, typename ST>
+__global__ void k_conv(DT* __restrict__ dst, const ST* __restrict__ src, long ncell, int nvel,
+                       int dvs, int svs, int cpb) {
+  const long c0 = (long)blockIdx.x * cpb;
+  for (int r = 0; r < cpb; ++r) {
+    const long c = c0 + r;
+    if (c >= ncell) return;
+    for (int v = threadIdx.x; v < nvel; v += blockDim.x) dst[c * dvs + v] = (DT)src[c * svs + v];
+  }
 }
 __global__ void k_pack_w(double* dst4, const double* src, long ncell, int nw) {
   long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -938,19 +923,23 @@ int launch_slopes_dump(DevState& s, double* sh, double* sb, cudaStream_t st) {
 
 int launch_convert_in(void* dst, int prec, const double* src, long ncell, int nvel, int vstride,
                       cudaStream_t st) {
-  long n = ncell * nvel;
-  if (n == 0) return 0;
-  if (prec == 0) k_conv_in_d<<<nblk(n, 256), 256, 0, st>>>((double*)dst, src, ncell, nvel, vstride);
-  else k_conv_in_f<<<nblk(n, 256), 256, 0, st>>>((float*)dst, src, ncell, nvel, vstride);
+  if (ncell * nvel == 0) return 0;
+  const int cpb = std::max(1, 2048 / nvel);
+  const unsigned nb = (unsigned)((ncell + cpb - 1) / cpb);
+  if (prec == 0) k_conv<double, double><<<nb, 256, 0, st>>>((double*)dst, src, ncell, nvel, vstride, nvel, cpb);
+  else k_conv<float, double><<<nb, 256, 0, st>>>((float*)dst, src, ncell, nvel, vstride, nvel, cpb);
   return 1;
 }
 
 int launch_convert_out(double* dst, int prec, const void* src, long ncell, int nvel, int vstride,
                        cudaStream_t st) {
-  long n = ncell * nvel;
-  if (n == 0) return 0;
-  if (prec == 0) k_conv_out_d<<<nblk(n, 256), 256, 0, st>>>(dst, (const double*)src, ncell, nvel, vstride);
-  else k_conv_out_f<<<nblk(n, 256), 256, 0, st>>>(dst, (const float*)src, ncell, nvel, vstride);
+  if (ncell * nvel == 0) return 0;
+  const int cpb = std::max(1, 2048 / nvel);
+  const unsigned nb = (unsigned)((ncell + cpb - 1) / cpb);
+  if (prec == 0)
+    k_conv<double, double><<<nb, 256, 0, st>>>(dst, (const double*)src, ncell, nvel, nvel, vstride, cpb);
+  else
+    k_conv<double, float><<<nb, 256, 0, st>>>(dst, (const float*)src, ncell, nvel, nvel, vstride, cpb);
   return 1;
 }
 
