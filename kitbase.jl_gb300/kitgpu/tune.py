@@ -21,7 +21,7 @@ CACHE = os.environ.get("KITGPU_TUNE_CACHE",
 
 MARCH_TX = (2, 4)
 MARCH_BS = (64, 128)
-MARCH_RY = (16, 32)
+MARCH_RY = (16, 32, 64)
 MOM_TS = (2, 4)
 
 
