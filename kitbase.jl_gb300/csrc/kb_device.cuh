@@ -187,9 +187,25 @@ __device__ inline void conserve_prim(const double* W, int nw, double g, double* 
   }
 }
 
+// Transcendental functions of the face and cell parameters.  FAST (the FP32
+// split form, whose fluxes are FP32 anyway) evaluates them in FP32 and widens
+// the result; otherwise the FP64 library functions.  Arithmetic, divisions
+// and the moment recursions stay FP64 either way.
+template <bool FAST>
+__device__ __forceinline__ double t_exp(double x) { return FAST ? (double)expf((float)x) : exp(x); }
+template <bool FAST>
+__device__ __forceinline__ double t_erfc(double x) { return FAST ? (double)erfcf((float)x) : erfc(x); }
+template <bool FAST>
+__device__ __forceinline__ double t_sqrt(double x) { return FAST ? (double)sqrtf((float)x) : sqrt(x); }
+template <bool FAST>
+__device__ __forceinline__ double t_pow(double x, double y) {
+  return FAST ? (double)powf((float)x, (float)y) : pow(x, y);
+}
+
 // vhs_collision_time, src/Theory/theory_relaxation.jl:28
+template <bool FAST = false>
 __device__ inline double vhs_time(double rho, double lam, double mu, double om) {
-  return mu * 2.0 * pow(lam, 1.0 - om) / rho;
+  return mu * 2.0 * t_pow<FAST>(lam, 1.0 - om) / rho;
 }
 
 // Moments of the Gaussian: orders 0..6 of the full / left / right half
@@ -201,17 +217,19 @@ struct GM {
 
 // half: 1 the left half range only (MuL, Mv, Mxi), 2 the right half only,
 // 3 everything.  1 / (2 lambda) is formed once and multiplied in.
+template <bool FAST = false>
 __device__ inline void gauss_moments(const double* p, int nw, double inK, GM& m, int half = 3) {
   double l = p[nw - 1], U = p[1];
   const double hl = 0.5 / l;
-  double e = 0.5 * exp(-l * (U * U)) / sqrt(PI * l);
+  const double sl = t_sqrt<FAST>(l);
+  double e = 0.5 * t_exp<FAST>(-l * (U * U)) / t_sqrt<FAST>(PI * l);
   if (half & 1) {
-    m.MuL[0] = 0.5 * erfc(-sqrt(l) * U);
+    m.MuL[0] = 0.5 * t_erfc<FAST>(-sl * U);
     m.MuL[1] = U * m.MuL[0] + e;
     for (int i = 2; i <= 6; ++i) m.MuL[i] = U * m.MuL[i - 1] + (i - 1) * hl * m.MuL[i - 2];
   }
   if (half & 2) {
-    m.MuR[0] = 0.5 * erfc(sqrt(l) * U);
+    m.MuR[0] = 0.5 * t_erfc<FAST>(sl * U);
     m.MuR[1] = U * m.MuR[0] - e;
     for (int i = 2; i <= 6; ++i) m.MuR[i] = U * m.MuR[i - 1] + (i - 1) * hl * m.MuR[i - 2];
   }

@@ -126,7 +126,8 @@ __device__ __forceinline__ FaceCoef32 face_coef32(const Geo& g, const FaceParam&
 // Interface equilibrium from the two half Maxwellians (flux_kcu.jl:480-495,
 // flux_ugks.jl:47-56), then the KCU / UGKS time integrals, UGKS slopes and
 // the analytic part of fw.  One thread per face.
-template <int D, int FLUX>
+// FAST: the FP32 split form (transcendentals in FP32, see t_exp).
+template <int D, int FLUX, bool FAST>
 __global__ void k_face_param(DevState s, double dt) {
   const Geo& g = s.g;
   int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -168,9 +169,9 @@ __global__ void k_face_param(DevState s, double dt) {
     conserve_prim(wL, NW, g.gamma, pL);
     conserve_prim(wR, NW, g.gamma, pR);
     GM m;
-    gauss_moments(pL, NW, g.K, m, 1);
+    gauss_moments<FAST>(pL, NW, g.K, m, 1);
     moments_conserve(m.MuL, m.Mv, m.Mxi, NW, 0, 0, 0, M1);
-    gauss_moments(pR, NW, g.K, m, 2);
+    gauss_moments<FAST>(pR, NW, g.K, m, 2);
     moments_conserve(m.MuR, m.Mv, m.Mxi, NW, 0, 0, 0, M2);
     for (int k = 0; k < 4; ++k) wi[k] = k < NW ? pL[0] * M1[k] + pR[0] * M2[k] : 0.0;
     conserve_prim(wi, NW, g.gamma, p);
@@ -179,14 +180,14 @@ __global__ void k_face_param(DevState s, double dt) {
     P.prim[1] = p[1];
     P.prim[2] = NW == 4 ? p[2] : 0.0;
     P.prim[3] = lam;
-    double tau = vhs_time(p[0], lam, g.mu_ref, g.omega);
+    double tau = vhs_time<FAST>(p[0], lam, g.mu_ref, g.omega);
     GM mi;
     if (FLUX == FLUX_KCU) {
       tau += fabs(pL[0] / pL[NW - 1] - pR[0] / pR[NW - 1]) /
              (pL[0] / pL[NW - 1] + pR[0] / pR[NW - 1]) * dt * 2.0;
-      P.Mt[1] = tau * (1.0 - exp(-dt / tau));
+      P.Mt[1] = tau * (1.0 - t_exp<FAST>(-dt / tau));
       P.Mt[0] = dt - P.Mt[1];
-      gauss_moments(p, NW, g.K, mi);
+      gauss_moments<FAST>(p, NW, g.K, mi);
       double Muv[4];
       moments_conserve(mi.Mu, mi.Mv, mi.Mxi, NW, 1, 0, 0, Muv);
       for (int k = 0; k < NW; ++k) P.fwa[k] = P.Mt[0] * p[0] * Muv[k] * len;
@@ -201,13 +202,13 @@ __global__ void k_face_param(DevState s, double dt) {
       double aL[4], aR[4], aT[4];
       pdf_slope(p, dL, NW, g.K, aL);
       pdf_slope(p, dR, NW, g.K, aR);
-      gauss_moments(p, NW, g.K, mi);
+      gauss_moments<FAST>(p, NW, g.K, mi);
       double MauL[4], MauR[4], MauT[4], Muv[4], tmp[4];
       moments_conserve_slope(aL, mi.MuL, mi.Mv, mi.Mxi, NW, 1, MauL);
       moments_conserve_slope(aR, mi.MuR, mi.Mv, mi.Mxi, NW, 1, MauR);
       for (int k = 0; k < 4; ++k) tmp[k] = -p[0] * (MauL[k] + MauR[k]);
       pdf_slope(p, tmp, NW, g.K, aT);
-      double ex = exp(-dt / tau);
+      double ex = t_exp<FAST>(-dt / tau);
       double Mt[5];
       Mt[3] = tau * (1.0 - ex);
       Mt[4] = -tau * dt * ex + tau * Mt[3];
@@ -818,21 +819,25 @@ int launch_reconstruct(DevState& s, cudaStream_t st) {
 
 int launch_face_param(DevState& s, double dt, cudaStream_t st) {
   int nf = s.nface_x + s.nface_y;
-  const bool two = s.g.D == 2;
+  const bool two = s.g.D == 2, fast = s.prec != 0;
+#define KB_FP(D, F)                                                              \
+  (fast ? k_face_param<D, F, true><<<nblk(nf, 128), 128, 0, st>>>(s, dt)        \
+        : k_face_param<D, F, false><<<nblk(nf, 128), 128, 0, st>>>(s, dt))
   switch (s.flux) {
     case FLUX_KFVS:
-      if (two) k_face_param<2, FLUX_KFVS><<<nblk(nf, 128), 128, 0, st>>>(s, dt);
-      else k_face_param<1, FLUX_KFVS><<<nblk(nf, 128), 128, 0, st>>>(s, dt);
+      if (two) KB_FP(2, FLUX_KFVS);
+      else KB_FP(1, FLUX_KFVS);
       break;
     case FLUX_KCU:
-      if (two) k_face_param<2, FLUX_KCU><<<nblk(nf, 128), 128, 0, st>>>(s, dt);
-      else k_face_param<1, FLUX_KCU><<<nblk(nf, 128), 128, 0, st>>>(s, dt);
+      if (two) KB_FP(2, FLUX_KCU);
+      else KB_FP(1, FLUX_KCU);
       break;
     default:
-      if (two) k_face_param<2, FLUX_UGKS><<<nblk(nf, 128), 128, 0, st>>>(s, dt);
-      else k_face_param<1, FLUX_UGKS><<<nblk(nf, 128), 128, 0, st>>>(s, dt);
+      if (two) KB_FP(2, FLUX_UGKS);
+      else KB_FP(1, FLUX_UGKS);
       break;
   }
+#undef KB_FP
   return 1;
 }
 
