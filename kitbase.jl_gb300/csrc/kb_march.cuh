@@ -312,8 +312,10 @@ struct MomStage {
 };
 constexpr int MOM_THREADS = 160;  // 4 consumer warps + 1 producer warp
 
+// Two faces per warp without the Shakhov heat flux fit in 80 registers, so
+// five CTAs (25 warps) share an SM; the other forms keep what they need.
 template <int D, int FLUX, int TS, bool SHAK, int DIR>
-__global__ void __launch_bounds__(MOM_THREADS) k_mom_st(const __grid_constant__ CUtensorMap tmh,
+__global__ void __maxnreg__(TS == 2 && !SHAK ? 80 : 255) k_mom_st(const __grid_constant__ CUtensorMap tmh,
                                                         const __grid_constant__ CUtensorMap tmb,
                                                         DevState s) {
   using R = float;
@@ -1944,8 +1946,11 @@ static void mom_st_go(DevState& s, cudaStream_t st) {
   static bool raised[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (SL::BYTES > 48 * 1024 && dev >= 0 && dev < 64 && !raised[dev]) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SL::BYTES);
+  if (dev >= 0 && dev < 64 && !raised[dev]) {
+    if (SL::BYTES > 48 * 1024)
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SL::BYTES);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
     raised[dev] = true;
   }
   kern<<<(unsigned)nblk, MOM_THREADS, SL::BYTES, st>>>(tm[0], tm[1], s);
