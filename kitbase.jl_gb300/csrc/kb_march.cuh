@@ -312,10 +312,8 @@ struct MomStage {
 };
 constexpr int MOM_THREADS = 160;  // 4 consumer warps + 1 producer warp
 
-// Two faces per warp without the Shakhov heat flux fit in 80 registers, so
-// five CTAs (25 warps) share an SM; the other forms keep what they need.
 template <int D, int FLUX, int TS, bool SHAK, int DIR>
-__global__ void __maxnreg__(TS == 2 && !SHAK ? 80 : 255) k_mom_st(const __grid_constant__ CUtensorMap tmh,
+__global__ void __launch_bounds__(MOM_THREADS) k_mom_st(const __grid_constant__ CUtensorMap tmh,
                                                         const __grid_constant__ CUtensorMap tmb,
                                                         DevState s) {
   using R = float;
@@ -528,10 +526,11 @@ __global__ void __maxnreg__(TS == 2 && !SHAK ? 80 : 255) k_mom_st(const __grid_c
         one(S, Sw, vl, fast_tag, I0{});
       }
     }
-    // flush the FP32 partials (8 velocities per lane) into the compensated sums
+    // flush the FP32 partials (8 velocities per lane) into the compensated
+    // sums; the interior form never touches the segment's last face
     if (k & 1) {
 #pragma unroll
-      for (int f = 0; f < TS + 1; ++f)
+      for (int f = 0; f < (FAST ? TS : TS + 1); ++f)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[f][q].flush();
 #pragma unroll
