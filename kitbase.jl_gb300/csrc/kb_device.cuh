@@ -172,8 +172,24 @@ __device__ __forceinline__ double slope_of<double>(int rule, double qm, double q
 
 // ---------------------------------------------------- scalar FP64 physics
 
-// conserve_prim!, src/Theory/theory_macro.jl:185-206
+// conserve_prim!, src/Theory/theory_macro.jl:185-206.  FAST (the FP32 split
+// form) multiplies by 1 / rho instead of dividing: GB300 runs FP64 at 1/64 of
+// the FP32 rate and each FP64 division costs several FP64 operations.
+template <bool FAST = false>
 __device__ inline void conserve_prim(const double* W, int nw, double g, double* p) {
+  if (FAST) {
+    const double r = 1.0 / W[0];
+    p[0] = W[0];
+    p[1] = W[1] * r;
+    if (nw == 3) {
+      p[2] = 0.5 * W[0] / ((g - 1.0) * (W[2] - 0.5 * (W[1] * W[1]) * r));
+      p[3] = 0.0;
+    } else {
+      p[2] = W[2] * r;
+      p[3] = 0.5 * W[0] / ((g - 1.0) * (W[3] - 0.5 * (W[1] * W[1] + W[2] * W[2]) * r));
+    }
+    return;
+  }
   if (nw == 3) {
     p[0] = W[0];
     p[1] = W[1] / W[0];
@@ -288,9 +304,32 @@ __device__ inline void moments_conserve_slope(const double* a, const double* Mu,
   }
 }
 
-// pdf_slope(prim, sw, inK) (src/Theory/theory_pdf.jl:11-49)
+// pdf_slope(prim, sw, inK) (src/Theory/theory_pdf.jl:11-49); FAST forms the
+// three reciprocals once (see conserve_prim)
+template <bool FAST = false>
 __device__ inline void pdf_slope(const double* p, const double* s, int nw, double inK,
                                  double* sl) {
+  if (FAST) {
+    const int e = nw - 1;  // energy slot
+    const double r0 = 1.0 / p[0], rl = 1.0 / p[e], rk = 1.0 / (inK + double(nw - 2));
+    const double U = p[1], V = nw == 4 ? p[2] : 0.0, sv = nw == 4 ? s[2] : 0.0;
+    const double q2 = U * U + V * V, c = 0.5 * (inK + double(nw - 2)) * rl;
+    const double se = 4.0 * (p[e] * p[e]) * rk * r0 *
+                      (2.0 * s[e] - 2.0 * U * s[1] - 2.0 * V * sv + s[0] * (q2 - c));
+    const double tl = 2.0 * p[e] * r0;
+    const double s1 = tl * (s[1] - U * s[0]) - U * se;
+    const double s2 = tl * (sv - V * s[0]) - V * se;
+    sl[0] = s[0] * r0 - U * s1 - V * s2 - 0.5 * (q2 + c) * se;
+    sl[1] = s1;
+    if (nw == 4) {
+      sl[2] = s2;
+      sl[3] = se;
+    } else {
+      sl[2] = se;
+      sl[3] = 0.0;
+    }
+    return;
+  }
   if (nw == 3) {
     sl[2] = 4.0 * (p[2] * p[2]) / (inK + 1.0) / p[0] *
             (2.0 * s[2] - 2.0 * p[1] * s[1] + s[0] * ((p[1] * p[1]) - 0.5 * (inK + 1.0) / p[2]));

@@ -166,15 +166,15 @@ __global__ void k_face_param(DevState s, double dt) {
       for (int k = 0; k < 4; ++k) { wL[k] = wl[k]; wR[k] = wr[k]; }
     }
     double pL[4], pR[4], wi[4], p[4], M1[4], M2[4];
-    conserve_prim(wL, NW, g.gamma, pL);
-    conserve_prim(wR, NW, g.gamma, pR);
+    conserve_prim<FAST>(wL, NW, g.gamma, pL);
+    conserve_prim<FAST>(wR, NW, g.gamma, pR);
     GM m;
     gauss_moments<FAST>(pL, NW, g.K, m, 1);
     moments_conserve(m.MuL, m.Mv, m.Mxi, NW, 0, 0, 0, M1);
     gauss_moments<FAST>(pR, NW, g.K, m, 2);
     moments_conserve(m.MuR, m.Mv, m.Mxi, NW, 0, 0, 0, M2);
     for (int k = 0; k < 4; ++k) wi[k] = k < NW ? pL[0] * M1[k] + pR[0] * M2[k] : 0.0;
-    conserve_prim(wi, NW, g.gamma, p);
+    conserve_prim<FAST>(wi, NW, g.gamma, p);
     double lam = p[NW - 1];
     P.prim[0] = p[0];
     P.prim[1] = p[1];
@@ -195,19 +195,20 @@ __global__ void k_face_param(DevState s, double dt) {
       P.tr[0] = P.Mt[1] * len;
     } else {
       double dL[4], dR[4];
+      const double rdx = FAST ? 1.0 / dxh : 0.0;
       for (int k = 0; k < 4; ++k) {
-        dL[k] = k < NW ? (wi[k] - wL[k]) / dxh : 0.0;
-        dR[k] = k < NW ? (wR[k] - wi[k]) / dxh : 0.0;
+        dL[k] = k < NW ? (FAST ? (wi[k] - wL[k]) * rdx : (wi[k] - wL[k]) / dxh) : 0.0;
+        dR[k] = k < NW ? (FAST ? (wR[k] - wi[k]) * rdx : (wR[k] - wi[k]) / dxh) : 0.0;
       }
       double aL[4], aR[4], aT[4];
-      pdf_slope(p, dL, NW, g.K, aL);
-      pdf_slope(p, dR, NW, g.K, aR);
+      pdf_slope<FAST>(p, dL, NW, g.K, aL);
+      pdf_slope<FAST>(p, dR, NW, g.K, aR);
       gauss_moments<FAST>(p, NW, g.K, mi);
       double MauL[4], MauR[4], MauT[4], Muv[4], tmp[4];
       moments_conserve_slope(aL, mi.MuL, mi.Mv, mi.Mxi, NW, 1, MauL);
       moments_conserve_slope(aR, mi.MuR, mi.Mv, mi.Mxi, NW, 1, MauR);
       for (int k = 0; k < 4; ++k) tmp[k] = -p[0] * (MauL[k] + MauR[k]);
-      pdf_slope(p, tmp, NW, g.K, aT);
+      pdf_slope<FAST>(p, tmp, NW, g.K, aT);
       double ex = t_exp<FAST>(-dt / tau);
       double Mt[5];
       Mt[3] = tau * (1.0 - ex);
