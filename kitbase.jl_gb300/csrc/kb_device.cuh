@@ -238,7 +238,9 @@ __device__ inline void gauss_moments(const double* p, int nw, double inK, GM& m,
   double l = p[nw - 1], U = p[1];
   const double hl = 0.5 / l;
   const double sl = t_sqrt<FAST>(l);
-  double e = 0.5 * t_exp<FAST>(-l * (U * U)) / t_sqrt<FAST>(PI * l);
+  // e = exp(-l U^2) / (2 sqrt(pi l)); FAST evaluates it in FP32 like its exp
+  const double e = FAST ? double(0.5f * expf(float(-l * (U * U))) * rsqrtf(float(PI * l)))
+                        : 0.5 * exp(-l * (U * U)) / sqrt(PI * l);
   if (half & 1) {
     m.MuL[0] = 0.5 * t_erfc<FAST>(-sl * U);
     m.MuL[1] = U * m.MuL[0] + e;

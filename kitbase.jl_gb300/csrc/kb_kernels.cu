@@ -91,35 +91,30 @@ __device__ __forceinline__ FaceCoef32 face_coef32(const Geo& g, const FaceParam&
     c.T.w = float(Mt[0] * cB * len);
     return c;
   }
-  const int e = g.D + 1;  // index of the energy slope
+  // the energy slope sits at index D + 1; selected between constant indices
+  // (a run-time index would place the slope arrays in local memory)
   const double* t = P.aT;
-  double tt = g.D == 2 ? t[2] : 0.0, Mxi2 = P.Mxi2;
-  c.T.z = float((Mt[0] + Mt[2] * (t[0] + 0.5 * t[e] * cB)) * len);
-  c.T.w = float((Mt[0] * cB + Mt[2] * (cB * t[0] + 0.5 * t[e] * Mxi2)) * len);
+  const double tt = g.D == 2 ? t[2] : 0.0, te = g.D == 2 ? t[3] : t[2], Mxi2 = P.Mxi2;
+  c.T.z = float((Mt[0] + Mt[2] * (t[0] + 0.5 * te * cB)) * len);
+  c.T.w = float((Mt[0] * cB + Mt[2] * (cB * t[0] + 0.5 * te * Mxi2)) * len);
   c.G.x = float(Mt[2] * tt * len);
-  c.G.y = float(0.5 * Mt[2] * t[e] * len);
+  c.G.y = float(0.5 * Mt[2] * te * len);
   c.G.z = float(Mt[2] * cB * tt * len);
-  c.G.w = float(0.5 * Mt[2] * cB * t[e] * len);
-  for (int sgn = 0; sgn < 2; ++sgn) {
-    const double* a = sgn == 0 ? P.aL : P.aR;
-    double at = g.D == 2 ? a[2] : 0.0;
-    float4 C, Dd;
-    C.x = float((Mt[1] * (a[0] + 0.5 * a[e] * cB) + Mt[2] * t[1]) * len);
+  c.G.w = float(0.5 * Mt[2] * cB * te * len);
+  // one upwind side's slope terms (a = aL for un >= 0, aR otherwise)
+  auto side = [&](const double (&a)[4], float4& C, float4& Dd) {
+    const double at = g.D == 2 ? a[2] : 0.0, ae = g.D == 2 ? a[3] : a[2];
+    C.x = float((Mt[1] * (a[0] + 0.5 * ae * cB) + Mt[2] * t[1]) * len);
     C.y = float(Mt[1] * a[1] * len);
     C.z = float(Mt[1] * at * len);
-    C.w = float(0.5 * Mt[1] * a[e] * len);
-    Dd.x = float((Mt[1] * (cB * a[0] + 0.5 * a[e] * Mxi2) + Mt[2] * cB * t[1]) * len);
+    C.w = float(0.5 * Mt[1] * ae * len);
+    Dd.x = float((Mt[1] * (cB * a[0] + 0.5 * ae * Mxi2) + Mt[2] * cB * t[1]) * len);
     Dd.y = float(Mt[1] * cB * a[1] * len);
     Dd.z = float(Mt[1] * cB * at * len);
-    Dd.w = float(0.5 * Mt[1] * cB * a[e] * len);
-    if (sgn == 0) {
-      c.Cp = C;
-      c.Dp = Dd;
-    } else {
-      c.Cm = C;
-      c.Dm = Dd;
-    }
-  }
+    Dd.w = float(0.5 * Mt[1] * cB * ae * len);
+  };
+  side(P.aL, c.Cp, c.Dp);
+  side(P.aR, c.Cm, c.Dm);
   return c;
 }
 
@@ -399,7 +394,7 @@ __global__ void __launch_bounds__(256) k_cell_param(DevState s, double dt) {
     P.coll = coll;
     double* w = s.w + (long)c * 4;
     double* p = s.prim + (long)c * 4;
-    int NW = g.NW;
+    constexpr int NW = D + 2;  // compile-time, so the small arrays stay in registers
     double lo = p[NW - 1];
     P.o_rho_n = D == 1 ? p[0] * sqrt(lo / PI) : p[0] * (lo / PI);
     P.oU = p[1];
