@@ -366,7 +366,7 @@ constexpr int SEG_ROWS = SEG + 4;
 constexpr int SEG_MAXNU = 256;
 __host__ __device__ inline int seg_stride(int nus) { return (nus + 31) / 32 * 32 + 4; }
 constexpr int SEG_SMEM = 2 * SEG_ROWS * (SEG_MAXNU + 4) * 4 + 2 * SEG_MAXNU * 4 +
-                         (SEG + 1) * 3 * 8 + SEG * 8 + SEG * 12 * 4 + 8 * 8;
+                         (SEG + 1) * 3 * 8 + SEG * 8 + 16 + SEG * 3 * 16 + 8 * 8;
 
 __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __restrict__ Hin,
                                                      const float* __restrict__ Bin,
@@ -403,7 +403,8 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
   float* sW = sU + SEG_MAXNU;
   double* sfw = (double*)(sW + SEG_MAXNU);  // [SEG + 1][3]
   double* sq = sfw + (SEG + 1) * 3;          // [SEG]
-  float* scc = (float*)(sq + SEG);           // [SEG][12]
+  // [SEG][3] float4 cell coefficients, 16-byte aligned
+  float4* scc = (float4*)(((unsigned long long)(sq + SEG) + 15) & ~15ull);
   // window rows r0 .. r1-1 (cells incl. ghosts), smem row = cell - r0
   const int r0 = max(i0 - 2, -ng), r1 = min(i1 + 2, nx + ng), nrow = r1 - r0;
   if (tid == 0) {
@@ -533,7 +534,8 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
   }
   __syncthreads();
   // ---- cell parameters of the stepped cells (one thread per cell, FP64)
-  double rr[6] = {0, 0, 0, 0, 0, 0};
+  // residual terms of the cell: a convergence monitor, summed in FP32 below
+  float rr[6] = {0, 0, 0, 0, 0, 0};
   if (tid < cb - ca) {
     const double dx = B.dx[b], dt = B.dt[b];
     const int i = ca + tid;
@@ -547,14 +549,14 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
     const double idx = 1.0 / dx;
     for (int m = 0; m < 3; ++m) w[m] += (fL[m] - fR[m]) * idx;
     double pn[4];
-    conserve_prim(w, 3, B.gamma, pn);
+    conserve_prim<true>(w, 3, B.gamma, pn);
     p[0] = pn[0];
     p[1] = pn[1];
     p[2] = pn[2];
     for (int m = 0; m < 3; ++m) {
       double d = w[m] - wo[m];
-      rr[m] += d * d;
-      rr[3 + m] += fabs(w[m]);
+      rr[m] = float(d * d);
+      rr[3 + m] = float(fabs(w[m]));
     }
     double lam = pn[2];
     if (!(pn[0] > 0.0) || !(lam > 0.0) || !isfinite(pn[0]) || !isfinite(lam)) atomicOr(B.status, 1);
@@ -565,87 +567,102 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
     const float tau = float(B.mu[b]) * 2.f * powf(lf, float(1.0 - B.omega)) / rf;
     const float dtt = float(dt) / tau;
     const float Kf = float(B.K);
-    float* kc = scc + tid * 12;
-    kc[0] = rf * sqrtf(lf * float(1.0 / PI));  // new Maxwellian
-    kc[1] = float(pn[1]);
-    kc[2] = lf;
-    kc[3] = Kf / (2.f * lf);
-    kc[4] = dtt;
-    kc[5] = 1.f / (1.f + dtt);
-    kc[6] = rof * sqrtf(lof * float(1.0 / PI));  // old Maxwellian (Shakhov)
-    kc[7] = float(Uo);
-    kc[8] = lof;
-    kc[9] = Kf / (2.f * lof);
-    kc[10] = B.coll == COLL_SHAKHOV ? float(0.8 * (1.0 - B.Pr)) * (lof * lof) / rof * float(sq[tid]) : 0.f;
+    float4* kc = scc + tid * 3;
+    // new Maxwellian: density factor, U, lambda, K / (2 lambda)
+    kc[0] = make_float4(rf * sqrtf(lf * float(1.0 / PI)), float(pn[1]), lf, Kf / (2.f * lf));
+    // dt / tau, 1 / (1 + dt / tau), old Maxwellian (Shakhov) density factor and U
+    kc[1] = make_float4(dtt, 1.f / (1.f + dtt), rof * sqrtf(lof * float(1.0 / PI)), float(Uo));
+    // old lambda, K / (2 lambda), Shakhov heat-flux factor
+    kc[2] = make_float4(lof, Kf / (2.f * lof),
+                        B.coll == COLL_SHAKHOV
+                            ? float(0.8 * (1.0 - B.Pr)) * (lof * lof) / rof * float(sq[tid])
+                            : 0.f,
+                        0.f);
   }
   // residual partial sums of the segment: the cells are all in the first
-  // warp (SEG <= 32), reduced in a fixed shuffle order
+  // warp (SEG <= 32), reduced in a fixed shuffle order (FP32: GB300's FP64
+  // pipe would make this tree the longest chain of the cell phase)
   static_assert(SEG <= 32, "the cell update of a segment runs in the first warp");
   if (wid == 0) {
+#pragma unroll
     for (int m = 0; m < 6; ++m) {
 #pragma unroll
       for (int o = 16; o >= 1; o >>= 1) rr[m] += __shfl_xor_sync(0xffffffffu, rr[m], o);
     }
   }
   __syncthreads();  // cell coefficients ready for the pointwise update
-  // ---- pointwise KFVS flux + relaxation, one thread per velocity
+  // ---- pointwise KFVS flux + relaxation, one thread per velocity.  Every
+  // upwind cell of a segment away from ghost-less ends takes the van Leer
+  // slope, so that form skips the per-face slope rule.
   const float idx = sconst[2];
-  for (int v = tid; v < nu; v += SEG_T) {
-    const float u = sU[v];
-    const bool pos = u >= 0.f;
-    const float side = pos ? 0.5f : -0.5f;
-    if (i0 == 0) {  // fixed end cells keep their state
-      Ho[(long)ng * ns + v] = rowH(0)[v];
-      Bo[(long)ng * ns + v] = rowB(0)[v];
-    }
-    if (i1 == nx) {
-      Ho[(long)(nx - 1 + ng) * ns + v] = rowH(nx - 1)[v];
-      Bo[(long)(nx - 1 + ng) * ns + v] = rowB(nx - 1)[v];
-    }
-    auto face = [&](int f, float& fh, float& fbv) {
-      const int up = pos ? f - 1 : f;
-      const int r = brule(up, nx, ng);
-      const float* hc = rowH(up);
-      const float* bc = rowB(up);
-      const float h0 = hc[v], b0 = bc[v];
-      float sh = 0.f, sb = 0.f;
-      if (r == 1) {
-        sh = bvl<float>(1, hc[v - sst], h0, hc[v + sst], epsd);
-        sb = bvl<float>(1, bc[v - sst], b0, bc[v + sst], epsd);
+  const bool all_vl = ng > 0 || (ca >= 2 && cb <= nx - 2);
+  auto pointwise = [&](auto vl_tag) {
+    constexpr bool VL = decltype(vl_tag)::value;
+    for (int v = tid; v < nu; v += SEG_T) {
+      const float u = sU[v];
+      const bool pos = u >= 0.f;
+      const float side = pos ? 0.5f : -0.5f;
+      const float Tu = T3 * u, Tuu = T4 * (u * u);
+      if (i0 == 0) {  // fixed end cells keep their state
+        Ho[(long)ng * ns + v] = rowH(0)[v];
+        Bo[(long)ng * ns + v] = rowB(0)[v];
       }
-      const float hf = h0 + side * sh, bf = b0 + side * sb;
-      fh = T3 * u * hf - T4 * (u * u) * sh;
-      fbv = T3 * u * bf - T4 * (u * u) * sb;
-    };
-    float fhL = 0.f, fbL = 0.f;
-    if (ca < cb) face(ca, fhL, fbL);
-    for (int i = ca; i < cb; ++i) {
-      float fhR, fbR;
-      face(i + 1, fhR, fbR);
-      const float* kc = scc + (i - ca) * 12;
-      const float h0 = rowH(i)[v], b0 = rowB(i)[v];
-      const float du = u - kc[1];
-      const float M = kc[0] * fexp(-kc[2] * du * du);
-      float MH = M, MB = M * kc[3];
-      if (B.coll == COLL_SHAKHOV) {
-        const float ou = u - kc[7];
-        const float OH = kc[6] * fexp(-kc[8] * ou * ou);
-        const float cq = kc[10] * ou;
-        const float tl = 2.f * kc[8] * ou * ou + float(B.K);
-        MH += cq * (tl - 5.f) * OH;
-        MB += cq * (tl - 3.f) * OH * kc[9];
+      if (i1 == nx) {
+        Ho[(long)(nx - 1 + ng) * ns + v] = rowH(nx - 1)[v];
+        Bo[(long)(nx - 1 + ng) * ns + v] = rowB(nx - 1)[v];
       }
-      const float dtau = kc[4], inv = kc[5];
-      Ho[(long)(i + ng) * ns + v] = (h0 + (fhL - fhR) * idx + dtau * MH) * inv;
-      Bo[(long)(i + ng) * ns + v] = (b0 + (fbL - fbR) * idx + dtau * MB) * inv;
-      fhL = fhR;
-      fbL = fbR;
+      // flux through face f, whose upwind cell row starts at hc / bc
+      auto face = [&](int f, const float* hc, const float* bc, float& fh, float& fbv) {
+        const float h0 = hc[0], b0 = bc[0];
+        float sh = 0.f, sb = 0.f;
+        if (VL || brule(pos ? f - 1 : f, nx, ng) == 1) {
+          sh = bvl<float>(1, hc[-sst], h0, hc[sst], epsd);
+          sb = bvl<float>(1, bc[-sst], b0, bc[sst], epsd);
+        }
+        fh = Tu * (h0 + side * sh) - Tuu * sh;
+        fbv = Tu * (b0 + side * sb) - Tuu * sb;
+      };
+      if (ca >= cb) continue;
+      // hr / br: row of cell i at this velocity; the upwind cell of face i + 1
+      // is i (pos) or i + 1
+      const int up = pos ? 0 : sst;
+      const float* hr = rowH(ca) + v;
+      const float* br = rowB(ca) + v;
+      float fhL, fbL;
+      face(ca, hr - sst + up, br - sst + up, fhL, fbL);
+      float* ph = Ho + (long)(ca + ng) * ns + v;
+      float* pb = Bo + (long)(ca + ng) * ns + v;
+      const float4* kc = scc;
+      for (int i = ca; i < cb; ++i, hr += sst, br += sst, ph += ns, pb += ns, kc += 3) {
+        float fhR, fbR;
+        face(i + 1, hr + up, br + up, fhR, fbR);
+        const float4 k0 = kc[0], k1 = kc[1];
+        const float h0 = hr[0], b0 = br[0];
+        const float du = u - k0.y;
+        const float M = k0.x * fexp(-k0.z * du * du);
+        float MH = M, MB = M * k0.w;
+        if (B.coll == COLL_SHAKHOV) {
+          const float4 k2 = kc[2];
+          const float ou = u - k1.w;
+          const float OH = k1.z * fexp(-k2.x * ou * ou);
+          const float cq = k2.z * ou;
+          const float tl = 2.f * k2.x * ou * ou + float(B.K);
+          MH += cq * (tl - 5.f) * OH;
+          MB += cq * (tl - 3.f) * OH * k2.y;
+        }
+        *ph = (h0 + (fhL - fhR) * idx + k1.x * MH) * k1.y;
+        *pb = (b0 + (fbL - fbR) * idx + k1.x * MB) * k1.y;
+        fhL = fhR;
+        fbL = fbR;
+      }
     }
-  }
+  };
+  if (all_vl) pointwise(std::true_type{});
+  else pointwise(std::false_type{});
   // ---- the instance's last segment sums the partials in segment order
   if (tid == 0) {
     double* pr = B.respart + (long)k * 8;
-    for (int m = 0; m < 6; ++m) pr[m] = rr[m];
+    for (int m = 0; m < 6; ++m) pr[m] = (double)rr[m];
     __threadfence();
     const int prev = atomicAdd(&B.done[b], 1);
     if (prev == B.nseg[b] - 1) {
