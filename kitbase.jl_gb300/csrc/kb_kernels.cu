@@ -39,6 +39,9 @@ void face_kinds_host(const Geo& g, signed char* kind) {
 
 // reconstruct! for w (src/Solver/solver_reconstruction.jl:111-122 1D, :496-537 2D):
 // one thread per (physical cell, direction).
+// FAST (the FP32 split form): one reciprocal of the cell size per thread in
+// place of two FP64 divisions per component.
+template <bool FAST>
 __global__ void k_wslope(DevState s) {
   const Geo& g = s.g;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -51,11 +54,17 @@ __global__ void k_wslope(DevState s) {
   int step = d == 0 ? 1 : g.nxt;
   double dd = d == 0 ? g.dx : g.dy;  // 0.5 * (dx[i-1] + dx[i]) on a uniform mesh
   double* out = s.sw + ((long)c * 2 + d) * 4;
+  const double rd = FAST ? 1.0 / dd : 0.0;
   for (int k = 0; k < g.NW; ++k) {
     double q0 = s.w[(long)c * 4 + k];
     double qm = (rule == 1 || rule == 3) ? s.w[(long)(c - step) * 4 + k] : 0.0;
     double qp = (rule == 1 || rule == 2) ? s.w[(long)(c + step) * 4 + k] : 0.0;
-    out[k] = slope_of<double>(rule, qm, q0, qp, dd);
+    if (FAST) {
+      const double a = (q0 - qm) * rd, b = (qp - q0) * rd;
+      out[k] = rule == 1 ? vanleer(a, b) : (rule == 2 ? b : (rule == 3 ? a : 0.0));
+    } else {
+      out[k] = slope_of<double>(rule, qm, q0, qp, dd);
+    }
   }
 }
 
@@ -809,7 +818,8 @@ int launch_reconstruct(DevState& s, cudaStream_t st) {
   if (s.flux == FLUX_KFVS) return 0;  // KFVS reads no w slopes
   long n = (long)s.g.nx * s.g.ny * s.g.D;
   if (s.g.interp == 1) return 0;
-  k_wslope<<<nblk(n, 128), 128, 0, st>>>(s);
+  if (s.prec != 0) k_wslope<true><<<nblk(n, 128), 128, 0, st>>>(s);
+  else k_wslope<false><<<nblk(n, 128), 128, 0, st>>>(s);
   return 1;
 }
 
