@@ -1274,9 +1274,10 @@ struct M3Layout {
 // Pass B in the 2D FP32 form.  Thread = one velocity; CTA = 128 velocities x
 // a strip of TX columns x RY rows, marching up the rows.  Rows arrive by TMA
 // (h and b boxes) plus bulk copies (coefficients) into a ring of NS slots,
-// NS - 5 rows ahead of the 4-row stencil window; thread 0 refills a slot once
-// every warp has released the row it held (per-slot "empty" mbarriers), so
-// warps never wait on one another and the window costs no registers.  Each
+// NS - 4 rows ahead of the 4-row stencil window: at the start of row j,
+// thread 0 refills the slot of row j - 2 once every warp has released it
+// (per-slot "empty" mbarriers), so only thread 0 ever waits on other warps
+// and the window costs no registers.  Each
 // x face and y face is evaluated once per velocity and feeds both neighbours.
 template <int FLUX, int TX, int NS>
 __global__ void __launch_bounds__(M3_BS) k_march3(const __grid_constant__ CUtensorMap tmh,
@@ -1475,9 +1476,10 @@ __global__ void __launch_bounds__(M3_BS) k_march3(const __grid_constant__ CUtens
   const bool fastx = g.interp == 2 && i0 >= 2 && i0 + TX <= g.nx - 2;
   for (int j = j0; j < j1; ++j) {
     if (tid == 0 && *vbad == 0) {
-      // refill the slot of row q - NS (released after row q - NS + 1)
-      const int q = j + NS - 3;
-      if (j > j0 && q <= qend) {
+      // refill the slot of row q - NS = j - 2, which every warp released at
+      // the end of row j - 1: the ring then runs NS - 4 rows ahead
+      const int q = j + NS - 2;
+      if (q <= qend) {
         const int r = q - q0;
         if (mbar_wait(&empty[r % NS], ((r - NS) / NS) & 1)) {
           fence_async_smem();
@@ -1897,8 +1899,8 @@ __global__ void __launch_bounds__(M4_THREADS * G, G == 2 ? 4 : 1) k_march4(const
   const bool fastx = g.interp == 2 && i0 >= 2 && i0 + TX <= g.nx - 2;
   for (int j = j0; j < j1; ++j) {
     if (tid == 0 && *vbad == 0) {
-      const int q = j + NS - 3;
-      if (j > j0 && q <= qend) {
+      const int q = j + NS - 2;  // into the slot of row j - 2 (see k_march3)
+      if (q <= qend) {
         const int r = q - q0;
         if (mbar_wait(&empty[r % NS], ((r - NS) / NS) & 1)) {
           fence_async_smem();
