@@ -67,6 +67,8 @@ struct BatchDev {
   const int* nseg;
   int* done;             // [n] segments of the instance finished this step
   double* respart;       // [segments][8] residual partial sums
+  int sst_max;           // largest shared-memory row stride of the batch (floats)
+  int nu4_max;           // largest velocity count, rounded up to 4
   double K, gamma, omega, Pr, tol;
   int coll;
 };
@@ -365,8 +367,18 @@ constexpr int SEG_T = 128;
 constexpr int SEG_ROWS = SEG + 4;
 constexpr int SEG_MAXNU = 256;
 __host__ __device__ inline int seg_stride(int nus) { return (nus + 31) / 32 * 32 + 4; }
-constexpr int SEG_SMEM = 2 * SEG_ROWS * (SEG_MAXNU + 4) * 4 + 2 * SEG_MAXNU * 4 +
-                         (SEG + 1) * 3 * 8 + SEG * 8 + 16 + SEG * 3 * 16 + 8 * 8;
+constexpr int SEG_FT = SEG_T / (SEG + 1);  // threads per face in the face-moment phase
+static_assert(SEG_FT >= 1 && SEG * 8 <= SEG_T, "thread groups of the moment phases");
+// Dynamic shared memory of a segment CTA, sized by the batch's largest row
+// stride and velocity count: h and b windows, velocity tables, fw, q, the
+// 16-byte aligned cell coefficients and the face-moment partials.
+__host__ __device__ inline int seg_smem(int sst_max, int nu4_max) {
+  return 2 * SEG_ROWS * sst_max * 4 + 2 * nu4_max * 4 + (SEG + 1) * 3 * 8 + SEG * 8 + 16 +
+         SEG * 3 * 16 + SEG_T * 6 * 4 + 8 * 8;
+}
+constexpr int SEG_SMEM_MAX = 2 * SEG_ROWS * ((SEG_MAXNU + 31) / 32 * 32 + 4) * 4 +
+                             2 * SEG_MAXNU * 4 + (SEG + 1) * 3 * 8 + SEG * 8 + 16 +
+                             SEG * 3 * 16 + SEG_T * 6 * 4 + 8 * 8;
 
 __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __restrict__ Hin,
                                                      const float* __restrict__ Bin,
@@ -398,13 +410,14 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
   }
   const int sst = seg_stride(ns);
   float* sH = (float*)sm;
-  float* sB = sH + SEG_ROWS * (SEG_MAXNU + 4);
-  float* sU = sB + SEG_ROWS * (SEG_MAXNU + 4);
-  float* sW = sU + SEG_MAXNU;
-  double* sfw = (double*)(sW + SEG_MAXNU);  // [SEG + 1][3]
+  float* sB = sH + SEG_ROWS * B.sst_max;
+  float* sU = sB + SEG_ROWS * B.sst_max;
+  float* sW = sU + B.nu4_max;
+  double* sfw = (double*)(sW + B.nu4_max);  // [SEG + 1][3]
   double* sq = sfw + (SEG + 1) * 3;          // [SEG]
   // [SEG][3] float4 cell coefficients, 16-byte aligned
   float4* scc = (float4*)(((unsigned long long)(sq + SEG) + 15) & ~15ull);
+  float* sred = (float*)(scc + SEG * 3);  // [SEG_T][6]: face-moment DF partials
   // window rows r0 .. r1-1 (cells incl. ghosts), smem row = cell - r0
   const int r0 = max(i0 - 2, -ng), r1 = min(i1 + 2, nx + ng), nrow = r1 - r0;
   if (tid == 0) {
@@ -447,21 +460,22 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
   auto rowH = [&](int c) { return sH + (c - r0) * sst; };
   auto rowB = [&](int c) { return sB + (c - r0) * sst; };
 
-  // ---- face moments of faces fa .. fb (4 threads per face, velocities v = q mod 4)
+  // ---- face moments of faces fa .. fb: SEG_FT threads per face (velocities
+  // v = q mod SEG_FT), so the SEG + 1 faces keep all four warps busy
   const int fa = max(i0, 1), fb = min(i1, nx - 1);
   const int ca = max(i0, 1), cb = min(i1, nx - 1);  // stepped cells [ca, cb)
   {
-    const int j = tid >> 2, q = tid & 3;
+    const int j = tid / SEG_FT, q = tid - j * SEG_FT;
     const int f = fa + j;
     BSum<float> s0, s1, s2;
     s0.init();
     s1.init();
     s2.init();
-    if (f <= fb) {
+    if (j <= SEG && f <= fb) {
       const int iL = f - 1, iR = f;
       const int rL = brule(iL, nx, ng), rR = brule(iR, nx, ng);
       int it = 0;
-      for (int v = q; v < nu; v += 4, ++it) {
+      for (int v = q; v < nu; v += SEG_FT, ++it) {
         const float u = sU[v];
         const bool pos = u >= 0.f;
         const int c = pos ? iL : iR;
@@ -489,38 +503,32 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
         }
       }
     }
-    // the 4 threads of a face: compensated pair sums over lanes q
-    DF d0, d1, d2;
+    // each thread's compensated partials, merged per face below in thread
+    // order: both segments that share a face map it to the same threads q,
+    // so they compute bit-identical fw (conservation holds exactly)
     s0.flush();
     s1.flush();
     s2.flush();
-    d0 = s0.d;
-    d1 = s1.d;
-    d2 = s2.d;
-#pragma unroll
-    for (int m = 1; m <= 2; m <<= 1) {
-      d0 = df_merge(d0, df_shfl_xor(d0, m));
-      d1 = df_merge(d1, df_shfl_xor(d1, m));
-      d2 = df_merge(d2, df_shfl_xor(d2, m));
-    }
-    if (q == 0 && f <= fb) {
-      sfw[j * 3 + 0] = (double)d0.hi + (double)d0.lo;
-      sfw[j * 3 + 1] = (double)d1.hi + (double)d1.lo;
-      sfw[j * 3 + 2] = 0.5 * ((double)d2.hi + (double)d2.lo);
-    }
+    float* o = sred + tid * 6;
+    o[0] = s0.d.hi;
+    o[1] = s0.d.lo;
+    o[2] = s1.d.hi;
+    o[3] = s1.d.lo;
+    o[4] = s2.d.hi;
+    o[5] = s2.d.lo;
   }
-  // ---- old heat flux of the stepped cells (Shakhov), 4 threads per cell
+  // ---- old heat flux of the stepped cells (Shakhov), 8 threads per cell
   if (B.coll == COLL_SHAKHOV) {
-    const int j = tid >> 2, q = tid & 3;
+    const int j = tid >> 3, q = tid & 7;
     const int i = ca + j;
     BSum<float> s;
     s.init();
-    if (i < cb) {
+    if (j < SEG && i < cb) {
       const float Uc = float(B.prim[(c0 + i + ng) * 4 + 1]);
       const float* hc = rowH(i);
       const float* bc = rowB(i);
       int it = 0;
-      for (int v = q; v < nu; v += 4, ++it) {
+      for (int v = q; v < nu; v += 8, ++it) {
         const float cu = sU[v] - Uc;
         s.add(sW[v] * cu * (cu * cu * hc[v] + bc[v]));
         if ((it & 7) == 7) s.flush();
@@ -529,8 +537,27 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
     s.flush();
     DF d = s.d;
 #pragma unroll
-    for (int m = 1; m <= 2; m <<= 1) d = df_merge(d, df_shfl_xor(d, m));
-    if (q == 0 && i < cb) sq[j] = 0.5 * ((double)d.hi + (double)d.lo);
+    for (int m = 1; m <= 4; m <<= 1) d = df_merge(d, df_shfl_xor(d, m));
+    if (q == 0 && j < SEG && i < cb) sq[j] = 0.5 * ((double)d.hi + (double)d.lo);
+  }
+  __syncthreads();
+  // face f = fa + j, moment m: the SEG_FT partials of its threads
+  if (tid < 3 * (SEG + 1)) {
+    const int j = tid / 3, m = tid - 3 * j;
+    if (fa + j <= fb) {
+      const float* o = sred + j * SEG_FT * 6 + 2 * m;
+      DF d;
+      d.hi = o[0];
+      d.lo = o[1];
+      for (int t = 1; t < SEG_FT; ++t) {
+        DF e;
+        e.hi = o[6 * t];
+        e.lo = o[6 * t + 1];
+        d = df_merge(d, e);
+      }
+      const double v = (double)d.hi + (double)d.lo;
+      sfw[j * 3 + m] = m == 2 ? 0.5 * v : v;
+    }
   }
   __syncthreads();
   // ---- cell parameters of the stepped cells (one thread per cell, FP64)
@@ -937,6 +964,12 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   d.nseg = d_nseg;
   d.done = d_done;
   d.respart = d_respart;
+  d.sst_max = 4;
+  d.nu4_max = 4;
+  for (int b = 0; b < n; ++b) {
+    d.sst_max = std::max(d.sst_max, kb::seg_stride(B->nus[b]));
+    d.nu4_max = std::max(d.nu4_max, B->nus[b]);
+  }
   d.cell_off = d_co;
   d.elem_off = d_eo;
   d.vel_off = d_vo;
@@ -1078,12 +1111,13 @@ static void batch_launch(kb_batch* B, int cur) {
     static bool raised[64] = {false};
     int dev = 0;
     cudaGetDevice(&dev);
-    if (kb::SEG_SMEM > 48 * 1024 && dev >= 0 && dev < 64 && !raised[dev]) {
+    if (dev >= 0 && dev < 64 && !raised[dev]) {
       cudaFuncSetAttribute(kb::k_batch_seg, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kb::SEG_SMEM);
+                           kb::SEG_SMEM_MAX);
       raised[dev] = true;
     }
-    kb::k_batch_seg<<<(unsigned)B->nseg, kb::SEG_T, kb::SEG_SMEM, B->stream>>>(
+    const int smem = kb::seg_smem(B->d.sst_max, B->d.nu4_max);
+    kb::k_batch_seg<<<(unsigned)B->nseg, kb::SEG_T, smem, B->stream>>>(
         B->d, (const float*)B->h[cur], (const float*)B->bq[cur], (float*)B->h[cur ^ 1],
         (float*)B->bq[cur ^ 1]);
     return;
