@@ -65,7 +65,6 @@ struct BatchDev {
   const int* seg_i0;
   const int* seg_first;
   const int* nseg;
-  int* done;             // [n] segments of the instance finished this step
   double* respart;       // [segments][8] residual partial sums
   int sst_max;           // largest shared-memory row stride of the batch (floats)
   int nu4_max;           // largest velocity count, rounded up to 4
@@ -686,27 +685,36 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
   };
   if (all_vl) pointwise(std::true_type{});
   else pointwise(std::false_type{});
-  // ---- the instance's last segment sums the partials in segment order
+  // ---- this segment's residual partial sums (k_batch_seg_res adds them up)
   if (tid == 0) {
     double* pr = B.respart + (long)k * 8;
     for (int m = 0; m < 6; ++m) pr[m] = (double)rr[m];
-    __threadfence();
-    const int prev = atomicAdd(&B.done[b], 1);
-    if (prev == B.nseg[b] - 1) {
-      __threadfence();
-      double t[6] = {0, 0, 0, 0, 0, 0};
-      const int s0 = B.seg_first[b], s1 = s0 + B.nseg[b];
-      for (int sgi = s0; sgi < s1; ++sgi)
-        for (int m = 0; m < 6; ++m) t[m] += __ldcg(B.respart + (long)sgi * 8 + m);
-      double mx = 0.0;
-      for (int m = 0; m < 3; ++m) {
-        double r = sqrt(t[m] * nx) / (t[3 + m] + 1.e-7);
-        B.residual[b * 4 + m] = r;
-        mx = fmax(mx, r);
-      }
-      if (mx < B.tol) B.active[b] = 0;
-      B.done[b] = 0;
+  }
+}
+
+// Residual of each active instance of the segment form
+// (src/Solver/solver_update.jl:86-88) and its convergence flag.  One warp per
+// instance: lane l adds the partial sums of segments l, l + 32, ... in order,
+// then a fixed shuffle tree combines the lanes (deterministic).  Launched
+// after k_batch_seg on the same stream, so no segment CTA waits on a fence or
+// an atomic counter of the others.
+__global__ void k_batch_seg_res(BatchDev B) {
+  const int b = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (b >= B.n || !B.active[b]) return;  // warp-uniform
+  double t[6] = {0, 0, 0, 0, 0, 0};
+  const int s0 = B.seg_first[b], s1 = s0 + B.nseg[b];
+  for (int sgi = s0 + lane; sgi < s1; sgi += 32)
+    for (int m = 0; m < 6; ++m) t[m] += B.respart[(long)sgi * 8 + m];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) t[m] = warp_sum(t[m]);
+  if (lane == 0) {
+    double mx = 0.0;
+    for (int m = 0; m < 3; ++m) {
+      const double r = sqrt(t[m] * B.nx[b]) / (t[3 + m] + 1.e-7);
+      B.residual[b * 4 + m] = r;
+      mx = fmax(mx, r);
     }
+    if (mx < B.tol) B.active[b] = 0;
   }
 }
 
@@ -870,7 +878,7 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   if ((rc = balloc(B, &p, sizeof(T) * (size_t)(count))) != KB_OK) return fail_out(rc); \
   dst = (T*)p;
   int *d_order, *d_nx, *d_ng, *d_nu, *d_vo, *d_active, *d_counter, *d_status;
-  int *d_nus, *d_segb, *d_segi0, *d_segfirst, *d_nseg, *d_done;
+  int *d_nus, *d_segb, *d_segi0, *d_segfirst, *d_nseg;
   double* d_respart;
   long *d_co, *d_eo, *d_fo;
   double *d_dx, *d_dt, *d_mu, *d_u, *d_w, *d_wv, *d_prim, *d_fw, *d_q, *d_cp, *d_res;
@@ -884,7 +892,6 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   BALLOC(d_segi0, int, B->nseg);
   BALLOC(d_segfirst, int, n);
   BALLOC(d_nseg, int, n);
-  BALLOC(d_done, int, n);
   BALLOC(d_respart, double, B->nseg * 8);
   BALLOC(d_vo, int, n);
   BALLOC(d_active, int, n);
@@ -931,7 +938,6 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   ok &= cudaMemcpy(d_segi0, seg_i0.data(), sizeof(int) * B->nseg, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_segfirst, seg_first.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_nseg, nseg.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
-  ok &= cudaMemset(d_done, 0, sizeof(int) * n) == cudaSuccess;
   ok &= cudaMemset(d_respart, 0, sizeof(double) * B->nseg * 8) == cudaSuccess;
   ok &= cudaMemcpy(d_vo, vel_off.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_active, ones.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -962,7 +968,6 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   d.seg_i0 = d_segi0;
   d.seg_first = d_segfirst;
   d.nseg = d_nseg;
-  d.done = d_done;
   d.respart = d_respart;
   d.sst_max = 4;
   d.nu4_max = 4;
@@ -1106,6 +1111,10 @@ extern "C" int kb_batch_set_dt(kb_batch_t* B, const double* dt) {
   return KB_OK;
 }
 
+// Kernels batch_launch issues per step: the FP32 segment form adds the
+// per-instance residual kernel.
+static int batch_kernels_per_step(const kb_batch* B) { return B->prec == KB_PREC_FP32 ? 2 : 1; }
+
 static void batch_launch(kb_batch* B, int cur) {
   if (B->prec == KB_PREC_FP32) {  // fused segments (one pass over HBM)
     static bool raised[64] = {false};
@@ -1120,6 +1129,7 @@ static void batch_launch(kb_batch* B, int cur) {
     kb::k_batch_seg<<<(unsigned)B->nseg, kb::SEG_T, smem, B->stream>>>(
         B->d, (const float*)B->h[cur], (const float*)B->bq[cur], (float*)B->h[cur ^ 1],
         (float*)B->bq[cur ^ 1]);
+    kb::k_batch_seg_res<<<(unsigned)((B->n + 3) / 4), 128, 0, B->stream>>>(B->d);
     return;
   }
   cudaMemsetAsync(B->d.counter, 0, sizeof(int), B->stream);
@@ -1171,11 +1181,11 @@ extern "C" int kb_batch_step(kb_batch_t* B, int32_t nsteps, double tol, double* 
   for (int k = 0; k < pairs; ++k) {
     if (cudaGraphLaunch(B->graph, B->stream) != cudaSuccess)
       return bfail(KB_ERR_CUDA, "graph launch failed");
-    B->launches += 2;
+    B->launches += 2 * batch_kernels_per_step(B);
   }
   if (nsteps & 1) {
     batch_launch(B, B->cur);
-    B->launches++;
+    B->launches += batch_kernels_per_step(B);
     B->cur ^= 1;
   }
   if (cudaStreamSynchronize(B->stream) != cudaSuccess)
