@@ -359,8 +359,8 @@ __device__ __forceinline__ float fexp(float x) {
 // the step is one pass over HBM (each value read once, plus a 2-cell halo on
 // each side, and written once).  The window arrives by bulk async copies, one
 // per row, into rows whose stride is = 4 (mod 32) floats so that the face
-// threads read without bank conflicts.  Per-instance residuals are summed by
-// the instance's last segment in segment order (deterministic).
+// threads read without bank conflicts.  Per-instance residuals are summed
+// by k_batch_seg_res after the step, in segment order (deterministic).
 constexpr int SEG = 16;
 constexpr int SEG_T = 128;
 constexpr int SEG_ROWS = SEG + 4;
@@ -372,12 +372,12 @@ static_assert(SEG_FT >= 1 && SEG * 8 <= SEG_T, "thread groups of the moment phas
 // stride and velocity count: h and b windows, velocity tables, fw, q, the
 // 16-byte aligned cell coefficients and the face-moment partials.
 __host__ __device__ inline int seg_smem(int sst_max, int nu4_max) {
-  return 2 * SEG_ROWS * sst_max * 4 + 2 * nu4_max * 4 + (SEG + 1) * 3 * 8 + SEG * 8 + 16 +
-         SEG * 3 * 16 + SEG_T * 6 * 4 + 8 * 8;
+  return 2 * SEG_ROWS * sst_max * 4 + 2 * nu4_max * 4 + (SEG + 1) * 3 * 8 + 16 + SEG * 3 * 16 +
+         SEG_T * 6 * 4 + SEG * 3 * 8 + 8 * 8;
 }
 constexpr int SEG_SMEM_MAX = 2 * SEG_ROWS * ((SEG_MAXNU + 31) / 32 * 32 + 4) * 4 +
-                             2 * SEG_MAXNU * 4 + (SEG + 1) * 3 * 8 + SEG * 8 + 16 +
-                             SEG * 3 * 16 + SEG_T * 6 * 4 + 8 * 8;
+                             2 * SEG_MAXNU * 4 + (SEG + 1) * 3 * 8 + 16 + SEG * 3 * 16 +
+                             SEG_T * 6 * 4 + SEG * 3 * 8 + 8 * 8;
 
 __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __restrict__ Hin,
                                                      const float* __restrict__ Bin,
@@ -413,9 +413,8 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
   float* sU = sB + SEG_ROWS * B.sst_max;
   float* sW = sU + B.nu4_max;
   double* sfw = (double*)(sW + B.nu4_max);  // [SEG + 1][3]
-  double* sq = sfw + (SEG + 1) * 3;          // [SEG]
   // [SEG][3] float4 cell coefficients, 16-byte aligned
-  float4* scc = (float4*)(((unsigned long long)(sq + SEG) + 15) & ~15ull);
+  float4* scc = (float4*)(((unsigned long long)(sfw + (SEG + 1) * 3) + 15) & ~15ull);
   float* sred = (float*)(scc + SEG * 3);  // [SEG_T][6]: face-moment DF partials
   // window rows r0 .. r1-1 (cells incl. ghosts), smem row = cell - r0
   const int r0 = max(i0 - 2, -ng), r1 = min(i1 + 2, nx + ng), nrow = r1 - r0;
@@ -516,105 +515,129 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
     o[4] = s2.d.hi;
     o[5] = s2.d.lo;
   }
-  // ---- old heat flux of the stepped cells (Shakhov), 8 threads per cell
-  if (B.coll == COLL_SHAKHOV) {
-    const int j = tid >> 3, q = tid & 7;
-    const int i = ca + j;
-    BSum<float> s;
-    s.init();
-    if (j < SEG && i < cb) {
-      const float Uc = float(B.prim[(c0 + i + ng) * 4 + 1]);
-      const float* hc = rowH(i);
-      const float* bc = rowB(i);
-      int it = 0;
-      for (int v = q; v < nu; v += 8, ++it) {
-        const float cu = sU[v] - Uc;
-        s.add(sW[v] * cu * (cu * cu * hc[v] + bc[v]));
-        if ((it & 7) == 7) s.flush();
-      }
-    }
-    s.flush();
-    DF d = s.d;
-#pragma unroll
-    for (int m = 1; m <= 4; m <<= 1) d = df_merge(d, df_shfl_xor(d, m));
-    if (q == 0 && j < SEG && i < cb) sq[j] = 0.5 * ((double)d.hi + (double)d.lo);
-  }
-  __syncthreads();
-  // face f = fa + j, moment m: the SEG_FT partials of its threads
-  if (tid < 3 * (SEG + 1)) {
-    const int j = tid / 3, m = tid - 3 * j;
-    if (fa + j <= fb) {
-      const float* o = sred + j * SEG_FT * 6 + 2 * m;
-      DF d;
-      d.hi = o[0];
-      d.lo = o[1];
-      for (int t = 1; t < SEG_FT; ++t) {
-        DF e;
-        e.hi = o[6 * t];
-        e.lo = o[6 * t + 1];
-        d = df_merge(d, e);
-      }
-      const double v = (double)d.hi + (double)d.lo;
-      sfw[j * 3 + m] = m == 2 ? 0.5 * v : v;
-    }
-  }
-  __syncthreads();
-  // ---- cell parameters of the stepped cells (one thread per cell, FP64)
-  // residual terms of the cell: a convergence monitor, summed in FP32 below
-  float rr[6] = {0, 0, 0, 0, 0, 0};
+  // the old prim of the stepped cells, read before warp 0 overwrites it
+  // (warps 1 and 2 need the old U while warp 0 updates the cells)
+  double* spo = (double*)(sred + SEG_T * 6);  // [SEG][3] rho, U, lambda
   if (tid < cb - ca) {
-    const double dx = B.dx[b], dt = B.dt[b];
-    const int i = ca + tid;
-    const long c = c0 + i + ng;
-    double* w = B.w + c * 4;
-    double* p = B.prim + c * 4;
-    const double* fL = sfw + (i - fa) * 3;
-    const double* fR = sfw + (i + 1 - fa) * 3;
-    double wo[3] = {w[0], w[1], w[2]};
-    double lo = p[2], rho_o = p[0], Uo = p[1];
-    const double idx = 1.0 / dx;
-    for (int m = 0; m < 3; ++m) w[m] += (fL[m] - fR[m]) * idx;
-    double pn[4];
-    conserve_prim<true>(w, 3, B.gamma, pn);
-    p[0] = pn[0];
-    p[1] = pn[1];
-    p[2] = pn[2];
-    for (int m = 0; m < 3; ++m) {
-      double d = w[m] - wo[m];
-      rr[m] = float(d * d);
-      rr[3 + m] = float(fabs(w[m]));
-    }
-    double lam = pn[2];
-    if (!(pn[0] > 0.0) || !(lam > 0.0) || !isfinite(pn[0]) || !isfinite(lam)) atomicOr(B.status, 1);
-    // w, prim and q stay FP64; the coefficients below feed only the FP32
-    // pointwise update, so they are formed in FP32 (GB300's FP64 rate is
-    // 1/64 of its FP32 rate, and in 1D a cell has only ~100 velocities)
-    const float rf = float(pn[0]), lf = float(lam), rof = float(rho_o), lof = float(lo);
-    const float tau = float(B.mu[b]) * 2.f * powf(lf, float(1.0 - B.omega)) / rf;
-    const float dtt = float(dt) / tau;
-    const float Kf = float(B.K);
-    float4* kc = scc + tid * 3;
-    // new Maxwellian: density factor, U, lambda, K / (2 lambda)
-    kc[0] = make_float4(rf * sqrtf(lf * float(1.0 / PI)), float(pn[1]), lf, Kf / (2.f * lf));
-    // dt / tau, 1 / (1 + dt / tau), old Maxwellian (Shakhov) density factor and U
-    kc[1] = make_float4(dtt, 1.f / (1.f + dtt), rof * sqrtf(lof * float(1.0 / PI)), float(Uo));
-    // old lambda, K / (2 lambda), Shakhov heat-flux factor
-    kc[2] = make_float4(lof, Kf / (2.f * lof),
-                        B.coll == COLL_SHAKHOV
-                            ? float(0.8 * (1.0 - B.Pr)) * (lof * lof) / rof * float(sq[tid])
-                            : 0.f,
-                        0.f);
+    const double* p = B.prim + (c0 + ca + tid + ng) * 4;
+    spo[tid * 3 + 0] = p[0];
+    spo[tid * 3 + 1] = p[1];
+    spo[tid * 3 + 2] = p[2];
   }
-  // residual partial sums of the segment: the cells are all in the first
-  // warp (SEG <= 32), reduced in a fixed shuffle order (FP32: GB300's FP64
-  // pipe would make this tree the longest chain of the cell phase)
-  static_assert(SEG <= 32, "the cell update of a segment runs in the first warp");
+  __syncthreads();  // face partials and old prim in shared memory
+  // Warp 0: merge the face moments, then the FP64 cell update; warps 1 and 2
+  // meanwhile: the old heat flux (Shakhov) of the stepped cells.
+  static_assert(SEG <= 32 && 4 * SEG <= 64, "cell update on warp 0, heat flux on warps 1-2");
   if (wid == 0) {
+    // residual terms of the cell: a convergence monitor, summed in FP32 below
+    float rr[6] = {0, 0, 0, 0, 0, 0};
+    // face f = fa + jf, moment m: the SEG_FT partials of its threads, in order
+    for (int t0 = lane; t0 < 3 * (SEG + 1); t0 += 32) {
+      const int jf = t0 / 3, m = t0 - 3 * jf;
+      if (fa + jf <= fb) {
+        const float* o = sred + jf * SEG_FT * 6 + 2 * m;
+        DF d;
+        d.hi = o[0];
+        d.lo = o[1];
+        for (int t = 1; t < SEG_FT; ++t) {
+          DF e;
+          e.hi = o[6 * t];
+          e.lo = o[6 * t + 1];
+          d = df_merge(d, e);
+        }
+        const double v = (double)d.hi + (double)d.lo;
+        sfw[jf * 3 + m] = m == 2 ? 0.5 * v : v;
+      }
+    }
+    __syncwarp();
+    // ---- cell parameters of the stepped cells (one lane per cell, FP64)
+    if (lane < cb - ca) {
+      const double dx = B.dx[b], dt = B.dt[b];
+      const int i = ca + lane;
+      const long c = c0 + i + ng;
+      double* w = B.w + c * 4;
+      double* p = B.prim + c * 4;
+      const double* fL = sfw + (i - fa) * 3;
+      const double* fR = sfw + (i + 1 - fa) * 3;
+      double wo[3] = {w[0], w[1], w[2]};
+      const double rho_o = spo[lane * 3 + 0], Uo = spo[lane * 3 + 1], lo = spo[lane * 3 + 2];
+      const double idx = 1.0 / dx;
+      for (int m = 0; m < 3; ++m) w[m] += (fL[m] - fR[m]) * idx;
+      double pn[4];
+      conserve_prim<true>(w, 3, B.gamma, pn);
+      p[0] = pn[0];
+      p[1] = pn[1];
+      p[2] = pn[2];
+      for (int m = 0; m < 3; ++m) {
+        double d = w[m] - wo[m];
+        rr[m] = float(d * d);
+        rr[3 + m] = float(fabs(w[m]));
+      }
+      double lam = pn[2];
+      if (!(pn[0] > 0.0) || !(lam > 0.0) || !isfinite(pn[0]) || !isfinite(lam)) atomicOr(B.status, 1);
+      // w, prim and q stay FP64; the coefficients below feed only the FP32
+      // pointwise update, so they are formed in FP32 (GB300's FP64 rate is
+      // 1/64 of its FP32 rate, and in 1D a cell has only ~100 velocities)
+      const float rf = float(pn[0]), lf = float(lam), rof = float(rho_o), lof = float(lo);
+      const float tau = float(B.mu[b]) * 2.f * powf(lf, float(1.0 - B.omega)) / rf;
+      const float dtt = float(dt) / tau;
+      const float Kf = float(B.K);
+      float4* kc = scc + lane * 3;
+      // new Maxwellian: density factor, U, lambda, K / (2 lambda)
+      kc[0] = make_float4(rf * sqrtf(lf * float(1.0 / PI)), float(pn[1]), lf, Kf / (2.f * lf));
+      // dt / tau, 1 / (1 + dt / tau), old Maxwellian (Shakhov) density factor and U
+      kc[1] = make_float4(dtt, 1.f / (1.f + dtt), rof * sqrtf(lof * float(1.0 / PI)), float(Uo));
+      // old lambda, K / (2 lambda); .z (the Shakhov heat-flux factor) comes
+      // from warps 1-2
+      float* k2 = (float*)(kc + 2);
+      k2[0] = lof;
+      k2[1] = Kf / (2.f * lof);
+      k2[3] = 0.f;
+    }
+    // residual partial sums of the segment, in a fixed shuffle order (FP32:
+    // GB300's FP64 pipe would make this tree the longest chain of the phase)
 #pragma unroll
     for (int m = 0; m < 6; ++m) {
 #pragma unroll
       for (int o = 16; o >= 1; o >>= 1) rr[m] += __shfl_xor_sync(0xffffffffu, rr[m], o);
     }
+    // this segment's residual partial sums (k_batch_seg_res adds them up)
+    if (lane == 0) {
+      double* pr = B.respart + (long)k * 8;
+#pragma unroll
+      for (int m = 0; m < 6; ++m) pr[m] = (double)rr[m];
+    }
+  } else if (wid <= 2) {
+    // ---- old heat flux of the stepped cells, 4 threads per cell, and the
+    // Shakhov factor 0.8 (1 - Pr) lambda^2 / rho q of the cell coefficients
+    const int lt = tid - 32, jc = lt >> 2, q = lt & 3;
+    const int i = ca + jc;
+    float qf = 0.f;
+    if (B.coll == COLL_SHAKHOV) {
+      BSum<float> sm4;
+      sm4.init();
+      if (i < cb) {
+        const float Uc = float(spo[jc * 3 + 1]);
+        const float* hc = rowH(i);
+        const float* bc = rowB(i);
+        int it = 0;
+        for (int v = q; v < nu; v += 4, ++it) {
+          const float cu = sU[v] - Uc;
+          sm4.add(sW[v] * cu * (cu * cu * hc[v] + bc[v]));
+          if ((it & 7) == 7) sm4.flush();
+        }
+      }
+      sm4.flush();
+      DF d = sm4.d;
+#pragma unroll
+      for (int m = 1; m <= 2; m <<= 1) d = df_merge(d, df_shfl_xor(d, m));
+      if (i < cb) {
+        const double qc = 0.5 * ((double)d.hi + (double)d.lo);
+        const float rof = float(spo[jc * 3 + 0]), lof = float(spo[jc * 3 + 2]);
+        qf = float(0.8 * (1.0 - B.Pr)) * (lof * lof) / rof * float(qc);
+      }
+    }
+    if (q == 0 && i < cb) ((float*)(scc + jc * 3 + 2))[2] = qf;
   }
   __syncthreads();  // cell coefficients ready for the pointwise update
   // ---- pointwise KFVS flux + relaxation, one thread per velocity.  Every
@@ -685,11 +708,6 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
   };
   if (all_vl) pointwise(std::true_type{});
   else pointwise(std::false_type{});
-  // ---- this segment's residual partial sums (k_batch_seg_res adds them up)
-  if (tid == 0) {
-    double* pr = B.respart + (long)k * 8;
-    for (int m = 0; m < 6; ++m) pr[m] = (double)rr[m];
-  }
 }
 
 // Residual of each active instance of the segment form
