@@ -5,14 +5,19 @@
 // (ghosts included) and a velocity table at vel_off[b] of length nu[b]; its
 // distributions start at elem_off[b] in the flat h / b arrays and are
 // [cell][nus[b]] (velocity fastest, rows padded to a multiple of 4 values so
-// every row starts 16-byte aligned for bulk copies).  A CTA takes instances from a work counter
-// (largest first) and runs the whole step of an instance:
-//   A  face moments fw (one thread per face looping over velocities, blocked
-//      compensated sums) and the old heat flux q (one thread per cell)
-//   C  cell parameters: w, prim, tau, residual terms (one thread per cell),
-//      block-reduced residual and the instance's convergence flag
+// every row starts 16-byte aligned for bulk copies).  Each step runs three
+// phases per instance:
+//   A  face moments fw (blocked compensated sums over velocities) and the
+//      old heat flux q
+//   C  cell parameters: w, prim, tau, residual terms, the instance's
+//      residual and convergence flag
 //   D  pointwise KFVS flux + BGK / Shakhov relaxation (one thread per
-//      velocity, marching the cells with a register window)
+//      velocity, marching the cells)
+// FP32 split form: k_batch_seg fuses A, C and D for one 16-cell segment of
+// one instance per CTA (one pass over HBM), and k_batch_seg_res forms each
+// instance's residual from its segments' partial sums.  FP64 form
+// (k_batch_step, the comparator): a CTA takes whole instances from a work
+// counter (largest first).
 // Covers the configuration of the batched shock-structure ensemble: KFVS,
 // BGK or Shakhov, fixed boundaries, van Leer, up to 256 velocities.
 #include <cuda_runtime.h>
