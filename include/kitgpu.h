@@ -228,8 +228,9 @@ int kb_get_stream(kb_handle_t* h, void** stream);
 
 /* ------------------------------------------------------------------ batch
  * Many independent 1D2F1V solves with uneven cell counts and velocity grids,
- * advanced by one persistent kernel launch per step over a flattened ragged
- * index, two steps captured as a CUDA graph.  Each instance is what the
+ * advanced by one fused kernel launch per step over a flattened ragged index
+ * (the FP32 split form adds a small per-instance residual kernel), two steps
+ * captured as a CUDA graph.  Each instance is what the
  * reference would run as its own solve! (src/Solver/solver_main.jl:12-76) with
  * KFVS, BGK / Shakhov, fixed boundaries and van Leer slopes; a launch is the
  * loop of that call over all instances.  Instance b has nx[b] cells (plus
