@@ -374,8 +374,9 @@ __host__ __device__ inline int seg_stride(int nus) { return (nus + 31) / 32 * 32
 constexpr int SEG_FT = SEG_T / (SEG + 1);  // threads per face in the face-moment phase
 static_assert(SEG_FT >= 1 && SEG * 8 <= SEG_T, "thread groups of the moment phases");
 // Dynamic shared memory of a segment CTA, sized by the batch's largest row
-// stride and velocity count: h and b windows, velocity tables, fw, q, the
-// 16-byte aligned cell coefficients and the face-moment partials.
+// stride and velocity count: h and b windows, velocity tables, fw, the
+// 16-byte aligned cell coefficients, the face-moment partials and the old
+// prim of the stepped cells.
 __host__ __device__ inline int seg_smem(int sst_max, int nu4_max) {
   return 2 * SEG_ROWS * sst_max * 4 + 2 * nu4_max * 4 + (SEG + 1) * 3 * 8 + 16 + SEG * 3 * 16 +
          SEG_T * 6 * 4 + SEG * 3 * 8 + 8 * 8;

@@ -1253,7 +1253,7 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 && TX < 4 ? 384 : 256) / B
 // Shared-memory ring of the 2D FP32 update: one slot per grid row of the
 // strip.  The slots' h and b boxes (TX+4 columns incl. the 2-cell x halo on
 // each side, M3_BS velocities; [column][velocity]) come first, each box on a
-// multiple of 4 KB; then the slots' coefficient blocks (x faces [TX+1], y
+// multiple of 1 KB; then the slots' coefficient blocks (x faces [TX+1], y
 // faces above the row [TX], cells [TX]), packed at 16-byte multiples so that
 // no padding sits between slots.
 constexpr int M3_BS = KB_TMA_VBOX;  // velocities (threads) per CTA, one TMA box
