@@ -526,9 +526,9 @@ __global__ void __launch_bounds__(MOM_THREADS) k_mom_st(const __grid_constant__ 
         one(S, Sw, vl, fast_tag, I0{});
       }
     }
-    // flush the FP32 partials (8 velocities per lane) into the compensated
+    // flush the FP32 partials (16 velocities per lane) into the compensated
     // sums; the interior form never touches the segment's last face
-    if (k & 1) {
+    if ((k & 3) == 3) {
 #pragma unroll
       for (int f = 0; f < (FAST ? TS : TS + 1); ++f)
 #pragma unroll
