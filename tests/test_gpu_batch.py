@@ -57,6 +57,28 @@ def test_batch_fp32_split_error(gpu_lib):
         assert max(rho_u_t_error(outs[k]["prim"], ref["prim"])) < 1e-5
 
 
+@pytest.mark.parametrize("coll", ["shakhov", "bgk"])
+def test_batch_fp32_edge_sizes(gpu_lib, coll):
+    """Segment and velocity edge cases of the FP32 segment form: the smallest
+    grid (3 cells), a one-segment instance (16 cells), a last segment of one
+    cell (17), a last segment of one stepped cell (33), and velocity counts
+    that are odd, not a multiple of 4, just above and at the 128 / 256
+    boundaries of the thread mapping.  Each instance against its own FP64
+    single solve, within 1e-5."""
+    cfgs = [KB.shock_config(Ma, nx, nu, coll=coll) for Ma, nx, nu in
+            [(1.5, 3, 5), (2.0, 16, 31), (3.0, 17, 128), (4.0, 33, 129), (6.0, 40, 256),
+             (1.2, 18, 7)]]
+    sets = KB.solver_sets(cfgs)
+    bt = KB.Batch(sets, "fp32")
+    bt.upload_initial()
+    dt = bt.timestep()
+    bt.step(40)
+    outs = bt.download()
+    for k, KS in enumerate(sets):
+        ref = single(KS, dt[k], 40)
+        assert max(rho_u_t_error(outs[k]["prim"], ref["prim"])) < 1e-5, k
+
+
 def test_instance_independent_of_batch(gpu_lib):
     cfgs = small_ensemble(n=5, seed=3)
     sets = KB.solver_sets(cfgs)
