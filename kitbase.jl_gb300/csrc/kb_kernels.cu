@@ -72,9 +72,12 @@ __global__ void k_wslope(DevState s) {
 
 // log2-form exponent of rho (lam/pi)^(D/2) exp(-lam ((un-U)^2 + (ut-V)^2)) as
 // E.x + E.y un + E.z ut + E.w c2.
+// FAST (the FP32 split form): log2 of the density factor in FP32.
+template <bool FAST = false>
 __device__ inline float4 maxwell_exp2(double rho_n, double U, double V, double lam) {
   float4 E;
-  E.x = rho_n > 0.0 ? float(log2(rho_n) - lam * (U * U + V * V) * LOG2E) : -200.f;
+  const double l2r = rho_n > 0.0 ? (FAST ? double(log2f(float(rho_n))) : log2(rho_n)) : 0.0;
+  E.x = rho_n > 0.0 ? float(l2r - lam * (U * U + V * V) * LOG2E) : -200.f;
   E.y = float(2.0 * lam * U * LOG2E);
   E.z = float(2.0 * lam * V * LOG2E);
   E.w = float(-lam * LOG2E);
@@ -82,6 +85,7 @@ __device__ inline float4 maxwell_exp2(double rho_n, double U, double V, double l
 }
 
 // FP32 monomial coefficients of the interface flux (see FaceCoef32).
+template <bool FAST = false>
 __device__ __forceinline__ FaceCoef32 face_coef32(const Geo& g, const FaceParam& P, int flux, double dd) {
   FaceCoef32 c;
   float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -91,8 +95,8 @@ __device__ __forceinline__ FaceCoef32 face_coef32(const Geo& g, const FaceParam&
   c.T.y = float(P.tr[1] / dd);
   if (flux == FLUX_KFVS) return c;
   double lam = P.prim[3], rho = P.prim[0];
-  double rho_n = g.D == 1 ? rho * sqrt(lam / PI) : rho * (lam / PI);
-  c.E = maxwell_exp2(rho_n, P.prim[1], P.prim[2], lam);
+  double rho_n = g.D == 1 ? rho * t_sqrt<FAST>(lam / PI) : rho * (lam / PI);
+  c.E = maxwell_exp2<FAST>(rho_n, P.prim[1], P.prim[2], lam);
   double cB = g.K / (2.0 * lam);
   const double* Mt = P.Mt;
   if (flux == FLUX_KCU) {
@@ -241,7 +245,7 @@ __global__ void k_face_param(DevState s, double dt) {
     }
   }
   s.fp[f] = P;
-  s.fc[f] = face_coef32(g, P, FLUX, r.d == 0 ? g.dx : g.dy);
+  s.fc[f] = face_coef32<FAST>(g, P, FLUX, r.d == 0 ? g.dx : g.dy);
   FaceParamF F;
   double lam = P.prim[3] > 0 ? P.prim[3] : 1.0;
   F.rho_n = float(g.D == 1 ? P.prim[0] * sqrt(lam / PI) : P.prim[0] * (lam / PI));
@@ -385,7 +389,10 @@ __device__ inline int update_group(const Geo& g, int i, int j) {
 // step! scalar part (src/Solver/step_2f.jl:6-64, :179-249): Shakhov factors of
 // the old state, w += flux divergence, prim, tau, residual terms.  One thread
 // per physical cell; each block writes its residual partials in a fixed order.
-template <int D>
+// FAST (the FP32 split form): tau, the density factors and the exponent
+// offsets of the coefficient blocks with FP32 transcendentals, conserve_prim
+// by reciprocals (see t_exp); w and prim stay FP64.
+template <int D, bool FAST>
 __global__ void __launch_bounds__(256) k_cell_param(DevState s, double dt) {
   const Geo& g = s.g;
   __shared__ double red[256][8];
@@ -405,7 +412,7 @@ __global__ void __launch_bounds__(256) k_cell_param(DevState s, double dt) {
     double* p = s.prim + (long)c * 4;
     constexpr int NW = D + 2;  // compile-time, so the small arrays stay in registers
     double lo = p[NW - 1];
-    P.o_rho_n = D == 1 ? p[0] * sqrt(lo / PI) : p[0] * (lo / PI);
+    P.o_rho_n = D == 1 ? p[0] * t_sqrt<FAST>(lo / PI) : p[0] * (lo / PI);
     P.oU = p[1];
     P.oV = D == 2 ? p[2] : 0.0;
     P.olam = lo;
@@ -431,7 +438,7 @@ __global__ void __launch_bounds__(256) k_cell_param(DevState s, double dt) {
         for (int k = 0; k < 4; ++k) w[k] += (fL[k] - fR[k] + fD[k] - fU[k]) / ds;
       }
       double pn[4];
-      conserve_prim(w, NW, g.gamma, pn);
+      conserve_prim<FAST>(w, NW, g.gamma, pn);
       for (int k = 0; k < NW; ++k) p[k] = pn[k];
       for (int k = 0; k < NW; ++k) {
         double dw = w[k] - wo[k];
@@ -439,8 +446,8 @@ __global__ void __launch_bounds__(256) k_cell_param(DevState s, double dt) {
         rr[4 + k] = fabs(w[k]);
       }
       double lam = pn[NW - 1];
-      double tau = vhs_time(pn[0], lam, g.mu_ref, g.omega);
-      P.rho_n = D == 1 ? pn[0] * sqrt(lam / PI) : pn[0] * (lam / PI);
+      double tau = vhs_time<FAST>(pn[0], lam, g.mu_ref, g.omega);
+      P.rho_n = D == 1 ? pn[0] * t_sqrt<FAST>(lam / PI) : pn[0] * (lam / PI);
       P.U = pn[1];
       P.V = D == 2 ? pn[2] : 0.0;
       P.lam = lam;
@@ -477,11 +484,11 @@ __global__ void __launch_bounds__(256) k_cell_param(DevState s, double dt) {
     float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     K.EM = K.EO = K.Q = K.TL = z;
     if (P.upd) {
-      K.EM = maxwell_exp2(P.rho_n, P.U, P.V, P.lam);
+      K.EM = maxwell_exp2<FAST>(P.rho_n, P.U, P.V, P.lam);
       double ds = D == 1 ? g.dx : g.dx * g.dy;
       K.A = make_float4(float(P.cB), float(P.dtau), float(P.inv), float(1.0 / ds));
       if (P.coll == COLL_SHAKHOV) {
-        K.EO = maxwell_exp2(P.o_rho_n, P.oU, P.oV, P.olam);
+        K.EO = maxwell_exp2<FAST>(P.o_rho_n, P.oU, P.oV, P.olam);
         double s0 = P.sfac * P.q0, s1 = P.sfac * P.q1;
         K.Q = make_float4(float(-(s0 * P.oU + s1 * P.oV)), float(s0), float(s1), float(P.ocB));
         double l2 = 2.0 * P.olam;
@@ -871,8 +878,14 @@ int launch_evolve(DevState& s, double dt, cudaStream_t st) {
 }
 
 int launch_cell_param(DevState& s, double dt, cudaStream_t st) {
-  if (s.g.D == 1) k_cell_param<1><<<s.res_blocks, 256, 0, st>>>(s, dt);
-  else k_cell_param<2><<<s.res_blocks, 256, 0, st>>>(s, dt);
+  const bool fast = s.prec != 0;
+  if (s.g.D == 1) {
+    if (fast) k_cell_param<1, true><<<s.res_blocks, 256, 0, st>>>(s, dt);
+    else k_cell_param<1, false><<<s.res_blocks, 256, 0, st>>>(s, dt);
+  } else {
+    if (fast) k_cell_param<2, true><<<s.res_blocks, 256, 0, st>>>(s, dt);
+    else k_cell_param<2, false><<<s.res_blocks, 256, 0, st>>>(s, dt);
+  }
   return 1;
 }
 
