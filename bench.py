@@ -239,6 +239,58 @@ def run_reference(args):
     return 0
 
 
+ERROR_CASES = (
+    ("sod 1D2F1V 200 cells x 101 velocities, KFVS + Shakhov, Kn=1e-4, to t=0.2",
+     dict(matter="gas", case="sod", space="1d2f1v", flux="kfvs", collision="shakhov", nSpecies=1,
+          interpOrder=2, limiter="vanleer", boundary="fix", cfl=0.5, maxTime=0.2, x0=0.0,
+          x1=1.0, nx=200, nxg=0, umin=-5.0, umax=5.0, nu=101, vMeshType="newton",
+          knudsen=1e-4, mach=0.0, prandtl=2.0 / 3.0, inK=2.0, omega=0.81, alphaRef=1.0,
+          omegaRef=0.5), None),
+    ("cavity 2D2F2V 64^2 cells x 28^2 velocities, KCU + Shakhov, Kn=0.075, Maxwell walls, "
+     "lid 0.15, 2000 steps",
+     dict(matter="gas", case="cavity", space="2d2f2v", flux="kcu", collision="shakhov",
+          nSpecies=1, interpOrder=2, limiter="vanleer", boundary="maxwell", cfl=0.8,
+          maxTime=1.0, x0=0.0, x1=1.0, nx=64, nxg=0, y0=0.0, y1=1.0, ny=64, nyg=0, umin=-5.0,
+          umax=5.0, nu=28, vmin=-5.0, vmax=5.0, nv=28, vMeshType="newton", knudsen=0.075,
+          mach=0.0, prandtl=2.0 / 3.0, inK=1.0, omega=0.72, alphaRef=1.0, omegaRef=0.5,
+          uLid=0.15, vLid=0.0, tLid=1.0), 2000),
+    ("four-quadrant 2D2F2V 128^2 cells x 64^2 velocities, UGKS + BGK, Kn=1e-3, 40 steps",
+     "quadrant128", 40),
+)
+
+
+def error_table(args):
+    """L-inf of the FP32-split form against the plain FP64 GPU path after the
+    same steps: rho, U, T (prim_errors) and q relative to max |q|."""
+    import kitgpu
+    rows = []
+    for name, cfg, nsteps in ERROR_CASES:
+        if cfg == "quadrant128":
+            cfg = quadrant_cfg(**dict(WORKLOAD, nx=128, ny=128))
+        KS = kitgpu.solver_set(cfg)
+        outs = {}
+        for prec in ("fp32", "fp64"):
+            ctr = kitgpu.init_fvm(KS, prec)[0]
+            dt = kitgpu.timestep(KS, ctr, 0.0)
+            n = nsteps or int(np.floor(KS.set.maxTime / dt)) + 1
+            kitgpu.step(KS, ctr, dt, n)
+            outs[prec] = ctr.handle.download()
+            ctr.handle.close()
+        vs = KS.vs
+        u, v, wt = ((vs.u, None, vs.weights) if KS.dim == 1
+                    else (vs.flat(vs.u), vs.flat(vs.v), vs.flat(vs.weights)))
+        e = prim_errors(outs["fp32"]["prim"], outs["fp64"]["prim"])
+        qa, qb = heat_flux(outs["fp32"], u, v, wt), heat_flux(outs["fp64"], u, v, wt)
+        eq = float(np.max(np.abs(qa - qb)) / max(np.max(np.abs(qb)), 1e-300))
+        wa, wb = outs["fp32"]["w"], outs["fp64"]["w"]
+        rows.append({"case": name, "steps": n, "rho": e[0], "U": e[1], "T": e[2],
+                     "q_rel_to_max": eq,
+                     "mass_fp32_vs_fp64": float(abs(wa[:, 0].sum() - wb[:, 0].sum())
+                                                / wb[:, 0].sum())})
+    return {"reference": "plain FP64 GPU path (held to the FP64 oracle within 1e-12 by the "
+                         "parity tests)", "cases": rows}
+
+
 def run_ours(args):
     import torch
     ws, rank, local, pg = dist_setup(args)
@@ -369,43 +421,12 @@ def run_ours(args):
                              "frac": 32.0 * cv / (u64 / 1e3) / 1e9 / peak},
                 "stage_ms": {k: v[0] / max(v[1], 1) for k, v in t64.items()}}
 
-    # L-inf error of the FP32-split form against the FP64 path (pinned to the
-    # oracle at 1e-12 by the parity tests) on a 128x128-cell sub-case
+    # L-inf error of the FP32-split form against the plain FP64 GPU path (which
+    # the parity tests hold to the FP64 oracle within 1e-12) on the small
+    # configurations at full size and on the headline physics at 128^2 cells
     err = None
-    if not args.no_error:
-        wl2 = dict(WORKLOAD, nx=128, ny=128)
-        KS2 = kitgpu.solver_set(quadrant_cfg(**wl2))
-        outs = {}
-        for prec in ("fp32", "fp64"):
-            hh = kitgpu.Handle(kitgpu.kb_config(KS2, prec), KS2.vs.flat(KS2.vs.u),
-                               KS2.vs.flat(KS2.vs.v), KS2.vs.flat(KS2.vs.weights))
-            w2, p2, h2, b2 = quadrant_state(KS2)
-            hh.upload(w2, p2, h2, b2)
-            dt2 = hh.timestep(KS2.set.cfl, 0.0, 1.0)
-            hh.step(dt2, args.err_steps)
-            outs[prec] = hh.download()
-            hh.close()
-        pa, pb = outs["fp32"]["prim"], outs["fp64"]["prim"]
-        e_rho = float(np.max(np.abs(pa[:, 0] - pb[:, 0]) / pb[:, 0]))
-        e_u = float(np.max(np.abs(pa[:, 1:3] - pb[:, 1:3]) * np.sqrt(pb[:, 3:4])))
-        e_t = float(np.max(np.abs(1 / pa[:, 3] - 1 / pb[:, 3]) * pb[:, 3]))
-        # heat flux from the distributions (theory_moments.jl:567-578)
-        def qflux(o):
-            u, v, wq = KS2.vs.flat(KS2.vs.u), KS2.vs.flat(KS2.vs.v), KS2.vs.flat(KS2.vs.weights)
-            P = o["prim"]
-            cu = u[None, :] - P[:, 1:2]
-            cvv = v[None, :] - P[:, 2:3]
-            c2 = cu * cu + cvv * cvv
-            q1 = 0.5 * ((wq * cu * c2 * o["h"]).sum(1) + (wq * cu * o["b"]).sum(1))
-            q2 = 0.5 * ((wq * cvv * c2 * o["h"]).sum(1) + (wq * cvv * o["b"]).sum(1))
-            return np.stack([q1, q2], 1)
-        qa, qb = qflux(outs["fp32"]), qflux(outs["fp64"])
-        e_q = float(np.max(np.abs(qa - qb)) / max(np.max(np.abs(qb)), 1e-300))
-        wa, wb = outs["fp32"]["w"], outs["fp64"]["w"]
-        err = {"case": "128x128 cells x 64x64 velocities, %d steps" % args.err_steps,
-               "rho": e_rho, "U": e_u, "T": e_t, "q_rel_to_max": e_q,
-               "mass_drift_fp32": float(abs(wa[:, 0].sum() - wb[:, 0].sum()) / wb[:, 0].sum()),
-               "reference": "FP64 GPU path (equal to the FP64 oracle within 1e-12 in tests)"}
+    if not args.no_error and rank == 0:
+        err = error_table(args)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -415,6 +436,11 @@ def run_ours(args):
 
     if rank != 0:
         return 0
+    blocks = {}
+    if not args.no_batch:
+        blocks["batch"] = batch_block(args, peak)
+    if not args.no_serve:
+        blocks["serve"] = serve_block(args)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -446,24 +472,51 @@ def run_ours(args):
         "linf_error_vs_fp64": err,
         "cpu_baseline": cpu,
     }
+    line.update(blocks)
     print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()
     return 0
 
 
-def run_batch(args):
-    """Batched shock-structure ensemble: 512 instances, FP32 split, one
-    persistent launch per step (CUDA graph), against the plain FP64 GPU path
-    looped per instance."""
+def prim_errors(pa, pb):
+    """L-inf of rho (relative), U (against the thermal speed sqrt(1/lambda)) and
+    T = 1/(2 lambda) (relative) of prim pa against pb ([..., dim+2])."""
+    pa, pb = np.asarray(pa), np.asarray(pb)
+    nw = pa.shape[-1]
+    e_rho = float(np.max(np.abs(pa[..., 0] - pb[..., 0]) / pb[..., 0]))
+    e_u = float(np.max(np.abs(pa[..., 1:nw - 1] - pb[..., 1:nw - 1]) * np.sqrt(pb[..., -1:])))
+    e_t = float(np.max(np.abs(1 / pa[..., -1] - 1 / pb[..., -1]) * pb[..., -1]))
+    return e_rho, e_u, e_t
+
+
+def heat_flux(st, u, v, wt):
+    """q per cell from h, b (heat_flux 2F1V / 2F2V, src/Theory/theory_moments.jl:530-531,
+    :567-578); st holds prim [ncell, nw], h, b [ncell, nvel]."""
+    P = st["prim"]
+    cu = u[None, :] - P[:, 1:2]
+    if v is None:
+        return (0.5 * ((wt * cu ** 3 * st["h"]).sum(1) + (wt * cu * st["b"]).sum(1)))[:, None]
+    cvv = v[None, :] - P[:, 2:3]
+    c2 = cu * cu + cvv * cvv
+    q1 = 0.5 * ((wt * cu * c2 * st["h"]).sum(1) + (wt * cu * st["b"]).sum(1))
+    q2 = 0.5 * ((wt * cvv * c2 * st["h"]).sum(1) + (wt * cvv * st["b"]).sum(1))
+    return np.stack([q1, q2], 1)
+
+
+def batch_block(args, peak):
+    """Batched shock-structure ensemble (512 instances): FP32-split batch step
+    (fused launch per step, CUDA graph), its roofline fraction, the run to the
+    1e-8 steady residual, L-inf against the FP64 batch after the same steps,
+    and the plain FP64 GPU path looped per instance."""
     import torch
     import kitgpu
     from kitgpu import batch as KB
-    torch.cuda.set_device(0)
-    kitgpu.load()
     sets = KB.solver_sets(KB.shock_ensemble(args.instances))
     out = {"workload": "batched ensemble of %d 1D shock-structure solves (Mach U(1.2,8), cells "
-                       "U{50..400}, velocities U{48..200}), KFVS + Shakhov, Kn=1" % len(sets)}
+                       "U{50..400}, velocities U{48..200} on +-(5+2Ma)), KFVS + Shakhov, Kn=1, "
+                       "upstream rho=1, lambda=0.5" % len(sets)}
+    states = {}
     for prec in ("fp32", "fp64"):
         bt = KB.Batch(sets, prec)
         bt.upload_initial()
@@ -472,21 +525,44 @@ def run_batch(args):
         cv = bt.cell_velocity_points()
         # an FP32 batch step is ~0.2 ms: time at least 500 of them so the
         # host's launch and synchronisation cost is amortised
-        nst = max(args.steps, 500) if prec == "fp32" else args.steps
+        nst = max(args.steps, 500) if prec == "fp32" else max(args.steps, 50)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         bt.step(nst)
         el = time.perf_counter() - t0
-        out[prec] = {"value": cv * nst / el, "unit": UNIT, "ms_per_step": 1e3 * el / nst,
-                     "steps": nst}
+        val = cv * nst / el
+        esz = 16.0 if prec == "fp32" else 32.0
+        out[prec] = {"value": val, "unit": UNIT, "ms_per_step": 1e3 * el / nst, "steps": nst,
+                     "cell_velocity_per_step": cv,
+                     "roofline": {"bound": "hbm", "achieved": val * esz / 1e9, "peak": peak,
+                                  "unit": "GB/s", "frac": val * esz / 1e9 / peak,
+                                  "bytes_per_cv": esz}}
+        # same number of steps from the initial state in both forms
+        bt.upload_initial()
+        bt.timestep()
+        bt.step(args.batch_err_steps)
+        states[prec] = bt.download()
         if prec == "fp32":
             bt.upload_initial()
             bt.timestep()
             t0 = time.perf_counter()
             left = bt.run_to_steady(tol=1e-8, max_steps=args.max_steady, chunk=500)
-            out["fp32"]["steady"] = {"tol": 1e-8, "steps": bt.steps, "seconds": time.perf_counter() - t0,
-                                     "unconverged": left}
+            out["fp32"]["steady"] = {"tol": 1e-8, "steps": bt.steps,
+                                     "seconds": time.perf_counter() - t0,
+                                     "unconverged": left, "instances": bt.n}
+            tun = getattr(bt, "tuning", None)
+            if tun:
+                out["fp32"]["tuning"] = tun
         bt.close()
+    er = np.zeros(4)
+    for K, a, b in zip(sets, states["fp32"], states["fp64"]):
+        e = prim_errors(a["prim"], b["prim"])
+        qa = heat_flux(a, K.vs.u, None, K.vs.weights)
+        qb = heat_flux(b, K.vs.u, None, K.vs.weights)
+        eq = float(np.max(np.abs(qa - qb)) / max(np.max(np.abs(qb)), 1e-300))
+        er = np.maximum(er, list(e) + [eq])
+    out["linf_fp32_vs_fp64"] = {"steps": args.batch_err_steps, "rho": er[0], "U": er[1],
+                                "T": er[2], "q_rel_to_max": er[3], "instances": len(sets)}
     # plain FP64 GPU path, one handle per instance, looped
     sample = sets[:: max(1, len(sets) // args.loop_sample)][: args.loop_sample]
     hs = []
@@ -499,33 +575,58 @@ def run_batch(args):
     for h, dt, _ in hs:
         h.step(dt, args.loop_steps)
     el = time.perf_counter() - t0
+    for h, _, _ in hs:
+        h.close()
     out["fp64_loop"] = {"value": sum(c for _, _, c in hs) * args.loop_steps / el, "unit": UNIT,
                         "instances_sampled": len(hs)}
     out["speedup_fp32_batch_vs_fp64_loop"] = out["fp32"]["value"] / out["fp64_loop"]["value"]
+    return out
+
+
+def run_batch(args):
+    import torch
+    import kitgpu
+    torch.cuda.set_device(0)
+    kitgpu.load()
+    out = batch_block(args, measured_peaks()[0])
     print(json.dumps({"metric": METRIC, "workload": "batch", "result": out}), flush=True)
     return 0
 
 
-def run_serve(args):
-    """Served mixed stream (Poisson arrivals), FP32 split vs plain FP64."""
-    import torch
-    import kitgpu
+def serve_block(args):
+    """Served mixed stream (Poisson arrivals): the FP32-split server at each
+    offered rate with a realistic step cap, and the plain FP64 server against
+    the FP32 one on one shorter stream (the FP64 form is ~100x slower)."""
     from kitgpu import serve as S
-    torch.cuda.set_device(0)
-    kitgpu.load()
-    res = {}
-    for prec in ("fp32", "fp64"):
-        reqs = S.mixed_stream(rate=args.rate, duration=args.duration, seed=20261203,
+    mix = ("60% 1D Sod (cells 64..2048, velocities 32..256), 40% 2D cavity (16^2..128^2 cells, "
+           "16^2..48^2 velocities, Kn 1e-4..1)")
+    out = {"stream": {"mix": mix, "tol": 1e-6, "max_steps": args.max_steps,
+                      "duration_s": args.duration}, "fp32": {}}
+    for rate in args.rates:
+        reqs = S.mixed_stream(rate=rate, duration=args.duration, seed=20261203,
                               max_steps=args.max_steps, tol=1e-6)
+        srv = S.Server(precision="fp32", hbm_budget=args.hbm_gb << 30, max_slots=args.slots,
+                       chunk=args.chunk)
+        out["fp32"]["rate_%g" % rate] = srv.run(reqs)
+    cmp_ = {"rate_per_s": 50.0, "duration_s": args.cmp_duration, "max_steps": args.cmp_steps}
+    for prec in ("fp32", "fp64"):
+        reqs = S.mixed_stream(rate=50.0, duration=args.cmp_duration, seed=20261203,
+                              max_steps=args.cmp_steps, tol=1e-6)
         srv = S.Server(precision=prec, hbm_budget=args.hbm_gb << 30, max_slots=args.slots,
                        chunk=args.chunk)
-        res[prec] = srv.run(reqs)
-    res["throughput_ratio_fp32_vs_fp64"] = res["fp32"]["throughput"] / res["fp64"]["throughput"]
+        cmp_[prec] = srv.run(reqs)
+    cmp_["throughput_ratio_fp32_vs_fp64"] = cmp_["fp32"]["throughput"] / cmp_["fp64"]["throughput"]
+    out["same_stream_fp32_vs_fp64"] = cmp_
+    return out
+
+
+def run_serve(args):
+    import torch
+    import kitgpu
+    torch.cuda.set_device(0)
+    kitgpu.load()
+    res = serve_block(args)
     print(json.dumps({"metric": METRIC + " and p50/p99 latency", "workload": "serve",
-                      "stream": {"rate_per_s": args.rate, "duration_s": args.duration,
-                                 "mix": "60% 1D Sod (cells 64..2048, velocities 32..256), 40% 2D "
-                                        "cavity (16^2..128^2 cells, 16^2..48^2 velocities, "
-                                        "Kn 1e-4..1)", "max_steps": args.max_steps, "tol": 1e-6},
                       "result": res}), flush=True)
     return 0
 
@@ -547,9 +648,14 @@ def main():
     ap.add_argument("--max-steady", type=int, default=40000)
     ap.add_argument("--loop-sample", type=int, default=64)
     ap.add_argument("--loop-steps", type=int, default=20)
-    ap.add_argument("--rate", type=float, default=50.0)
-    ap.add_argument("--duration", type=float, default=4.0)
-    ap.add_argument("--max-steps", type=int, default=200)
+    ap.add_argument("--batch-err-steps", type=int, default=200)
+    ap.add_argument("--rates", type=float, nargs="+", default=[20.0, 50.0, 200.0])
+    ap.add_argument("--duration", type=float, default=2.0)
+    ap.add_argument("--max-steps", type=int, default=2000)
+    ap.add_argument("--cmp-duration", type=float, default=1.0)
+    ap.add_argument("--cmp-steps", type=int, default=100)
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--slots", type=int, default=64)
     ap.add_argument("--chunk", type=int, default=20)
     ap.add_argument("--hbm-gb", type=int, default=64)

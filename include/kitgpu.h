@@ -143,7 +143,10 @@ int kb_timestep(kb_handle_t* h, double cfl, double sim_time, double max_time,
  * KB_NOALLOC_MAX_CELLS physical cells are rejected with KB_ERR_ARG.  Every
  * call reuses that array: calls that overlap on the GPU race.  The first call
  * on a device looks up the array's device address; make that first call
- * before any stream capture. */
+ * before any stream capture.  That address is kept for the life of the
+ * process: do not use this call again after a reset of its device
+ * (cudaDeviceReset, CUDA.jl device_reset!).  A CUDA error already pending on
+ * the calling thread is reported as KB_ERR_CUDA and left in place. */
 #define KB_NOALLOC_MAX_CELLS 2097152
 int kb_timestep_noalloc(const kb_config_t* cfg, const double* d_prim, double* d_tmax,
                         void* stream);
@@ -188,6 +191,13 @@ int kb_download_faces(kb_handle_t* h, double dt, double* fw, double* fh, double*
  * would store them (ctr.sw / ctr.sh / ctr.sb; 2D slopes use the last index
  * for the direction, src/Data/data_array.jl:15-50).  Any pointer may be NULL. */
 int kb_download_slopes(kb_handle_t* h, double* sw, double* sh, double* sb);
+
+/* Restore the w slopes sw [ncell][dim][dim+2] (layout of kb_download_slopes),
+ * e.g. from a checkpoint.  reconstruct! recomputes them for the cells it
+ * updates; ghost cells keep the slopes bc_extra! copied into them the step
+ * before (src/Boundary/bc_extra.jl:10-50), which is state a restart needs
+ * (ctr.sw of ControlVolume2F, src/Struct/struct_ctr.jl:94-117). */
+int kb_upload_slopes(kb_handle_t* h, const double* sw);
 
 /* Status word of the handle: KB_OK, KB_ERR_NUMERIC once a step produced a
  * non-finite or non-positive density / lambda, or KB_ERR_TIMEOUT once a

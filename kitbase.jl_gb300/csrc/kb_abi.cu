@@ -788,6 +788,18 @@ int kb_download_faces(kb_handle_t* h, double dt, double* fw, double* fh, double*
   return KB_OK;
 }
 
+int kb_upload_slopes(kb_handle_t* h, const double* sw) {
+  if (!h || !sw) return fail(KB_ERR_ARG, "kb_upload_slopes: null argument");
+  const Geo& g = h->s.g;
+  KB_TRY(sync(h));
+  std::vector<double> s8((size_t)h->ncell * 8, 0.0);
+  for (long c = 0; c < h->ncell; ++c)
+    for (int d = 0; d < g.D; ++d)
+      for (int k = 0; k < g.NW; ++k) s8[(size_t)c * 8 + d * 4 + k] = sw[((size_t)c * g.D + d) * g.NW + k];
+  KB_CUDA(cudaMemcpy(h->s.sw, s8.data(), sizeof(double) * s8.size(), cudaMemcpyHostToDevice));
+  return KB_OK;
+}
+
 int kb_download_slopes(kb_handle_t* h, double* sw, double* sh, double* sb) {
   if (!h) return fail(KB_ERR_ARG, "kb_download_slopes: null handle");
   const Geo& g = h->s.g;

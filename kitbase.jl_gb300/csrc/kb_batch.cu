@@ -1033,6 +1033,13 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb::k_batch_step<float, 256>, 256, 0);
   B->grid = std::min(n, std::max(1, sms * per));
+  // the segment kernel's dynamic shared memory limit, raised on this device
+  // once per batch here rather than at launch (launches may sit inside a
+  // stream capture, and batches may be driven from several host threads)
+  if (B->prec == KB_PREC_FP32 &&
+      cudaFuncSetAttribute(kb::k_batch_seg, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kb::SEG_SMEM_MAX) != cudaSuccess)
+    return fail_out(bfail(KB_ERR_CUDA, "kb_batch_create: shared-memory attribute refused"));
   *out = B;
   return KB_OK;
 }
@@ -1141,14 +1148,6 @@ static int batch_kernels_per_step(const kb_batch* B) { return B->prec == KB_PREC
 
 static void batch_launch(kb_batch* B, int cur) {
   if (B->prec == KB_PREC_FP32) {  // fused segments (one pass over HBM)
-    static bool raised[64] = {false};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && !raised[dev]) {
-      cudaFuncSetAttribute(kb::k_batch_seg, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kb::SEG_SMEM_MAX);
-      raised[dev] = true;
-    }
     const int smem = kb::seg_smem(B->d.sst_max, B->d.nu4_max);
     kb::k_batch_seg<<<(unsigned)B->nseg, kb::SEG_T, smem, B->stream>>>(
         B->d, (const float*)B->h[cur], (const float*)B->bq[cur], (float*)B->h[cur ^ 1],

@@ -299,50 +299,47 @@ __global__ void __launch_bounds__(256) k_wall(DevState s, double dt) {
   const R* W = vtab<R>(s, 2);
   long vs = g.vstride;
   R Uw = R(bw[1]), Vw = R(bw[2]), Lw = R(lw);
-  Acc<R> sf, sg;
+  // One pass: the outgoing half from the interior cell's h, b; the incoming
+  // half as moments of the unit-density wall Maxwellian, scaled by the wall
+  // density afterwards in FP64.  The mass flux S0 = SF + rho_n * I0 then
+  // cancels to FP64 round-off by construction (the density is chosen so that
+  // no mass crosses the wall), also when h is stored in FP32.
+  Acc<R> o0, o1, o2, o3, i0, i1, i2, i3;
   for (int v = lane; v < g.nvel; v += 32) {
     R un, ut;
     if (D == 1) { un = U[v]; ut = R(0); }
     else if (r.d == 0) { un = U[v]; ut = V[v]; }
     else { un = V[v]; ut = -U[v]; }
-    bool in = un * R(rot) >= R(0);
-    R du = un - Uw, e = du * du;
-    if (D == 2) { R dv = ut - Vw; e += dv * dv; }
-    if (in) sg.add(W[v] * un * mexp(-Lw * e));
-    else sf.add(W[v] * un * H[(long)c * vs + v]);
-  }
-  double SF = sf.total(), SG = sg.total();
-  SG *= D == 1 ? sqrt(lw / PI) : (lw / PI);
-  double rho = -SF / SG;
-  double len = D == 2 ? (r.d == 0 ? g.dy : g.dx) : 1.0;
-  double sc = D == 2 ? len * dt : dt;
-  R rn = R(D == 1 ? rho * sqrt(lw / PI) : rho * (lw / PI));
-  R cB = R(g.K / (2.0 * lw));
-  Acc<R> a0, a1, a2, a3;
-  for (int v = lane; v < g.nvel; v += 32) {
-    R un, ut;
-    if (D == 1) { un = U[v]; ut = R(0); }
-    else if (r.d == 0) { un = U[v]; ut = V[v]; }
-    else { un = V[v]; ut = -U[v]; }
-    bool in = un * R(rot) >= R(0);
-    R hw, bwv;
+    const bool in = un * R(rot) >= R(0);
+    R c2 = un * un;
+    if (D == 2) c2 += ut * ut;
     if (in) {
       R du = un - Uw, e = du * du;
       if (D == 2) { R dv = ut - Vw; e += dv * dv; }
-      hw = rn * mexp(-Lw * e);
-      bwv = hw * cB;
+      const R t = W[v] * un * mexp(-Lw * e);
+      i0.add(t);
+      i1.add(t * un);
+      if (D == 2) i2.add(t * ut);
+      i3.add(t * c2);
     } else {
-      hw = H[(long)c * vs + v];
-      bwv = Bq[(long)c * vs + v];
+      const R t = W[v] * un * H[(long)c * vs + v];
+      o0.add(t);
+      o1.add(t * un);
+      if (D == 2) o2.add(t * ut);
+      o3.add(t * c2 + W[v] * un * Bq[(long)c * vs + v]);
     }
-    R t = W[v] * un * hw;
-    a0.add(t);
-    a1.add(t * un);
-    R c2 = un * un;
-    if (D == 2) { a2.add(t * ut); c2 += ut * ut; }
-    a3.add(t * c2 + W[v] * un * bwv);
   }
-  double S0 = a0.total(), S1 = a1.total(), S2 = D == 2 ? a2.total() : 0.0, S3 = a3.total();
+  const double norm = D == 1 ? sqrt(lw / PI) : (lw / PI);
+  const double SF = o0.total(), I0 = i0.total();
+  const double rho = -SF / (I0 * norm);
+  const double rn = rho * norm;  // wall density times the Maxwellian's normalisation
+  const double cBw = g.K / (2.0 * lw);
+  double len = D == 2 ? (r.d == 0 ? g.dy : g.dx) : 1.0;
+  double sc = D == 2 ? len * dt : dt;
+  const double S0 = SF + rn * I0;
+  const double S1 = o1.total() + rn * i1.total();
+  const double S2 = D == 2 ? o2.total() + rn * i2.total() : 0.0;
+  const double S3 = o3.total() + rn * (i3.total() + cBw * I0);
   if (lane == 0) {
     s.rhow[f] = rho;
     FaceCoef32 wc;

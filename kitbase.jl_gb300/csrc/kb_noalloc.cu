@@ -28,6 +28,11 @@ constexpr int NA_MAX_DEVICES = 64;
 // start at zero; calls that overlap on the GPU share it and race.
 static __device__ __align__(256) double g_na_partial[NA_MAX_BLOCKS];
 
+// Device address of g_na_partial per device, looked up by the first call on
+// that device.  A device reset (cudaDeviceReset, or a Julia session's
+// device_reset!) unloads the module and releases the array, so the cached
+// address is stale afterwards: the entry point must not be used again in a
+// process after a reset of its device.
 double* g_na_addr[NA_MAX_DEVICES] = {nullptr};
 std::mutex g_na_mutex;
 
@@ -96,6 +101,16 @@ extern "C" int kb_timestep_noalloc(const kb_config_t* cfg, const double* d_prim,
                                    " physical cells exceed the fixed scratch limit of " +
                                    std::to_string((long)KB_NOALLOC_MAX_CELLS) +
                                    " (KB_NOALLOC_MAX_CELLS); use kb_timestep");
+  // An error already pending on this thread belongs to the caller's earlier
+  // work: report it without taking it (it stays for the caller to read), so
+  // that it is neither lost nor mistaken for a failure of these launches.
+  {
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess)
+      return na_fail(KB_ERR_CUDA, std::string("kb_timestep_noalloc: an earlier CUDA error is "
+                                              "pending on this thread (left in place): ") +
+                                      cudaGetErrorString(pending));
+  }
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) {
     cudaGetLastError();
@@ -122,9 +137,14 @@ extern "C" int kb_timestep_noalloc(const kb_config_t* cfg, const double* d_prim,
   cudaStream_t st = (cudaStream_t)stream;
   k_na_partial<<<nblocks, NA_THREADS, 0, st>>>(d_prim, part, cfg->dim, cfg->nx, ny, cfg->ngx, ngy,
                                                dx, dy, cfg->umax, cfg->vmax, cfg->gamma);
-  k_na_final<<<1, NA_THREADS, 0, st>>>(part, nblocks, d_tmax);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
-    return na_fail(KB_ERR_CUDA, std::string("kb_timestep_noalloc: launch: ") + cudaGetErrorString(e));
+    return na_fail(KB_ERR_CUDA, std::string("kb_timestep_noalloc: launch of the per-block "
+                                            "partial maxima: ") + cudaGetErrorString(e));
+  k_na_final<<<1, NA_THREADS, 0, st>>>(part, nblocks, d_tmax);
+  e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return na_fail(KB_ERR_CUDA, std::string("kb_timestep_noalloc: launch of the final maximum: ") +
+                                    cudaGetErrorString(e));
   return KB_OK;
 }

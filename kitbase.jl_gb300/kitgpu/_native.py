@@ -68,6 +68,7 @@ SIGNATURES = {
     "kb_step": [_H, ctypes.c_double, ctypes.c_int32, _D],
     "kb_download_faces": [_H, ctypes.c_double, _D, _D, _D],
     "kb_download_slopes": [_H, _D, _D, _D],
+    "kb_upload_slopes": [_H, _D],
     "kb_status": [_H],
     "kb_device_bytes": [_H, ctypes.POINTER(ctypes.c_int64)],
     "kb_launch_count": [_H, ctypes.POINTER(ctypes.c_int64)],

@@ -404,6 +404,8 @@ class SolverSet:
     vs: object
     gas: Gas
     ib: IB
+    config: dict = None  # the key/value configuration the set was built from
+    ib_kw: dict = None   # keyword overrides of the initial-condition preset
 
     @property
     def dim(self):
@@ -445,4 +447,4 @@ def solver_set(config, **ib_kw):
     if s.case == "cavity" and "uLid" in D:
         kw.update(Um=D["uLid"], Vm=D["vLid"], Tm=D["tLid"])
     ib = config_ib(s, ps, vs, gas, **kw)
-    return SolverSet(s, ps, vs, gas, ib)
+    return SolverSet(s, ps, vs, gas, ib, D, dict(ib_kw))

@@ -9,6 +9,7 @@ the cells and faces live in HBM behind a libkitgpu handle; `Cells` and
 reference's names (without the `!`), argument order and keyword meaning.
 """
 import ctypes
+import json
 import math
 from collections import namedtuple
 
@@ -151,6 +152,13 @@ class Handle:
         fb = np.zeros_like(fh)
         self.call("kb_download_faces", float(dt), N.ptr(fw), N.ptr(fh), N.ptr(fb))
         return fw, fh, fb
+
+    def upload_slopes(self, sw):
+        """w slopes [ncell, dim, dim+2] (ctr.sw), e.g. from a checkpoint."""
+        sw = np.ascontiguousarray(sw, dtype=np.float64)
+        if sw.shape != (self.ncell, self.dim, self.nw):
+            raise ValueError("sw has shape %s, expected %s" % (sw.shape, (self.ncell, self.dim, self.nw)))
+        self.call("kb_upload_slopes", N.ptr(sw))
 
     def slopes(self):
         sw = np.zeros((self.ncell, self.dim, self.nw))
@@ -326,10 +334,23 @@ def init_fvm(KS, precision="fp64"):
     return ctr, Faces(handle, 0), Faces(handle, 1)
 
 
-def initialize(config, precision="fp64", **ib_kw):
-    """initialize(config) (src/Solver/solver_init.jl:10-48): (KS, ctr, face..., t)."""
+def initialize(config, precision=None, **ib_kw):
+    """initialize(config) (src/Solver/solver_init.jl:10-48): (KS, ctr, face..., t).
+
+    `config` is a config file path, a dict, or a checkpoint written by
+    write_checkpoint (a path ending in ".npz"): like the reference's
+    initialize("*.jld2") (src/Solver/solver_init.jl:19-26) the solver set and
+    cells come from the file and the time is the checkpoint's.  `precision`
+    ("fp64" or "fp32") defaults to "fp64", or to the checkpoint's own."""
+    if isinstance(config, str) and config.endswith(".npz"):
+        d = np.load(config, allow_pickle=False)
+        meta = json.loads(str(d["set"]))
+        KS = solver_set(meta["config"], **meta.get("ib_kw", {}))
+        out = init_fvm(KS, precision or meta.get("precision", "fp64"))
+        t = read_checkpoint(d, out[0])
+        return (KS,) + out + (t,)
     KS = solver_set(config, **ib_kw)
-    return (KS,) + init_fvm(KS, precision) + (0.0,)
+    return (KS,) + init_fvm(KS, precision or "fp64") + (0.0,)
 
 
 def _check_mode(KS, name, given, expect):
@@ -411,14 +432,69 @@ def extract_sol(KS, ctr):
     return grid[c.ngy:c.ngy + c.ny, c.ngx:c.ngx + c.nx].transpose(1, 0, 2).copy()
 
 
-def write_checkpoint(path, KS, ctr, t):
-    """Checkpoint of the device state (the role of write_jld, src/IO/io_write.jl:34-40)."""
-    s = ctr.handle.download()
-    np.savez(path, t=t, **s)
+CKPT_VERSION = 1
+
+
+def _cell_shape(handle, KS):
+    """Per-cell shape of h / b in the checkpoint: (nu,) in 1D and (nv, nu) in
+    2D, i.e. a C-order array whose reversed axes are the reference's
+    column-major h[u, v] matrix of a ControlVolume2F."""
+    return (KS.vs.nu,) if KS.dim == 1 else (KS.vs.nv, KS.vs.nu)
+
+
+def write_checkpoint(path, KS, ctr, t, slopes=False, precision=None):
+    """Checkpoint of the device state (the role of write_jld, src/IO/io_write.jl:34-40,
+    which saves Dict("set" => KS, "ctr" => ctr, "t" => t)).
+
+    Keys: "t"; "set" (JSON: the configuration dict the SolverSet was built
+    from, its initial-condition keywords, the storage precision); and the
+    fields of the reference's ControlVolume2F cells (src/Struct/struct_ctr.jl:94-117)
+    as one array per field over all cells incl. ghosts, x fastest (the
+    column-major order of the OffsetArray ctr[i, j]): "ctr.w", "ctr.prim"
+    [ncell, dim+2], "ctr.h", "ctr.b" [ncell, (nv,) nu], "ctr.sw" [ncell, dim,
+    dim+2] (part of the state: ghost cells carry the w slopes bc_extra! copied
+    the step before); with slopes=True also "ctr.sh", "ctr.sb"
+    [ncell, dim, (nv,) nu] as reconstruct! would store them.  "cells" holds (nx + 2 ngx, ny + 2 ngy)
+    and "ghosts" (ngx, ngy): the OffsetArray axes 1-ng : n+ng."""
+    hd = ctr.handle
+    s = hd.download()
+    cs = _cell_shape(hd, KS)
+    c = hd.cfg
+    prec = precision or ("fp32" if c.precision == N.PRECISION["fp32"] else "fp64")
+    meta = dict(version=CKPT_VERSION, config=KS.config, ib_kw=KS.ib_kw or {}, precision=prec)
+    arrs = {"t": np.float64(t), "set": np.array(json.dumps(meta)),
+            "cells": np.array([hd.nxt, hd.nyt], dtype=np.int64),
+            "ghosts": np.array([c.ngx, c.ngy], dtype=np.int64),
+            "ctr.w": s["w"], "ctr.prim": s["prim"],
+            "ctr.h": s["h"].reshape((hd.ncell,) + cs), "ctr.b": s["b"].reshape((hd.ncell,) + cs)}
+    if slopes:
+        sw, sh, sb = hd.slopes()
+        arrs["ctr.sh"] = sh.reshape((hd.ncell, hd.dim) + cs)
+        arrs["ctr.sb"] = sb.reshape((hd.ncell, hd.dim) + cs)
+    else:
+        sw = np.zeros((hd.ncell, hd.dim, hd.nw))
+        N.check(hd.lib.kb_download_slopes(hd.h, N.ptr(sw), None, None))
+    # the w slopes are state: ghost cells keep the slopes bc_extra! copied
+    # into them the step before, and the face states read them
+    arrs["ctr.sw"] = sw
+    np.savez(path, **arrs)
 
 
 def read_checkpoint(path, ctr):
-    """Restore a checkpoint written by write_checkpoint; returns t."""
-    d = np.load(path)
-    ctr.handle.upload(d["w"], d["prim"], d["h"], d["b"])
+    """Restore the cells of a checkpoint written by write_checkpoint into an
+    existing solver of the same shape; returns t.  Raises ValueError when
+    the checkpoint's cells or velocity grid do not match the solver's."""
+    d = np.load(path, allow_pickle=False) if isinstance(path, str) else path
+    hd = ctr.handle
+    w, p = d["ctr.w"], d["ctr.prim"]
+    h = d["ctr.h"].reshape(len(d["ctr.h"]), -1)
+    b = d["ctr.b"].reshape(len(d["ctr.b"]), -1)
+    want = (hd.ncell, hd.nw, hd.nvel)
+    got = (w.shape[0], w.shape[1], h.shape[1])
+    if got != want or p.shape != w.shape or b.shape != h.shape or h.shape[0] != hd.ncell:
+        raise ValueError("checkpoint cells (ncell, nw, nvel) = %s do not match the solver's %s"
+                         % (got, want))
+    hd.upload(w, p, h, b)
+    if "ctr.sw" in d:
+        hd.upload_slopes(d["ctr.sw"])
     return float(d["t"])

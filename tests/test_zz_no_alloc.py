@@ -55,6 +55,37 @@ def test_noalloc_timestep_matches_kb_timestep_twice(gpu_lib):
     assert cfl / tmax3 == pytest.approx(dt3, rel=1e-14)
 
 
+def test_noalloc_allocates_no_device_memory(gpu_lib):
+    """After the first call (which loads the module and looks up the scratch
+    address), further calls on grids of any allowed size leave the device's
+    free memory unchanged."""
+    import torch
+    KS, ctr, a, b, t = kitgpu.initialize(quadrant(nx=40, ny=30, nu=4, nv=4))
+    hd = ctr.handle
+    prim = hd.download(("prim",))["prim"]
+    d_prim = torch.tensor(prim, dtype=torch.float64, device="cuda")
+    d_out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    big = torch.ones((1448 * 1448, 4), dtype=torch.float64, device="cuda")  # ~2.1M cells
+    lib = N.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    cfg_big = N.KbConfig()
+    ctypes.memmove(ctypes.byref(cfg_big), ctypes.byref(hd.cfg), ctypes.sizeof(cfg_big))
+    cfg_big.nx, cfg_big.ny, cfg_big.ngx, cfg_big.ngy = 1448, 1448, 0, 0
+    assert lib.kb_timestep_noalloc(ctypes.byref(hd.cfg), d_prim.data_ptr(), d_out.data_ptr(),
+                                   stream) == 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        assert lib.kb_timestep_noalloc(ctypes.byref(cfg_big), big.data_ptr(), d_out.data_ptr(),
+                                       stream) == 0
+        assert lib.kb_timestep_noalloc(ctypes.byref(hd.cfg), d_prim.data_ptr(), d_out.data_ptr(),
+                                       stream) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert KS.set.cfl / float(d_out.item()) == pytest.approx(
+        hd.timestep(KS.set.cfl, 0.0, 1e9), rel=1e-14)
+
+
 def test_noalloc_rejects_oversized_grid(gpu_lib):
     KS, ctr, a, b, t = kitgpu.initialize(quadrant(nx=8, ny=8, nu=4, nv=4))
     cfg = N.KbConfig()
