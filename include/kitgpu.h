@@ -77,6 +77,12 @@ typedef struct kb_config {
   double mu_ref;         /* reference viscosity (ref_vhs_vis) */
   double omega;          /* VHS viscosity index (gas.omega) */
   double Pr;             /* Prandtl number */
+  int32_t nf;            /* distributions per cell: 2 (or 0) for the 2F models 1D2F1V /
+                            2D2F2V (h, b); 1 for the 1F models 1D1F1V / 2D1F2V (f only,
+                            passed as h; b is absent: NULL on upload, zero on download).
+                            1F takes KFVS or KCU (src/Flux/flux_kfvs.jl:238-262, :615-650;
+                            src/Flux/flux_kcu.jl:241-303, :828-894; step!
+                            src/Solver/step_1f.jl) */
 } kb_config_t;
 
 typedef struct kb_handle kb_handle_t;

@@ -162,6 +162,17 @@ static int validate(const kb_config_t* c) {
   if (c->ngx < 0 || c->ngx > 2 || (c->dim == 2 && (c->ngy < 0 || c->ngy > 2)))
     return fail(KB_ERR_CONFIG, "ghost layers must be in [0, 2]");
   if (c->flux < 0 || c->flux > 2) return fail(KB_ERR_CONFIG, "unknown flux");
+  if (c->nf < 0 || c->nf > 2) return fail(KB_ERR_CONFIG, "nf must be 1 (1F) or 2 (2F)");
+  if (c->nf == 1 && c->flux == KB_FLUX_UGKS)
+    return fail(KB_ERR_CONFIG, "the 1F models take KFVS or KCU (the reference has no 1F UGKS step)");
+  if (c->nf == 1 && c->dim == 1 && (c->bc[0] == KB_BC_MAXWELL || c->bc[1] == KB_BC_MAXWELL))
+    return fail(KB_ERR_CONFIG,
+                "1D1F1V has no Maxwell wall in the reference (evolve_boundary! covers the 2F "
+                "cells only, src/Solver/evolve_boundary.jl:4-47)");
+  if (c->nf == 1 && c->dim == 2 && c->collision == KB_COLL_SHAKHOV)
+    return fail(KB_ERR_CONFIG,
+                "2D1F2V runs BGK only: the reference's Shakhov branch of its step! reads an "
+                "undefined b (src/Solver/step_1f.jl:194)");
   if (c->collision < 0 || c->collision > 1) return fail(KB_ERR_CONFIG, "unknown collision");
   if (c->interp_order != 1 && c->interp_order != 2)
     return fail(KB_ERR_CONFIG, "interp_order must be 1 or 2");
@@ -228,6 +239,8 @@ int kb_create(const kb_config_t* cfg, const double* u, const double* v, const do
   g.x0 = c.x0;
   g.y0 = c.dim == 2 ? c.y0 : 0.0;
   g.K = c.K;
+  g.nf = c.nf == 1 ? 1 : 2;
+  g.Kb = g.nf == 1 ? 0.0 : c.K;
   g.gamma = c.gamma;
   g.mu_ref = c.mu_ref;
   g.omega = c.omega;
@@ -428,7 +441,8 @@ static int dist_out(kb_handle* h, double* dst, const void* src) {
 
 int kb_upload_state(kb_handle_t* h, const double* w, const double* prim, const double* hdist,
                     const double* bdist) {
-  if (!h || !w || !prim || !hdist || !bdist) return fail(KB_ERR_ARG, "kb_upload_state: null argument");
+  if (!h || !w || !prim || !hdist || (!bdist && h->s.g.nf != 1))
+    return fail(KB_ERR_ARG, "kb_upload_state: null argument");
   int NW = h->s.g.NW;
   std::vector<double> w4((size_t)h->ncell * 4, 0.0), p4((size_t)h->ncell * 4, 0.0);
   for (long c = 0; c < h->ncell; ++c)
@@ -442,7 +456,12 @@ int kb_upload_state(kb_handle_t* h, const double* w, const double* prim, const d
   KB_CUDA(cudaMemsetAsync(h->s.status, 0, sizeof(int), h->stream));
   h->s.cur = 0;
   KB_TRY(dist_in(h, h->s.h[0], hdist));
-  KB_TRY(dist_in(h, h->s.b[0], bdist));
+  if (bdist) {
+    KB_TRY(dist_in(h, h->s.b[0], bdist));
+  } else {  // 1F: no second distribution
+    KB_CUDA(cudaMemsetAsync(h->s.b[0], 0, (size_t)h->ncell * h->vstride * (h->s.prec == KB_PREC_FP64 ? 8 : 4),
+                            h->stream));
+  }
   // both ping-pong buffers start equal: ghost cells of fix / Maxwell solves are
   // never rewritten, so the second buffer must hold them too
   size_t dist = (size_t)h->ncell * h->vstride * (h->s.prec == KB_PREC_FP64 ? 8 : 4);

@@ -52,6 +52,7 @@ struct BatchDev {
   const double* u;       // velocity tables (FP64)
   const double* wt;
   const float* uf;       // FP32 copies
+  const float* ul;       // u - uf: the FP32 velocities as hi + lo pairs
   const float* wtf;
   double* w;             // [cell][4] (3 used)
   double* prim;          // [cell][4]
@@ -377,12 +378,13 @@ static_assert(SEG_FT >= 1 && SEG * 8 <= SEG_T, "thread groups of the moment phas
 // stride and velocity count: h and b windows, velocity tables, fw, the
 // 16-byte aligned cell coefficients, the face-moment partials and the old
 // prim of the stepped cells.
+constexpr int SEG_CC = 4;  // float4 coefficient blocks per cell
 __host__ __device__ inline int seg_smem(int sst_max, int nu4_max) {
-  return 2 * SEG_ROWS * sst_max * 4 + 2 * nu4_max * 4 + (SEG + 1) * 3 * 8 + 16 + SEG * 3 * 16 +
-         SEG_T * 6 * 4 + SEG * 3 * 8 + 8 * 8;
+  return 2 * SEG_ROWS * sst_max * 4 + 3 * nu4_max * 4 + (SEG + 1) * 3 * 8 + 16 +
+         SEG * SEG_CC * 16 + SEG_T * 6 * 4 + SEG * 3 * 8 + 8 * 8;
 }
 constexpr int SEG_SMEM_MAX = 2 * SEG_ROWS * ((SEG_MAXNU + 31) / 32 * 32 + 4) * 4 +
-                             2 * SEG_MAXNU * 4 + (SEG + 1) * 3 * 8 + 16 + SEG * 3 * 16 +
+                             3 * SEG_MAXNU * 4 + (SEG + 1) * 3 * 8 + 16 + SEG * SEG_CC * 16 +
                              SEG_T * 6 * 4 + SEG * 3 * 8 + 8 * 8;
 
 __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __restrict__ Hin,
@@ -418,10 +420,11 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
   float* sB = sH + SEG_ROWS * B.sst_max;
   float* sU = sB + SEG_ROWS * B.sst_max;
   float* sW = sU + B.nu4_max;
-  double* sfw = (double*)(sW + B.nu4_max);  // [SEG + 1][3]
-  // [SEG][3] float4 cell coefficients, 16-byte aligned
+  float* sUl = sW + B.nu4_max;               // low parts of the velocities
+  double* sfw = (double*)(sUl + B.nu4_max);  // [SEG + 1][3]
+  // [SEG][SEG_CC] float4 cell coefficients, 16-byte aligned
   float4* scc = (float4*)(((unsigned long long)(sfw + (SEG + 1) * 3) + 15) & ~15ull);
-  float* sred = (float*)(scc + SEG * 3);  // [SEG_T][6]: face-moment DF partials
+  float* sred = (float*)(scc + SEG * SEG_CC);  // [SEG_T][6]: face-moment DF partials
   // window rows r0 .. r1-1 (cells incl. ghosts), smem row = cell - r0
   const int r0 = max(i0 - 2, -ng), r1 = min(i1 + 2, nx + ng), nrow = r1 - r0;
   if (tid == 0) {
@@ -441,6 +444,7 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
   }
   for (int v = tid; v < nu; v += SEG_T) {
     sU[v] = B.uf[B.vel_off[b] + v];
+    sUl[v] = B.ul[B.vel_off[b] + v];
     sW[v] = B.wtf[B.vel_off[b] + v];
   }
   if (tid == 0) {
@@ -582,23 +586,31 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
       double lam = pn[2];
       if (!(pn[0] > 0.0) || !(lam > 0.0) || !isfinite(pn[0]) || !isfinite(lam)) atomicOr(B.status, 1);
       // w, prim and q stay FP64; the coefficients below feed only the FP32
-      // pointwise update, so they are formed in FP32 (GB300's FP64 rate is
-      // 1/64 of its FP32 rate, and in 1D a cell has only ~100 velocities)
-      const float rf = float(pn[0]), lf = float(lam), rof = float(rho_o), lof = float(lo);
+      // pointwise update.  The Maxwellian's density factor, U and lambda are
+      // formed in FP64 and rounded once, and U is carried as an FP32 pair
+      // (hi + lo) so that u - U is exact to FP32 rounding of the difference:
+      // at high Mach the energy is mostly kinetic, and an FP32-rounded U or
+      // density factor would bias the moments of the equilibrium by more
+      // than the FP32 split form's 1e-5 budget in T.  tau only sets the
+      // relaxation rate and is formed in FP32 (GB300's FP64 rate is 1/64 of
+      // its FP32 rate).
+      const float rf = float(pn[0]), lf = float(lam);
       const float tau = float(B.mu[b]) * 2.f * powf(lf, float(1.0 - B.omega)) / rf;
       const float dtt = float(dt) / tau;
-      const float Kf = float(B.K);
-      float4* kc = scc + lane * 3;
-      // new Maxwellian: density factor, U, lambda, K / (2 lambda)
-      kc[0] = make_float4(rf * sqrtf(lf * float(1.0 / PI)), float(pn[1]), lf, Kf / (2.f * lf));
-      // dt / tau, 1 / (1 + dt / tau), old Maxwellian (Shakhov) density factor and U
-      kc[1] = make_float4(dtt, 1.f / (1.f + dtt), rof * sqrtf(lof * float(1.0 / PI)), float(Uo));
+      const double Kd = B.K;
+      const float Uh = float(pn[1]), oUh = float(Uo);
+      float4* kc = scc + lane * SEG_CC;
+      // new Maxwellian: density factor, U (hi), lambda, K / (2 lambda)
+      kc[0] = make_float4(float(pn[0] * sqrt(lam * (1.0 / PI))), Uh, lf, float(Kd / (2.0 * lam)));
+      // dt / tau, 1 / (1 + dt / tau), old Maxwellian (Shakhov) density factor and U (hi)
+      kc[1] = make_float4(dtt, 1.f / (1.f + dtt), float(rho_o * sqrt(lo * (1.0 / PI))), oUh);
       // old lambda, K / (2 lambda); .z (the Shakhov heat-flux factor) comes
-      // from warps 1-2
+      // from warps 1-2; .w the low part of U
       float* k2 = (float*)(kc + 2);
-      k2[0] = lof;
-      k2[1] = Kf / (2.f * lof);
-      k2[3] = 0.f;
+      k2[0] = float(lo);
+      k2[1] = float(Kd / (2.0 * lo));
+      k2[3] = float(pn[1] - (double)Uh);
+      kc[3] = make_float4(float(Uo - (double)oUh), 0.f, 0.f, 0.f);
     }
     // residual partial sums of the segment, in a fixed shuffle order (FP32:
     // GB300's FP64 pipe would make this tree the longest chain of the phase)
@@ -623,12 +635,13 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
       BSum<float> sm4;
       sm4.init();
       if (i < cb) {
-        const float Uc = float(spo[jc * 3 + 1]);
+        const double Ud = spo[jc * 3 + 1];
+        const float Uc = float(Ud), Ul = float(Ud - (double)Uc);  // U as an FP32 pair
         const float* hc = rowH(i);
         const float* bc = rowB(i);
         int it = 0;
         for (int v = q; v < nu; v += 4, ++it) {
-          const float cu = sU[v] - Uc;
+          const float cu = (sU[v] - Uc) + (sUl[v] - Ul);
           sm4.add(sW[v] * cu * (cu * cu * hc[v] + bc[v]));
           if ((it & 7) == 7) sm4.flush();
         }
@@ -643,7 +656,7 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
         qf = float(0.8 * (1.0 - B.Pr)) * (lof * lof) / rof * float(qc);
       }
     }
-    if (q == 0 && i < cb) ((float*)(scc + jc * 3 + 2))[2] = qf;
+    if (q == 0 && i < cb) ((float*)(scc + jc * SEG_CC + 2))[2] = qf;
   }
   __syncthreads();  // cell coefficients ready for the pointwise update
   // ---- pointwise KFVS flux + relaxation, one thread per velocity.  Every
@@ -654,7 +667,7 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
   auto pointwise = [&](auto vl_tag) {
     constexpr bool VL = decltype(vl_tag)::value;
     for (int v = tid; v < nu; v += SEG_T) {
-      const float u = sU[v];
+      const float u = sU[v], ulo = sUl[v];
       const bool pos = u >= 0.f;
       const float side = pos ? 0.5f : -0.5f;
       const float Tu = T3 * u, Tuu = T4 * (u * u);
@@ -688,17 +701,16 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
       float* ph = Ho + (long)(ca + ng) * ns + v;
       float* pb = Bo + (long)(ca + ng) * ns + v;
       const float4* kc = scc;
-      for (int i = ca; i < cb; ++i, hr += sst, br += sst, ph += ns, pb += ns, kc += 3) {
+      for (int i = ca; i < cb; ++i, hr += sst, br += sst, ph += ns, pb += ns, kc += SEG_CC) {
         float fhR, fbR;
         face(i + 1, hr + up, br + up, fhR, fbR);
-        const float4 k0 = kc[0], k1 = kc[1];
+        const float4 k0 = kc[0], k1 = kc[1], k2 = kc[2];
         const float h0 = hr[0], b0 = br[0];
-        const float du = u - k0.y;
+        const float du = (u - k0.y) + (ulo - k2.w);
         const float M = k0.x * fexp(-k0.z * du * du);
         float MH = M, MB = M * k0.w;
         if (B.coll == COLL_SHAKHOV) {
-          const float4 k2 = kc[2];
-          const float ou = u - k1.w;
+          const float ou = (u - k1.w) + (ulo - kc[3].x);
           const float OH = k1.z * fexp(-k2.x * ou * ou);
           const float cq = k2.z * ou;
           const float tl = 2.f * k2.x * ou * ou + float(B.K);
@@ -829,7 +841,7 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   if (!base || n <= 0 || !nx || !ngx || !nu || !x0 || !x1 || !umax || !mu_ref || !u_all ||
       !w_all || !out)
     return bfail(KB_ERR_ARG, "kb_batch_create: null argument or empty batch");
-  if (base->dim != 1) return bfail(KB_ERR_CONFIG, "batched solves are 1D2F1V");
+  if (base->dim != 1 || base->nf == 1) return bfail(KB_ERR_CONFIG, "batched solves are 1D2F1V");
   if (base->flux != KB_FLUX_KFVS) return bfail(KB_ERR_CONFIG, "batched solves use KFVS");
   if (base->bc[0] != KB_BC_FIX || base->bc[1] != KB_BC_FIX)
     return bfail(KB_ERR_CONFIG, "batched solves use fixed boundaries");
@@ -906,7 +918,7 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   double* d_respart;
   long *d_co, *d_eo, *d_fo;
   double *d_dx, *d_dt, *d_mu, *d_u, *d_w, *d_wv, *d_prim, *d_fw, *d_q, *d_cp, *d_res;
-  float *d_uf, *d_wf;
+  float *d_uf, *d_wf, *d_ul;
   BALLOC(d_order, int, n);
   BALLOC(d_nx, int, n);
   BALLOC(d_ng, int, n);
@@ -930,6 +942,7 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   BALLOC(d_u, double, vels);
   BALLOC(d_wv, double, vels);
   BALLOC(d_uf, float, vels);
+  BALLOC(d_ul, float, vels);
   BALLOC(d_wf, float, vels);
   BALLOC(d_w, double, cells * 4);
   BALLOC(d_prim, double, cells * 4);
@@ -950,7 +963,8 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
     cudaMemset(B->bq[k], 0, esz * elems);
   }
 #undef BALLOC
-  std::vector<float> uf(u_all, u_all + vels), wf(w_all, w_all + vels);
+  std::vector<float> uf(u_all, u_all + vels), wf(w_all, w_all + vels), ul(vels);
+  for (long k = 0; k < vels; ++k) ul[k] = float(u_all[k] - (double)uf[k]);
   std::vector<int> ones(n, 1);
   bool ok = true;
   ok &= cudaMemcpy(d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -974,6 +988,7 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   ok &= cudaMemcpy(d_u, u_all, sizeof(double) * vels, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_wv, w_all, sizeof(double) * vels, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_uf, uf.data(), sizeof(float) * vels, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(d_ul, ul.data(), sizeof(float) * vels, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_wf, wf.data(), sizeof(float) * vels, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(B->d_umax, umax, sizeof(double) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemset(d_status, 0, sizeof(int)) == cudaSuccess;
@@ -1008,6 +1023,7 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   d.u = d_u;
   d.wt = d_wv;
   d.uf = d_uf;
+  d.ul = d_ul;
   d.wtf = d_wf;
   d.w = d_w;
   d.prim = d_prim;

@@ -33,6 +33,11 @@ struct Geo {
   int bc[4];
   double dx, dy, x0, y0;
   double K, gamma, mu_ref, omega, Pr;
+  // K in the terms of the second distribution b (its equilibrium
+  // B = H K / (2 lambda), the Shakhov factor 2 lambda c^2 + K - 5): K for the
+  // 2F models, 0 for the 1F models, which carry no b (src/Solver/step_1f.jl)
+  double Kb;
+  int nf;  // distributions per cell: 2 (h, b) or 1 (f, held in h; b stays 0)
 };
 
 // Interface quantities of one face in the face-local frame.  KFVS uses only

@@ -107,7 +107,7 @@ __device__ __forceinline__ FP<double> load_fp<double>(const DevState& s, int f) 
   r.U = p.prim[1];
   r.V = p.prim[2];
   r.lam = lam;
-  r.cB = s.g.K / (2.0 * lam);
+  r.cB = s.g.Kb / (2.0 * lam);
   r.Mxi2 = p.Mxi2;
   r.len = p.len;
   for (int k = 0; k < 5; ++k) r.Mt[k] = p.Mt[k];

@@ -97,7 +97,7 @@ __device__ __forceinline__ FaceCoef32 face_coef32(const Geo& g, const FaceParam&
   double lam = P.prim[3], rho = P.prim[0];
   double rho_n = g.D == 1 ? rho * t_sqrt<FAST>(lam / PI) : rho * (lam / PI);
   c.E = maxwell_exp2<FAST>(rho_n, P.prim[1], P.prim[2], lam);
-  double cB = g.K / (2.0 * lam);
+  double cB = g.Kb / (2.0 * lam);
   const double* Mt = P.Mt;
   if (flux == FLUX_KCU) {
     c.T.z = float(Mt[0] * len);
@@ -252,7 +252,7 @@ __global__ void k_face_param(DevState s, double dt) {
   F.U = float(P.prim[1]);
   F.V = float(P.prim[2]);
   F.lam = float(P.prim[3]);
-  F.cB = float(g.K / (2.0 * lam));
+  F.cB = float(g.Kb / (2.0 * lam));
   for (int k = 0; k < 5; ++k) F.Mt[k] = float(P.Mt[k]);
   for (int k = 0; k < 4; ++k) {
     F.aL[k] = float(P.aL[k]);
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(256) k_wall(DevState s, double dt) {
   const double SF = o0.total(), I0 = i0.total();
   const double rho = -SF / (I0 * norm);
   const double rn = rho * norm;  // wall density times the Maxwellian's normalisation
-  const double cBw = g.K / (2.0 * lw);
+  const double cBw = g.Kb / (2.0 * lw);
   double len = D == 2 ? (r.d == 0 ? g.dy : g.dx) : 1.0;
   double sc = D == 2 ? len * dt : dt;
   const double S0 = SF + rn * I0;
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(256) k_wall(DevState s, double dt) {
     float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     wc.G = wc.Cp = wc.Dp = wc.Cm = wc.Dm = z;
     wc.E = maxwell_exp2(D == 1 ? rho * sqrt(lw / PI) : rho * (lw / PI), bw[1], bw[2], lw);
-    wc.T = make_float4(float(sc), 0.f, float(g.K / (2.0 * lw)), float(rot));
+    wc.T = make_float4(float(sc), 0.f, float(g.Kb / (2.0 * lw)), float(rot));
     s.fc[f] = wc;
     double fl[4] = {S0 * sc, S1 * sc, 0.0, 0.0};
     if (D == 1) {
@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(256) k_cell_param(DevState s, double dt) {
     P.oU = p[1];
     P.oV = D == 2 ? p[2] : 0.0;
     P.olam = lo;
-    P.ocB = g.K / (2.0 * lo);
+    P.ocB = g.Kb / (2.0 * lo);
     P.sfac = 0.8 * (1.0 - g.Pr) * (lo * lo) / p[0];
     P.q0 = s.q[(long)c * 2 + 0];
     P.q1 = s.q[(long)c * 2 + 1];
@@ -448,7 +448,7 @@ __global__ void __launch_bounds__(256) k_cell_param(DevState s, double dt) {
       P.U = pn[1];
       P.V = D == 2 ? pn[2] : 0.0;
       P.lam = lam;
-      P.cB = g.K / (2.0 * lam);
+      P.cB = g.Kb / (2.0 * lam);
       P.dtau = dt / tau;
       P.inv = 1.0 / (1.0 + dt / tau);
       bool bad = !(pn[0] > 0.0) || !(lam > 0.0) || !isfinite(pn[0]) || !isfinite(lam) ||
@@ -489,7 +489,7 @@ __global__ void __launch_bounds__(256) k_cell_param(DevState s, double dt) {
         double s0 = P.sfac * P.q0, s1 = P.sfac * P.q1;
         K.Q = make_float4(float(-(s0 * P.oU + s1 * P.oV)), float(s0), float(s1), float(P.ocB));
         double l2 = 2.0 * P.olam;
-        K.TL = make_float4(float(l2 * (P.oU * P.oU + P.oV * P.oV) + g.K), float(-2.0 * l2 * P.oU),
+        K.TL = make_float4(float(l2 * (P.oU * P.oU + P.oV * P.oV) + g.Kb), float(-2.0 * l2 * P.oU),
                            float(-2.0 * l2 * P.oV), float(l2));
       } else {
         K.EO.x = -200.f;
@@ -584,7 +584,7 @@ __device__ __forceinline__ FaceCtx<R> make_ctx(const DevState& s, int f, int kin
     x.wV = R(D == 1 ? 0.0 : (r.d == 0 ? wp[2] : -wp[1]));
     x.wlam = R(lw);
     x.wrn = R(D == 1 ? rho * sqrt(lw / PI) : rho * (lw / PI));
-    x.wcB = R(g.K / (2.0 * lw));
+    x.wcB = R(g.Kb / (2.0 * lw));
     x.wsc = R(D == 2 ? (r.d == 0 ? g.dy : g.dx) * dt : dt);
   }
   return x;
@@ -799,7 +799,7 @@ __global__ void k_init_eq(DevState s, R* __restrict__ H, R* __restrict__ Bq) {
   const double* p = s.prim + c * 4;
   const double rho = p[0], U = p[1], V = g.D == 2 ? p[2] : 0.0, lam = p[g.NW - 1];
   const double rn = g.D == 1 ? rho * sqrt(lam / PI) : rho * (lam / PI);
-  const double cB = g.K / (2.0 * lam);
+  const double cB = g.Kb / (2.0 * lam);
   const long vs = g.vstride;
   for (int v = threadIdx.x; v < g.nvel; v += blockDim.x) {
     const double du = s.u[v] - U;

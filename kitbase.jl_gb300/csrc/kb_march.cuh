@@ -701,7 +701,7 @@ struct FEv<double> {
       wV = g.D == 1 ? 0.0 : (r.d == 0 ? wp[2] : -wp[1]);
       wlam = lw;
       wrn = g.D == 1 ? rho * sqrt(lw / PI) : rho * (lw / PI);
-      wcB = g.K / (2.0 * lw);
+      wcB = g.Kb / (2.0 * lw);
       wsc = g.D == 2 ? (r.d == 0 ? g.dy : g.dx) : 1.0;
       int p0 = r.d == 0 ? r.fi : r.fj;
       rot = p0 == 0 ? 1.0 : -1.0;
@@ -983,7 +983,7 @@ __global__ void __launch_bounds__(BS, (sizeof(R) == 4 && TX < 4 ? 384 : 256) / B
   const R epsx = R(1.e-7 * g.dx), epsy = R(1.e-7 * g.dy);
   const bool shak = s.coll == COLL_SHAKHOV;
   const double ds = D == 1 ? g.dx : g.dx * g.dy;
-  const double Kf = g.K;
+  const double Kf = g.Kb;
 
   bool exx[TX + 4];
   int rx[TX + 4];

@@ -46,6 +46,7 @@ class KbConfig(ctypes.Structure):
         ("umax", ctypes.c_double), ("vmax", ctypes.c_double),
         ("K", ctypes.c_double), ("gamma", ctypes.c_double), ("mu_ref", ctypes.c_double),
         ("omega", ctypes.c_double), ("Pr", ctypes.c_double),
+        ("nf", ctypes.c_int32),
     ]
 
 

@@ -411,14 +411,20 @@ class SolverSet:
     def dim(self):
         return int(self.set.space[0])
 
+    @property
+    def nf(self):
+        """Distributions per cell: 1 for the 1F models (f), 2 for 2F (h, b)."""
+        return int(self.set.space[2])
+
 
 def solver_set(config, **ib_kw):
     """SolverSet(file or dict) (src/Solver/solver_set.jl:73-117) without the
     output-folder side effect."""
     D = read_cfg(config) if isinstance(config, str) else dict(config)
     space = D["space"]
-    if space not in ("1d2f1v", "2d2f2v"):
-        raise ValueError("the GPU DVM path covers 1d2f1v and 2d2f2v, not %r" % space)
+    if space not in ("1d2f1v", "2d2f2v", "1d1f1v", "2d1f2v"):
+        raise ValueError("the GPU DVM path covers 1d2f1v, 2d2f2v, 1d1f1v and 2d1f2v, not %r"
+                         % space)
     dim = int(space[0])
     bc = D.get("boundary", ["fix"] * (2 * dim))
     if isinstance(bc, str):

@@ -51,6 +51,7 @@ def kb_config(KS, precision="fp64"):
     c.umax = vs.u1
     c.vmax = vs.v1 if D == 2 else 0.0
     c.K, c.gamma, c.mu_ref, c.omega, c.Pr = gas.K, gas.gamma, gas.mu_ref, gas.omega, gas.Pr
+    c.nf = KS.nf
     return c
 
 
@@ -90,8 +91,10 @@ class Handle:
     def call(self, name, *args):
         return N.check(getattr(self.lib, name)(self.h, *args))
 
-    def upload(self, w, prim, h, b):
-        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (w, prim, h, b)]
+    def upload(self, w, prim, h, b=None):
+        """Cell state host -> device; b may be None for the 1F models."""
+        a = [None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+             for x in (w, prim, h, b)]
         self.call("kb_upload_state", *[N.ptr(x) for x in a])
 
     def init_equilibrium(self, w, prim):
@@ -273,7 +276,8 @@ def initial_cells(KS):
 
 def initial_state(KS):
     """Per-cell (w, prim, h, b) of init_fvm (src/Solver/solver_init.jl:119-141,
-    :285-325), all cells incl. ghosts, x fastest; flat velocity order."""
+    :285-325), all cells incl. ghosts, x fastest; flat velocity order.  For
+    the 1F models h holds f and b is zero."""
     ps, ib, gas = KS.ps, KS.ib, KS.gas
     if KS.dim == 1:
         xs = list(ps.x)
@@ -295,7 +299,10 @@ def initial_state(KS):
                           np.asarray(b, dtype=np.float64))
         p, h, b = cache[key]
         ws.append(w); ps_.append(p); hs.append(h); bs.append(b)
-    return np.array(ws), np.array(ps_), np.array(hs), np.array(bs)
+    H = np.array(hs)
+    # the 1F models carry f alone (held as h); the second distribution is zero
+    B = np.zeros_like(H) if KS.nf == 1 else np.array(bs)
+    return np.array(ws), np.array(ps_), H, B
 
 
 def wall_states(KS):

@@ -761,6 +761,132 @@ static void flux_ugks(kbo_t* o, const face_in_t* F, double dt, double* fw, doubl
 
 /* flux_boundary_maxwell! 1D2F1V (src/Flux/flux_boundary.jl:39-61) and 2D2F2V
  * (:190-220).  un/ut are the face-frame velocities, bc the face-frame wall prim. */
+/* ------------------------------------------------------------- 1F models
+ * One distribution f per cell (ControlVolume1F / Interface1F,
+ * src/Struct/struct_ctr.jl, struct_face.jl), held in the h arrays of this
+ * oracle; b is unused.  Restated from the reference's 1F functions, not
+ * derived from the 2F ones above. */
+
+/* flux_kfvs! 1F1V (src/Flux/flux_kfvs.jl:238-262) and 1F2V (:615-650), with
+ * flux_conserve! 1f1v / 1f2v (src/Theory/theory_moments.jl:387-391, :401-406) */
+static void flux_kfvs_1f(kbo_t* o, const face_in_t* F, double dt, double* fw, double* ff) {
+  long nv = o->nvel;
+  double* t = scratch(o);
+  const double* om = o->wt;
+  for (long k = 0; k < nv; ++k) {
+    double d = heaviside(F->un[k]);
+    double f = F->hL[k] * d + F->hR[k] * (1.0 - d);
+    double sf = F->shL[k] * d + F->shR[k] * (1.0 - d);
+    double u = F->un[k];
+    ff[k] = dt * u * f - 0.5 * (dt * dt) * (u * u) * sf;
+    if (o->D == 2) ff[k] *= F->len;
+  }
+  for (long k = 0; k < nv; ++k) t[k] = om[k] * ff[k];
+  fw[0] = psum(t, nv);
+  for (long k = 0; k < nv; ++k) t[k] = F->un[k] * om[k] * ff[k];
+  fw[1] = psum(t, nv);
+  if (o->D == 1) {
+    for (long k = 0; k < nv; ++k) t[k] = (F->un[k] * F->un[k]) * om[k] * ff[k];
+    fw[2] = 0.5 * psum(t, nv);
+  } else {
+    for (long k = 0; k < nv; ++k) t[k] = F->ut[k] * om[k] * ff[k];
+    fw[2] = psum(t, nv);
+    for (long k = 0; k < nv; ++k)
+      t[k] = ((F->un[k] * F->un[k]) + (F->ut[k] * F->ut[k])) * om[k] * ff[k];
+    fw[3] = 0.5 * psum(t, nv);
+  }
+}
+
+/* flux_kcu! 1D1F1V (src/Flux/flux_kcu.jl:241-303) and 2D1F2V (:828-894):
+ * interface equilibrium from the half-range moments of both sides, M0 part
+ * of fw from moments_conserve (with the internal degrees of freedom inK),
+ * f0 part from the upwind f, ff = Mt1 u g + Mt2 u f (x len in 2D). */
+static void flux_kcu_1f(kbo_t* o, const face_in_t* F, double dt, double* fw, double* ff) {
+  int NW = o->NW;
+  long nv = o->nvel;
+  double K = o->c.K;
+  double primL[4] = {0}, primR[4] = {0}, w[4] = {0}, prim[4] = {0};
+  interface_prim(o, F->wL, F->wR, primL, primR, w, prim);
+  double tau = vhs_time(prim, NW, o->c.mu_ref, o->c.omega);
+  tau += fabs(primL[0] / primL[NW - 1] - primR[0] / primR[NW - 1]) /
+         (primL[0] / primL[NW - 1] + primR[0] / primR[NW - 1]) * dt * 2.0;
+  double Mt[2];
+  Mt[1] = tau * (1.0 - exp(-dt / tau)); /* f0 */
+  Mt[0] = dt - Mt[1];                   /* M0 */
+  double Mu[7], Mv[7], Mxi[3], MuL[7], MuR[7], Muv[4];
+  gauss_moments(prim, NW, K, Mu, Mv, Mxi, MuL, MuR);
+  double len = o->D == 2 ? F->len : 1.0;
+  if (NW == 3) {
+    mc1(Mu, Mxi, 1, 0, Muv);
+    for (int k = 0; k < 3; ++k) fw[k] = Mt[0] * prim[0] * Muv[k];
+  } else {
+    mc2(Mu, Mv, Mxi, 1, 0, 0, Muv);
+    for (int k = 0; k < 4; ++k) fw[k] = Mt[0] * prim[0] * Muv[k] * len;
+  }
+  double* g = scratch(o) + 2 * nv;
+  double* f = g + nv;
+  double* t = scratch(o);
+  const double *u = F->un, *v = F->ut, *om = o->wt;
+  for (long k = 0; k < nv; ++k) {
+    if (NW == 3)
+      g[k] = prim[0] * sqrt(prim[2] / M_PI) * exp(-prim[2] * ((u[k] - prim[1]) * (u[k] - prim[1])));
+    else
+      g[k] = prim[0] * (prim[3] / M_PI) *
+             exp(-prim[3] * ((u[k] - prim[1]) * (u[k] - prim[1]) + (v[k] - prim[2]) * (v[k] - prim[2])));
+    double d = heaviside(u[k]);
+    f[k] = F->hL[k] * d + F->hR[k] * (1.0 - d);
+  }
+  for (long k = 0; k < nv; ++k) t[k] = om[k] * u[k] * f[k];
+  fw[0] += Mt[1] * psum(t, nv) * len;
+  for (long k = 0; k < nv; ++k) t[k] = om[k] * (u[k] * u[k]) * f[k];
+  fw[1] += Mt[1] * psum(t, nv) * len;
+  if (NW == 3) {
+    for (long k = 0; k < nv; ++k) t[k] = om[k] * (u[k] * u[k] * u[k]) * f[k];
+    fw[2] += Mt[1] * 0.5 * psum(t, nv);
+  } else {
+    for (long k = 0; k < nv; ++k) t[k] = om[k] * v[k] * u[k] * f[k];
+    fw[2] += Mt[1] * psum(t, nv) * len;
+    for (long k = 0; k < nv; ++k) t[k] = om[k] * u[k] * ((u[k] * u[k]) + (v[k] * v[k])) * f[k];
+    fw[3] += Mt[1] * 0.5 * psum(t, nv) * len;
+  }
+  for (long k = 0; k < nv; ++k) ff[k] = (Mt[0] * u[k] * g[k] + Mt[1] * u[k] * f[k]) * len;
+}
+
+/* flux_boundary_maxwell! 2D1F2V (src/Flux/flux_boundary.jl:158-186), face frame. */
+static void flux_maxwell_1f(kbo_t* o, const double* bc, const double* fc, const double* un,
+                            const double* ut, double dt, double len, int rot, double* fw,
+                            double* ff) {
+  long nv = o->nvel;
+  double* t = scratch(o);
+  double* fW = t + nv;
+  const double* om = o->wt;
+  for (long k = 0; k < nv; ++k) t[k] = om[k] * un[k] * fc[k] * (1.0 - heaviside(un[k] * rot));
+  double SF = psum(t, nv);
+  double lw = bc[3];
+  for (long k = 0; k < nv; ++k)
+    t[k] = om[k] * un[k] *
+           exp(-lw * ((un[k] - bc[1]) * (un[k] - bc[1]) + (ut[k] - bc[2]) * (ut[k] - bc[2]))) *
+           heaviside(un[k] * rot);
+  double SG = (lw / M_PI) * psum(t, nv);
+  double prim[4] = {-SF / SG, bc[1], bc[2], bc[3]};
+  for (long k = 0; k < nv; ++k) {
+    double H = prim[0] * (prim[3] / M_PI) *
+               exp(-prim[3] * ((un[k] - prim[1]) * (un[k] - prim[1]) + (ut[k] - prim[2]) * (ut[k] - prim[2])));
+    double d = heaviside(un[k] * rot);
+    fW[k] = H * d + fc[k] * (1.0 - d);
+  }
+  /* discrete_moments(f, u, w, n) = sum(w .* u.^n .* f) (theory_moments.jl:432-437) */
+  for (long k = 0; k < nv; ++k) t[k] = om[k] * un[k] * fW[k];
+  fw[0] = psum(t, nv) * len * dt;
+  for (long k = 0; k < nv; ++k) t[k] = om[k] * (un[k] * un[k]) * fW[k];
+  fw[1] = psum(t, nv) * len * dt;
+  for (long k = 0; k < nv; ++k) t[k] = om[k] * ut[k] * (fW[k] * un[k]);
+  fw[2] = psum(t, nv) * len * dt;
+  for (long k = 0; k < nv; ++k) t[k] = om[k] * un[k] * (fW[k] * ((un[k] * un[k]) + (ut[k] * ut[k])));
+  fw[3] = 0.5 * psum(t, nv) * len * dt;
+  for (long k = 0; k < nv; ++k) ff[k] = un[k] * fW[k] * len * dt;
+}
+
 static void flux_maxwell(kbo_t* o, const double* bc, const double* hc, const double* bcell,
                          const double* un, const double* ut, double dt, double len, int rot,
                          double* fw, double* fh, double* fb) {
@@ -888,7 +1014,11 @@ static void interior_face(kbo_t* o, long cl, long cr, int d, double len, double 
     }
   }
   double fwl[4] = {0, 0, 0, 0};
-  if (o->c.flux == KB_FLUX_KFVS) flux_kfvs(o, &F, dt, fwl, fh, fb);
+  if (o->c.nf == 1) { /* 1F: ff in fh, no fb */
+    if (o->c.flux == KB_FLUX_KFVS) flux_kfvs_1f(o, &F, dt, fwl, fh);
+    else flux_kcu_1f(o, &F, dt, fwl, fh);
+    memset(fb, 0, sizeof(double) * nv);
+  } else if (o->c.flux == KB_FLUX_KFVS) flux_kfvs(o, &F, dt, fwl, fh, fb);
   else if (o->c.flux == KB_FLUX_KCU) flux_kcu(o, &F, dt, fwl, fh, fb);
   else flux_ugks(o, &F, dt, fwl, fh, fb);
   if (NW == 4) global_frame(fwl, n, fw);
@@ -975,8 +1105,13 @@ void kbo_evolve(kbo_t* o, double dt) {
         ut[k] = o->v[k] * n[0] - o->u[k] * n[1];
       }
       local_frame(o->wall[s] + (long)(q - 1) * 4, n, bcl);
-      flux_maxwell(o, bcl, Hc(o, c), Bc(o, c), un, ut, dt, len, (s == 0 || s == 2) ? 1 : -1,
-                   fwl, fh, fb);
+      if (o->c.nf == 1) {
+        flux_maxwell_1f(o, bcl, Hc(o, c), un, ut, dt, len, (s == 0 || s == 2) ? 1 : -1, fwl, fh);
+        memset(fb, 0, sizeof(double) * nv);
+      } else {
+        flux_maxwell(o, bcl, Hc(o, c), Bc(o, c), un, ut, dt, len, (s == 0 || s == 2) ? 1 : -1,
+                     fwl, fh, fb);
+      }
       global_frame(fwl, n, fw);
     }
   }
@@ -1073,6 +1208,63 @@ static void step_cell(kbo_t* o, long c, const double* const* fwv, const double* 
   }
 }
 
+/* step! 1D1F1V (src/Solver/step_1f.jl:6-58) and 2D1F2V (:164-224): f in h.
+ * Shakhov (1D): q = heat_flux(f, prim, u, w) (theory_moments.jl:522),
+ * S = shakhov(u, M, q, prim, Pr) (theory_equilibrium.jl:178-186).  The
+ * reference's 2D1F2V Shakhov branch names an undefined b (step_1f.jl:194),
+ * so 2D1F2V runs BGK only. */
+static void step_cell_1f(kbo_t* o, long c, const double* const* fwv, const double* const* ffv,
+                         double ds, double dt, int coll, double* res, double* avg) {
+  int NW = o->NW;
+  long nv = o->nvel;
+  double g = o->c.gamma, Pr = o->c.Pr;
+  double *w = o->w + c * 4, *prim = o->prim + c * 4, *f = Hc(o, c);
+  const double *u = o->u, *v = o->v, *om = o->wt;
+  double* t = scratch(o);
+  double* S = t + nv;
+  double w_old[4];
+  memcpy(w_old, w, sizeof(w_old));
+  if (coll == KB_COLL_SHAKHOV && NW == 3) {
+    for (long k = 0; k < nv; ++k) {
+      double cu = u[k] - prim[1];
+      t[k] = om[k] * cu * (cu * cu) * f[k];
+    }
+    double q = 0.5 * psum(t, nv);
+    for (long k = 0; k < nv; ++k) {
+      double cu = u[k] - prim[1];
+      double M = prim[0] * sqrt(prim[2] / M_PI) * exp(-prim[2] * (cu * cu));
+      S[k] = 0.8 * (1.0 - Pr) * (prim[2] * prim[2]) / prim[0] * cu * q *
+             (2.0 * prim[2] * (cu * cu) - 5.0) * M;
+    }
+  } else {
+    for (long k = 0; k < nv; ++k) S[k] = 0.0;
+  }
+  for (int k = 0; k < NW; ++k) {
+    if (NW == 3) w[k] += (fwv[0][k] - fwv[1][k]) / ds;
+    else w[k] += (fwv[0][k] - fwv[1][k] + fwv[2][k] - fwv[3][k]) / ds;
+  }
+  conserve_prim(w, NW, g, prim);
+  for (int k = 0; k < NW; ++k) {
+    res[k] = (w[k] - w_old[k]) * (w[k] - w_old[k]);
+    avg[k] = fabs(w[k]);
+  }
+  double tau = vhs_time(prim, NW, o->c.mu_ref, o->c.omega);
+  for (long k = 0; k < nv; ++k) {
+    double M;
+    if (NW == 3)
+      M = prim[0] * sqrt(prim[2] / M_PI) * exp(-prim[2] * ((u[k] - prim[1]) * (u[k] - prim[1])));
+    else
+      M = prim[0] * (prim[3] / M_PI) *
+          exp(-prim[3] * ((u[k] - prim[1]) * (u[k] - prim[1]) + (v[k] - prim[2]) * (v[k] - prim[2])));
+    M += S[k];
+    if (NW == 3)
+      f[k] = (f[k] + (ffv[0][k] - ffv[1][k]) / ds + dt / tau * M) / (1.0 + dt / tau);
+    else
+      f[k] = (f[k] + (ffv[0][k] - ffv[1][k] + ffv[2][k] - ffv[3][k]) / ds + dt / tau * M) /
+             (1.0 + dt / tau);
+  }
+}
+
 static void copy_ctr(kbo_t* o, long dst, long src) { /* copy_ctr!, src/Struct/struct.jl:55-66 */
   memcpy(o->w + dst * 4, o->w + src * 4, sizeof(double) * 4);
   memcpy(o->prim + dst * 4, o->prim + src * 4, sizeof(double) * 4);
@@ -1121,7 +1313,8 @@ void kbo_update(kbo_t* o, double dt, double* residual) {
       /* 1D boundary cells are stepped without the collision keyword, i.e. BGK
        * (src/Solver/update_boundary.jl:33,38) */
       int cc = (o->D == 1 && grp[c] >= 2) ? KB_COLL_BGK : coll;
-      step_cell(o, c, fwv, fhv, fbv, ds, dt, cc, res + c * 8, res + c * 8 + 4);
+      if (o->c.nf == 1) step_cell_1f(o, c, fwv, fhv, ds, dt, cc, res + c * 8, res + c * 8 + 4);
+      else step_cell(o, c, fwv, fhv, fbv, ds, dt, cc, res + c * 8, res + c * 8 + 4);
     }
   /* residuals in cell order (the reference sums racily under @threads) */
   double sR[4] = {0}, sA[4] = {0}, bR[4] = {0}, bA[4] = {0};

@@ -42,6 +42,7 @@ class KbConfig(ctypes.Structure):
         ("umax", ctypes.c_double), ("vmax", ctypes.c_double),
         ("K", ctypes.c_double), ("gamma", ctypes.c_double), ("mu_ref", ctypes.c_double),
         ("omega", ctypes.c_double), ("Pr", ctypes.c_double),
+        ("nf", ctypes.c_int32),
     ]
 
 
@@ -97,7 +98,7 @@ def _p(a):
 
 
 def make_config(dim, nx, ny, ngx, ngy, nu, nv, flux, collision, bc, interp_order, x0, x1, y0,
-                y1, umax, vmax, K, gamma, mu_ref, omega, Pr, precision=0):
+                y1, umax, vmax, K, gamma, mu_ref, omega, Pr, precision=0, nf=2):
     c = KbConfig()
     c.dim, c.nx, c.ny, c.ngx, c.ngy, c.nu, c.nv = dim, nx, ny, ngx, ngy, nu, nv
     c.flux = FLUX[flux] if isinstance(flux, str) else flux
@@ -109,6 +110,7 @@ def make_config(dim, nx, ny, ngx, ngy, nu, nv, flux, collision, bc, interp_order
     c.x0, c.x1, c.y0, c.y1 = x0, x1, y0, y1
     c.umax, c.vmax = umax, vmax
     c.K, c.gamma, c.mu_ref, c.omega, c.Pr = K, gamma, mu_ref, omega, Pr
+    c.nf = nf
     return c
 
 

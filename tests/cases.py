@@ -49,7 +49,7 @@ def oracle_for(KS, threads=None):
     c = O.make_config(cfg.dim, cfg.nx, cfg.ny, cfg.ngx, cfg.ngy, cfg.nu, cfg.nv, cfg.flux,
                       cfg.collision, [cfg.bc[k] for k in range(4)], cfg.interp_order,
                       cfg.x0, cfg.x1, cfg.y0, cfg.y1, cfg.umax, cfg.vmax, cfg.K, cfg.gamma,
-                      cfg.mu_ref, cfg.omega, cfg.Pr)
+                      cfg.mu_ref, cfg.omega, cfg.Pr, nf=cfg.nf)
     vs = KS.vs
     if KS.dim == 1:
         orc = O.Oracle(c, vs.u, None, vs.weights, threads=threads)

@@ -66,6 +66,11 @@ BAD = [
     ("interp", dict(interp_order=3)),
     ("precision", dict(precision=5)),
     ("gamma", dict(gamma=1.0)),
+    ("nf", dict(nf=3)),
+    # 1F: no UGKS step, no 1D1F1V Maxwell wall, no 2D1F2V Shakhov in the reference
+    ("1f-ugks", dict(nf=1, flux=2)),
+    ("1d1f-maxwell", dict(nf=1, bc=(3, 3, 0, 0))),
+    ("2d1f-shakhov", dict(nf=1, dim=2, ny=5, nv=4, collision=1)),
 ]
 
 
@@ -147,7 +152,7 @@ def test_cavity_lid_quirk():
 def test_unsupported_paths_raise():
     from cases import sod
     cfg = sod()
-    cfg["space"] = "1d1f1v"
+    cfg["space"] = "1d3f1v"
     with pytest.raises(ValueError):
         kitgpu.solver_set(cfg)
     cfg = sod()
