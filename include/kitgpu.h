@@ -262,6 +262,13 @@ int kb_batch_destroy(kb_batch_t* b);
 int kb_batch_upload(kb_batch_t* b, const double* w, const double* prim, const double* hdist,
                     const double* bdist);
 int kb_batch_download(kb_batch_t* b, double* w, double* prim, double* hdist, double* bdist);
+/* w, prim of every cell (same layout as kb_batch_upload) with h, b built on
+ * the device as each cell's equilibrium (init_fvm, src/Solver/solver_init.jl:
+ * 119-141).  The FP32 split form evaluates that Maxwellian with the same
+ * FP32 function as its relaxation, so a uniform equilibrium region (such as
+ * the fixed upstream state of a shock) stays bit-exact instead of drifting
+ * by FP32 rounding. */
+int kb_batch_init_equilibrium(kb_batch_t* b, const double* w, const double* prim);
 /* Per-instance CFL time step (timestep, src/Solver/solver_main.jl:240-288). */
 int kb_batch_timestep(kb_batch_t* b, double cfl, double* dt_out);
 int kb_batch_set_dt(kb_batch_t* b, const double* dt);
@@ -269,6 +276,41 @@ int kb_batch_set_dt(kb_batch_t* b, const double* dt);
  * state is carried unchanged).  residual [n][4] and active [n] may be NULL. */
 int kb_batch_step(kb_batch_t* b, int32_t nsteps, double tol, double* residual, int32_t* active);
 int kb_batch_info(kb_batch_t* b, int64_t* elems, int64_t* launches);
+/* Shape of the FP32 batch step kernel, chosen by the autotuner (kitgpu.tune):
+ * params[0] cells per segment (8, 16, 32), params[1] threads per CTA (64, 128,
+ * 256; compiled pairs: 8x64, 16x64, 16x128, 16x256, 32x128, 32x256), params[2]
+ * 1 for a persistent grid (as many CTAs as fit on the GPU, each looping over
+ * segments) or 0 for one CTA per segment.  Call outside stream capture; the
+ * FP64 batch ignores it.  No reference counterpart. */
+int kb_batch_set_tuning(kb_batch_t* b, const int32_t* params, int32_t n);
+int kb_batch_get_tuning(kb_batch_t* b, int32_t* params, int32_t n);
+
+/* ------------------------------------------------------------------- pool
+ * Continuous batching of 1D2F1V solves for a serving loop: a batch whose
+ * instances join and leave between steps.  kb_pool_create reserves
+ * max_instances slots, max_cells cells (ghosts included) and max_nu
+ * velocities per instance (FP32 split form, KFVS, fixed boundaries, as the
+ * batch above).  kb_pool_add places one solve in free ranges: velocity table
+ * u / weights (nu each), cells w / prim [nx + 2 ngx][3] (init_fvm's state; h
+ * and b are built on the device as its equilibrium), the time step
+ * cfl / max((max(umax, |U|) + c) / dx) of timestep (src/Solver/solver_main.jl:
+ * 240-288) returned in *dt_out; *slot receives the instance index used by
+ * the residual / active arrays of kb_batch_step.  kb_pool_remove releases a
+ * slot; kb_pool_download reads one slot's state (w, prim [ncell][3], h, b
+ * [ncell][nu]; any pointer may be NULL).  kb_batch_step advances every
+ * resident solve with one fused launch per step; kb_batch_set_tuning picks
+ * the kernel shape; kb_batch_destroy frees the pool.  The whole-batch
+ * upload / download / timestep / set_dt calls are refused on a pool.  Each
+ * resident solve is what the reference would run as its own solve!
+ * (src/Solver/solver_main.jl:12-76); no single reference counterpart. */
+int kb_pool_create(const kb_config_t* base, int32_t max_instances, int64_t max_cells,
+                   int32_t max_nu, kb_batch_t** out);
+int kb_pool_add(kb_batch_t* b, int32_t nx, int32_t ngx, int32_t nu, double x0, double x1,
+                double umax, double mu_ref, const double* u, const double* weights,
+                const double* w, const double* prim, double cfl, int32_t* slot, double* dt_out);
+int kb_pool_remove(kb_batch_t* b, int32_t slot);
+int kb_pool_download(kb_batch_t* b, int32_t slot, double* w, double* prim, double* hdist,
+                     double* bdist);
 
 #ifdef __cplusplus
 }

@@ -24,117 +24,16 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <cstring>
 #include <numeric>
 #include <string>
 #include <vector>
 
 #include "../../include/kitgpu.h"
-#include "kb_device.cuh"
-#include "kb_kernels.cuh"
-#include "kb_tma.cuh"
+#include "kb_batch.cuh"
 
 namespace kb {
-
-struct BatchDev {
-  int n;                 // instances
-  const int* order;      // processing order (largest first)
-  const int* nx;         // physical cells
-  const int* ng;         // ghost layers
-  const int* nu;         // velocities
-  const int* nus;        // row stride of the distributions: nu rounded up to 4
-  const long* cell_off;  // first cell (incl. ghosts)
-  const long* elem_off;  // first distribution element
-  const int* vel_off;    // velocity table offset
-  const double* dx;      // cell size
-  const double* dt;      // time step
-  const double* mu;      // reference viscosity
-  const double* u;       // velocity tables (FP64)
-  const double* wt;
-  const float* uf;       // FP32 copies
-  const float* ul;       // u - uf: the FP32 velocities as hi + lo pairs
-  const float* wtf;
-  double* w;             // [cell][4] (3 used)
-  double* prim;          // [cell][4]
-  double* fw;            // [instance faces][4] scratch: face flux per instance (nx+1 each)
-  const long* face_off;
-  double* q;             // [cell] old heat flux
-  double* cp;            // [cell][16] cell coefficients (see k_batch_step)
-  double* residual;      // [n][4]
-  int* active;           // [n] 1 while not converged
-  int* counter;          // work counter
-  int* status;
-  // FP32 segment form: segment k covers cells [seg_i0[k], seg_i0[k] + SEG) of
-  // instance seg_b[k]; an instance's segments are consecutive from
-  // seg_first[b] (nseg[b] of them)
-  const int* seg_b;
-  const int* seg_i0;
-  const int* seg_first;
-  const int* nseg;
-  double* respart;       // [segments][8] residual partial sums
-  int sst_max;           // largest shared-memory row stride of the batch (floats)
-  int nu4_max;           // largest velocity count, rounded up to 4
-  double K, gamma, omega, Pr, tol;
-  int coll;
-};
-
-template <typename R>
-__device__ __forceinline__ R bvl(int rule, R qm, R q0, R qp, R epsd) {
-  R a = q0 - qm, b = qp - q0;
-  if (rule == 1) return (a * fabs(b) + b * fabs(a)) / (fabs(a) + fabs(b) + epsd);
-  return R(0);
-}
-// FP32 form: one reciprocal and one multiply (subnormals flushed), the
-// division the FP32 passes of the 2D solver use as well
-template <>
-__device__ __forceinline__ float bvl<float>(int rule, float qm, float q0, float qp, float epsd) {
-  float a = q0 - qm, b = qp - q0;
-  if (rule != 1) return 0.f;
-  float r;
-  asm("div.approx.ftz.f32 %0, %1, %2;"
-      : "=f"(r)
-      : "f"(a * fabsf(b) + b * fabsf(a)), "f"(fabsf(a) + fabsf(b) + epsd));
-  return r;
-}
-
-// 1D slope rule: van Leer everywhere inside when ghosts exist, boundary cells
-// flat without ghosts (src/Solver/solver_reconstruction.jl:101-153).
-__device__ __forceinline__ int brule(int i, int nx, int ng) {
-  if (i < 0 || i >= nx) return 0;
-  if (ng == 0 && (i == 0 || i == nx - 1)) return 0;
-  return 1;
-}
-
-template <typename R>
-struct BSum;
-template <>
-struct BSum<float> {
-  float p;
-  DF d;
-  __device__ __forceinline__ void init() { p = 0.f; d.hi = d.lo = 0.f; }
-  __device__ __forceinline__ void add(float x) { p += x; }
-  __device__ __forceinline__ void flush() { df_add(d, p); p = 0.f; }
-  __device__ __forceinline__ double get() { flush(); return (double)d.hi + (double)d.lo; }
-};
-template <>
-struct BSum<double> {
-  double p;
-  __device__ __forceinline__ void init() { p = 0.0; }
-  __device__ __forceinline__ void add(double x) { p += x; }
-  __device__ __forceinline__ void flush() {}
-  __device__ __forceinline__ double get() { return p; }
-};
-
-template <typename R>
-__device__ __forceinline__ const R* btab(const BatchDev& B, int which);
-template <>
-__device__ __forceinline__ const double* btab<double>(const BatchDev& B, int which) {
-  return which == 0 ? B.u : B.wt;
-}
-template <>
-__device__ __forceinline__ const float* btab<float>(const BatchDev& B, int which) {
-  return which == 0 ? B.uf : B.wtf;
-}
 
 template <typename R, int BS>
 __global__ void __launch_bounds__(BS) k_batch_step(BatchDev B, const R* __restrict__ Hin,
@@ -350,383 +249,6 @@ __global__ void __launch_bounds__(BS) k_batch_step(BatchDev B, const R* __restri
   }
 }
 
-// e^x on the MUFU unit (2^(x log2 e), results below 2^-126 flushed to zero)
-__device__ __forceinline__ float fexp(float x) {
-  float y;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x * 1.4426950408889634f));
-  return y;
-}
-
-// ---- FP32 form: one CTA per segment of SEG cells, the whole step fused.
-// In 1D an instance has at most 256 velocities, so a segment's stencil window
-// (SEG + 4 cells x all velocities, h and b) fits in shared memory: the face
-// moments of the segment's faces, the new w / prim / tau of its cells and
-// the pointwise update all need only the old state inside that window, so
-// the step is one pass over HBM (each value read once, plus a 2-cell halo on
-// each side, and written once).  The window arrives by bulk async copies, one
-// per row, into rows whose stride is = 4 (mod 32) floats so that the face
-// threads read without bank conflicts.  Per-instance residuals are summed
-// by k_batch_seg_res after the step, in segment order (deterministic).
-constexpr int SEG = 16;
-constexpr int SEG_T = 128;
-constexpr int SEG_ROWS = SEG + 4;
-constexpr int SEG_MAXNU = 256;
-__host__ __device__ inline int seg_stride(int nus) { return (nus + 31) / 32 * 32 + 4; }
-constexpr int SEG_FT = SEG_T / (SEG + 1);  // threads per face in the face-moment phase
-static_assert(SEG_FT >= 1 && SEG * 8 <= SEG_T, "thread groups of the moment phases");
-// Dynamic shared memory of a segment CTA, sized by the batch's largest row
-// stride and velocity count: h and b windows, velocity tables, fw, the
-// 16-byte aligned cell coefficients, the face-moment partials and the old
-// prim of the stepped cells.
-constexpr int SEG_CC = 4;  // float4 coefficient blocks per cell
-__host__ __device__ inline int seg_smem(int sst_max, int nu4_max) {
-  return 2 * SEG_ROWS * sst_max * 4 + 3 * nu4_max * 4 + (SEG + 1) * 3 * 8 + 16 +
-         SEG * SEG_CC * 16 + SEG_T * 6 * 4 + SEG * 3 * 8 + 8 * 8;
-}
-constexpr int SEG_SMEM_MAX = 2 * SEG_ROWS * ((SEG_MAXNU + 31) / 32 * 32 + 4) * 4 +
-                             3 * SEG_MAXNU * 4 + (SEG + 1) * 3 * 8 + 16 + SEG * SEG_CC * 16 +
-                             SEG_T * 6 * 4 + SEG * 3 * 8 + 8 * 8;
-
-__global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __restrict__ Hin,
-                                                     const float* __restrict__ Bin,
-                                                     float* __restrict__ Hout,
-                                                     float* __restrict__ Bout) {
-  extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ unsigned long long bar;
-  __shared__ float sconst[4];  // T3, T4, 1/dx, 1e-7 dx
-  // GB300 runs FP64 at 1/64 of the FP32 rate: FP64 work below is done by as
-  // few warps as possible (the per-instance constants by one thread, the
-  // cell update and its residual by the first warp)
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int k = blockIdx.x;
-  const int b = B.seg_b[k], i0 = B.seg_i0[k];
-  const int nx = B.nx[b], ng = B.ng[b], nu = B.nu[b], ns = B.nus[b];
-  const int i1 = min(i0 + SEG, nx);
-  const long c0 = B.cell_off[b], e0 = B.elem_off[b];
-  const float* Hi = Hin + e0;
-  const float* Bi = Bin + e0;
-  float* Ho = Hout + e0;
-  float* Bo = Bout + e0;
-  if (!B.active[b]) {  // converged: carry this segment's cells over
-    for (long t = tid; t < (long)(i1 - i0) * ns; t += SEG_T) {
-      const long o = (long)(i0 + ng) * ns + t;
-      Ho[o] = Hi[o];
-      Bo[o] = Bi[o];
-    }
-    return;
-  }
-  const int sst = seg_stride(ns);
-  float* sH = (float*)sm;
-  float* sB = sH + SEG_ROWS * B.sst_max;
-  float* sU = sB + SEG_ROWS * B.sst_max;
-  float* sW = sU + B.nu4_max;
-  float* sUl = sW + B.nu4_max;               // low parts of the velocities
-  double* sfw = (double*)(sUl + B.nu4_max);  // [SEG + 1][3]
-  // [SEG][SEG_CC] float4 cell coefficients, 16-byte aligned
-  float4* scc = (float4*)(((unsigned long long)(sfw + (SEG + 1) * 3) + 15) & ~15ull);
-  float* sred = (float*)(scc + SEG * SEG_CC);  // [SEG_T][6]: face-moment DF partials
-  // window rows r0 .. r1-1 (cells incl. ghosts), smem row = cell - r0
-  const int r0 = max(i0 - 2, -ng), r1 = min(i1 + 2, nx + ng), nrow = r1 - r0;
-  if (tid == 0) {
-    mbar_init(&bar, 1);
-    fence_async_smem();
-  }
-  __syncthreads();
-  if (tid < 32) {
-    if (lane == 0) mbar_expect(&bar, 2u * nrow * ns * 4u);
-    __syncwarp();
-    for (int r = lane; r < 2 * nrow; r += 32) {
-      const int row = r >> 1;
-      const float* src = ((r & 1) ? Bi : Hi) + (long)(r0 + row + ng) * ns;
-      float* dst = ((r & 1) ? sB : sH) + row * sst;
-      bulk_g2s(dst, src, (unsigned)ns * 4u, &bar);
-    }
-  }
-  for (int v = tid; v < nu; v += SEG_T) {
-    sU[v] = B.uf[B.vel_off[b] + v];
-    sUl[v] = B.ul[B.vel_off[b] + v];
-    sW[v] = B.wtf[B.vel_off[b] + v];
-  }
-  if (tid == 0) {
-    const double dx0 = B.dx[b], dt0 = B.dt[b];
-    sconst[0] = float(dt0);
-    sconst[1] = float(0.5 * dt0 * dt0 / dx0);
-    sconst[2] = float(1.0 / dx0);
-    sconst[3] = float(1.e-7 * dx0);
-  }
-  // one thread waits for the window; the others wait at the CTA barrier
-  const bool ok = tid == 0 ? mbar_wait(&bar, 0) : true;
-  if (__syncthreads_or(!ok)) {  // CTA-uniform: bounded clean-up, then leave
-    if (tid == 0) {
-      atomicOr(B.status, 2);
-      mbar_wait(&bar, 0);
-    }
-    return;
-  }
-  const float epsd = sconst[3];
-  const float T3 = sconst[0], T4 = sconst[1];
-  auto rowH = [&](int c) { return sH + (c - r0) * sst; };
-  auto rowB = [&](int c) { return sB + (c - r0) * sst; };
-
-  // ---- face moments of faces fa .. fb: SEG_FT threads per face (velocities
-  // v = q mod SEG_FT), so the SEG + 1 faces keep all four warps busy
-  const int fa = max(i0, 1), fb = min(i1, nx - 1);
-  const int ca = max(i0, 1), cb = min(i1, nx - 1);  // stepped cells [ca, cb)
-  {
-    const int j = tid / SEG_FT, q = tid - j * SEG_FT;
-    const int f = fa + j;
-    BSum<float> s0, s1, s2;
-    s0.init();
-    s1.init();
-    s2.init();
-    if (j <= SEG && f <= fb) {
-      const int iL = f - 1, iR = f;
-      const int rL = brule(iL, nx, ng), rR = brule(iR, nx, ng);
-      int it = 0;
-      for (int v = q; v < nu; v += SEG_FT, ++it) {
-        const float u = sU[v];
-        const bool pos = u >= 0.f;
-        const int c = pos ? iL : iR;
-        const int r = pos ? rL : rR;
-        const float* hc = rowH(c);
-        const float* bc = rowB(c);
-        const float h0 = hc[v], b0 = bc[v];
-        float sh = 0.f, sb = 0.f;
-        if (r == 1) {
-          sh = bvl<float>(1, hc[v - sst], h0, hc[v + sst], epsd);
-          sb = bvl<float>(1, bc[v - sst], b0, bc[v + sst], epsd);
-        }
-        const float side = pos ? 0.5f : -0.5f;
-        const float hf = h0 + side * sh, bf = b0 + side * sb;
-        const float fh = T3 * u * hf - T4 * (u * u) * sh;
-        const float fbb = T3 * u * bf - T4 * (u * u) * sb;
-        const float wf = sW[v] * fh;
-        s0.add(wf);
-        s1.add(wf * u);
-        s2.add(wf * u * u + sW[v] * fbb);
-        if ((it & 7) == 7) {
-          s0.flush();
-          s1.flush();
-          s2.flush();
-        }
-      }
-    }
-    // each thread's compensated partials, merged per face below in thread
-    // order: both segments that share a face map it to the same threads q,
-    // so they compute bit-identical fw (conservation holds exactly)
-    s0.flush();
-    s1.flush();
-    s2.flush();
-    float* o = sred + tid * 6;
-    o[0] = s0.d.hi;
-    o[1] = s0.d.lo;
-    o[2] = s1.d.hi;
-    o[3] = s1.d.lo;
-    o[4] = s2.d.hi;
-    o[5] = s2.d.lo;
-  }
-  // the old prim of the stepped cells, read before warp 0 overwrites it
-  // (warps 1 and 2 need the old U while warp 0 updates the cells)
-  double* spo = (double*)(sred + SEG_T * 6);  // [SEG][3] rho, U, lambda
-  if (tid < cb - ca) {
-    const double* p = B.prim + (c0 + ca + tid + ng) * 4;
-    spo[tid * 3 + 0] = p[0];
-    spo[tid * 3 + 1] = p[1];
-    spo[tid * 3 + 2] = p[2];
-  }
-  __syncthreads();  // face partials and old prim in shared memory
-  // Warp 0: merge the face moments, then the FP64 cell update; warps 1 and 2
-  // meanwhile: the old heat flux (Shakhov) of the stepped cells.
-  static_assert(SEG <= 32 && 4 * SEG <= 64, "cell update on warp 0, heat flux on warps 1-2");
-  if (wid == 0) {
-    // residual terms of the cell: a convergence monitor, summed in FP32 below
-    float rr[6] = {0, 0, 0, 0, 0, 0};
-    // face f = fa + jf, moment m: the SEG_FT partials of its threads, in order
-    for (int t0 = lane; t0 < 3 * (SEG + 1); t0 += 32) {
-      const int jf = t0 / 3, m = t0 - 3 * jf;
-      if (fa + jf <= fb) {
-        const float* o = sred + jf * SEG_FT * 6 + 2 * m;
-        DF d;
-        d.hi = o[0];
-        d.lo = o[1];
-        for (int t = 1; t < SEG_FT; ++t) {
-          DF e;
-          e.hi = o[6 * t];
-          e.lo = o[6 * t + 1];
-          d = df_merge(d, e);
-        }
-        const double v = (double)d.hi + (double)d.lo;
-        sfw[jf * 3 + m] = m == 2 ? 0.5 * v : v;
-      }
-    }
-    __syncwarp();
-    // ---- cell parameters of the stepped cells (one lane per cell, FP64)
-    if (lane < cb - ca) {
-      const double dx = B.dx[b], dt = B.dt[b];
-      const int i = ca + lane;
-      const long c = c0 + i + ng;
-      double* w = B.w + c * 4;
-      double* p = B.prim + c * 4;
-      const double* fL = sfw + (i - fa) * 3;
-      const double* fR = sfw + (i + 1 - fa) * 3;
-      double wo[3] = {w[0], w[1], w[2]};
-      const double rho_o = spo[lane * 3 + 0], Uo = spo[lane * 3 + 1], lo = spo[lane * 3 + 2];
-      const double idx = 1.0 / dx;
-      for (int m = 0; m < 3; ++m) w[m] += (fL[m] - fR[m]) * idx;
-      double pn[4];
-      conserve_prim<true>(w, 3, B.gamma, pn);
-      p[0] = pn[0];
-      p[1] = pn[1];
-      p[2] = pn[2];
-      for (int m = 0; m < 3; ++m) {
-        double d = w[m] - wo[m];
-        rr[m] = float(d * d);
-        rr[3 + m] = float(fabs(w[m]));
-      }
-      double lam = pn[2];
-      if (!(pn[0] > 0.0) || !(lam > 0.0) || !isfinite(pn[0]) || !isfinite(lam)) atomicOr(B.status, 1);
-      // w, prim and q stay FP64; the coefficients below feed only the FP32
-      // pointwise update.  The Maxwellian's density factor, U and lambda are
-      // formed in FP64 and rounded once, and U is carried as an FP32 pair
-      // (hi + lo) so that u - U is exact to FP32 rounding of the difference:
-      // at high Mach the energy is mostly kinetic, and an FP32-rounded U or
-      // density factor would bias the moments of the equilibrium by more
-      // than the FP32 split form's 1e-5 budget in T.  tau only sets the
-      // relaxation rate and is formed in FP32 (GB300's FP64 rate is 1/64 of
-      // its FP32 rate).
-      const float rf = float(pn[0]), lf = float(lam);
-      const float tau = float(B.mu[b]) * 2.f * powf(lf, float(1.0 - B.omega)) / rf;
-      const float dtt = float(dt) / tau;
-      const double Kd = B.K;
-      const float Uh = float(pn[1]), oUh = float(Uo);
-      float4* kc = scc + lane * SEG_CC;
-      // new Maxwellian: density factor, U (hi), lambda, K / (2 lambda)
-      kc[0] = make_float4(float(pn[0] * sqrt(lam * (1.0 / PI))), Uh, lf, float(Kd / (2.0 * lam)));
-      // dt / tau, 1 / (1 + dt / tau), old Maxwellian (Shakhov) density factor and U (hi)
-      kc[1] = make_float4(dtt, 1.f / (1.f + dtt), float(rho_o * sqrt(lo * (1.0 / PI))), oUh);
-      // old lambda, K / (2 lambda); .z (the Shakhov heat-flux factor) comes
-      // from warps 1-2; .w the low part of U
-      float* k2 = (float*)(kc + 2);
-      k2[0] = float(lo);
-      k2[1] = float(Kd / (2.0 * lo));
-      k2[3] = float(pn[1] - (double)Uh);
-      kc[3] = make_float4(float(Uo - (double)oUh), 0.f, 0.f, 0.f);
-    }
-    // residual partial sums of the segment, in a fixed shuffle order (FP32:
-    // GB300's FP64 pipe would make this tree the longest chain of the phase)
-#pragma unroll
-    for (int m = 0; m < 6; ++m) {
-#pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) rr[m] += __shfl_xor_sync(0xffffffffu, rr[m], o);
-    }
-    // this segment's residual partial sums (k_batch_seg_res adds them up)
-    if (lane == 0) {
-      double* pr = B.respart + (long)k * 8;
-#pragma unroll
-      for (int m = 0; m < 6; ++m) pr[m] = (double)rr[m];
-    }
-  } else if (wid <= 2) {
-    // ---- old heat flux of the stepped cells, 4 threads per cell, and the
-    // Shakhov factor 0.8 (1 - Pr) lambda^2 / rho q of the cell coefficients
-    const int lt = tid - 32, jc = lt >> 2, q = lt & 3;
-    const int i = ca + jc;
-    float qf = 0.f;
-    if (B.coll == COLL_SHAKHOV) {
-      BSum<float> sm4;
-      sm4.init();
-      if (i < cb) {
-        const double Ud = spo[jc * 3 + 1];
-        const float Uc = float(Ud), Ul = float(Ud - (double)Uc);  // U as an FP32 pair
-        const float* hc = rowH(i);
-        const float* bc = rowB(i);
-        int it = 0;
-        for (int v = q; v < nu; v += 4, ++it) {
-          const float cu = (sU[v] - Uc) + (sUl[v] - Ul);
-          sm4.add(sW[v] * cu * (cu * cu * hc[v] + bc[v]));
-          if ((it & 7) == 7) sm4.flush();
-        }
-      }
-      sm4.flush();
-      DF d = sm4.d;
-#pragma unroll
-      for (int m = 1; m <= 2; m <<= 1) d = df_merge(d, df_shfl_xor(d, m));
-      if (i < cb) {
-        const double qc = 0.5 * ((double)d.hi + (double)d.lo);
-        const float rof = float(spo[jc * 3 + 0]), lof = float(spo[jc * 3 + 2]);
-        qf = float(0.8 * (1.0 - B.Pr)) * (lof * lof) / rof * float(qc);
-      }
-    }
-    if (q == 0 && i < cb) ((float*)(scc + jc * SEG_CC + 2))[2] = qf;
-  }
-  __syncthreads();  // cell coefficients ready for the pointwise update
-  // ---- pointwise KFVS flux + relaxation, one thread per velocity.  Every
-  // upwind cell of a segment away from ghost-less ends takes the van Leer
-  // slope, so that form skips the per-face slope rule.
-  const float idx = sconst[2];
-  const bool all_vl = ng > 0 || (ca >= 2 && cb <= nx - 2);
-  auto pointwise = [&](auto vl_tag) {
-    constexpr bool VL = decltype(vl_tag)::value;
-    for (int v = tid; v < nu; v += SEG_T) {
-      const float u = sU[v], ulo = sUl[v];
-      const bool pos = u >= 0.f;
-      const float side = pos ? 0.5f : -0.5f;
-      const float Tu = T3 * u, Tuu = T4 * (u * u);
-      if (i0 == 0) {  // fixed end cells keep their state
-        Ho[(long)ng * ns + v] = rowH(0)[v];
-        Bo[(long)ng * ns + v] = rowB(0)[v];
-      }
-      if (i1 == nx) {
-        Ho[(long)(nx - 1 + ng) * ns + v] = rowH(nx - 1)[v];
-        Bo[(long)(nx - 1 + ng) * ns + v] = rowB(nx - 1)[v];
-      }
-      // flux through face f, whose upwind cell row starts at hc / bc
-      auto face = [&](int f, const float* hc, const float* bc, float& fh, float& fbv) {
-        const float h0 = hc[0], b0 = bc[0];
-        float sh = 0.f, sb = 0.f;
-        if (VL || brule(pos ? f - 1 : f, nx, ng) == 1) {
-          sh = bvl<float>(1, hc[-sst], h0, hc[sst], epsd);
-          sb = bvl<float>(1, bc[-sst], b0, bc[sst], epsd);
-        }
-        fh = Tu * (h0 + side * sh) - Tuu * sh;
-        fbv = Tu * (b0 + side * sb) - Tuu * sb;
-      };
-      if (ca >= cb) continue;
-      // hr / br: row of cell i at this velocity; the upwind cell of face i + 1
-      // is i (pos) or i + 1
-      const int up = pos ? 0 : sst;
-      const float* hr = rowH(ca) + v;
-      const float* br = rowB(ca) + v;
-      float fhL, fbL;
-      face(ca, hr - sst + up, br - sst + up, fhL, fbL);
-      float* ph = Ho + (long)(ca + ng) * ns + v;
-      float* pb = Bo + (long)(ca + ng) * ns + v;
-      const float4* kc = scc;
-      for (int i = ca; i < cb; ++i, hr += sst, br += sst, ph += ns, pb += ns, kc += SEG_CC) {
-        float fhR, fbR;
-        face(i + 1, hr + up, br + up, fhR, fbR);
-        const float4 k0 = kc[0], k1 = kc[1], k2 = kc[2];
-        const float h0 = hr[0], b0 = br[0];
-        const float du = (u - k0.y) + (ulo - k2.w);
-        const float M = k0.x * fexp(-k0.z * du * du);
-        float MH = M, MB = M * k0.w;
-        if (B.coll == COLL_SHAKHOV) {
-          const float ou = (u - k1.w) + (ulo - kc[3].x);
-          const float OH = k1.z * fexp(-k2.x * ou * ou);
-          const float cq = k2.z * ou;
-          const float tl = 2.f * k2.x * ou * ou + float(B.K);
-          MH += cq * (tl - 5.f) * OH;
-          MB += cq * (tl - 3.f) * OH * k2.y;
-        }
-        *ph = (h0 + (fhL - fhR) * idx + k1.x * MH) * k1.y;
-        *pb = (b0 + (fbL - fbR) * idx + k1.x * MB) * k1.y;
-        fhL = fhR;
-        fbL = fbR;
-      }
-    }
-  };
-  if (all_vl) pointwise(std::true_type{});
-  else pointwise(std::false_type{});
-}
 
 // Residual of each active instance of the segment form
 // (src/Solver/solver_update.jl:86-88) and its convergence flag.  One warp per
@@ -754,8 +276,9 @@ __global__ void k_batch_seg_res(BatchDev B) {
   }
 }
 
-__global__ void k_batch_timestep(BatchDev B, const double* umax, double cfl, double* dt_out) {
-  const int b = blockIdx.x;
+__global__ void k_batch_timestep(BatchDev B, const double* umax, double cfl, double* dt_out,
+                                 int b0 = 0) {
+  const int b = b0 + blockIdx.x;
   __shared__ double red[256];
   const int nx = B.nx[b], ng = B.ng[b];
   double m = 0.0;
@@ -771,6 +294,39 @@ __global__ void k_batch_timestep(BatchDev B, const double* umax, double cfl, dou
     __syncthreads();
   }
   if (threadIdx.x == 0) dt_out[b] = cfl / red[0];
+}
+
+// Equilibrium h, b of instances' cells into both FP32 buffers with the
+// relaxation's own FP32 Maxwellian (seg_init_cell): blockIdx.y = instance
+// b0 + y, blockIdx.x = cell.
+__global__ void k_batch_init_eq32(BatchDev B, int b0, float* H0, float* B0, float* H1, float* B1) {
+  const int b = b0 + blockIdx.y;
+  if ((int)blockIdx.x >= B.nx[b] + 2 * B.ng[b]) return;
+  seg_init_cell(B, b, blockIdx.x, H0, B0, H1, B1);
+}
+
+// FP64 form: h = maxwellian(u, prim), b = h K / (2 lambda) in FP64
+// (src/Theory/theory_equilibrium.jl:8-13) into both buffers.
+__global__ void k_batch_init_eq64(BatchDev B, double* H0, double* B0, double* H1, double* B1) {
+  const int b = blockIdx.y;
+  if ((int)blockIdx.x >= B.nx[b] + 2 * B.ng[b]) return;
+  const double* p = B.prim + (B.cell_off[b] + blockIdx.x) * 4;
+  const double rn = p[0] * sqrt(p[2] / PI), cB = B.K / (2.0 * p[2]);
+  const int nu = B.nu[b], ns = B.nus[b];
+  const long e = B.elem_off[b] + (long)blockIdx.x * ns;
+  const double* u = B.u + B.vel_off[b];
+  for (int v = threadIdx.x; v < ns; v += blockDim.x) {
+    double hv = 0.0, bv = 0.0;
+    if (v < nu) {
+      const double du = u[v] - p[1];
+      hv = rn * exp(-p[2] * du * du);
+      bv = hv * cB;
+    }
+    H0[e + v] = hv;
+    B0[e + v] = bv;
+    H1[e + v] = hv;
+    B1[e + v] = bv;
+  }
 }
 
 template <typename R>
@@ -807,6 +363,22 @@ struct kb_batch {
   int graph_cur = -1;
   int grid = 0;
   int64_t launches = 0;
+  // FP32 segment kernel: shape (cells per segment, threads, persistent grid)
+  // and its launch; segment tables are rebuilt when the shape changes
+  int seg = 16, seg_t = 128, persist = 0;
+  const void* seg_fn = nullptr;
+  int seg_smem = 0, seg_grid = 0;
+  int* d_segb = nullptr;
+  int* d_segi0 = nullptr;
+  int* d_segfirst = nullptr;
+  int* d_nseg = nullptr;
+  long seg_cap = 0;  // capacity of the segment tables (segments of 8 cells)
+  // pool form (kb_pool_*): instance slots that requests join and leave, and
+  // first-fit allocators of the cell, element and velocity ranges
+  bool pool = false;
+  std::vector<char> used;
+  std::map<long, long> free_cells, free_elems, free_vels;  // offset -> length
+  std::vector<long> vel_off_h;
 };
 
 static int bfail(int code, const std::string& m) {
@@ -831,6 +403,71 @@ extern "C" int kb_batch_destroy(kb_batch_t* B) {
   for (void* p : B->allocs) cudaFree(p);
   if (B->stream) cudaStreamDestroy(B->stream);
   delete B;
+  return KB_OK;
+}
+
+// Compiled shapes of the FP32 segment kernel (kb_batch_seg_a.cu, _b.cu).
+static const std::vector<kb::SegVariant>& seg_variants() {
+  static const std::vector<kb::SegVariant> v = [] {
+    std::vector<kb::SegVariant> out;
+    kb::seg_variants_a(out);
+    kb::seg_variants_b(out);
+    return out;
+  }();
+  return v;
+}
+
+// Select the segment kernel's shape: segment tables for `seg` cells per
+// segment (instances in processing order, their segments consecutive),
+// the kernel's shared-memory limit, and the grid -- one CTA per segment, or
+// (persist) as many CTAs as fit on the GPU at once, each looping over
+// segments.  Runs outside any stream capture; invalidates the step graph.
+static int batch_set_shape(kb_batch* B, int seg, int threads, int persist) {
+  const kb::SegVariant* var = nullptr;
+  for (const auto& v : seg_variants())
+    if (v.seg == seg && v.threads == threads) var = &v;
+  if (!var) return bfail(KB_ERR_ARG, "batch shape: no segment kernel for " + std::to_string(seg) +
+                                         " cells x " + std::to_string(threads) + " threads");
+  std::vector<int> seg_b, seg_i0, seg_first(B->n), nseg(B->n);
+  for (int b = 0; b < B->n; ++b) {
+    seg_first[b] = (int)seg_b.size();
+    nseg[b] = B->pool && !B->used[b] ? 0 : (B->nx[b] + seg - 1) / seg;
+    for (int k = 0; k < nseg[b]; ++k) {
+      seg_b.push_back(b);
+      seg_i0.push_back(k * seg);
+    }
+  }
+  if ((long)seg_b.size() > B->seg_cap) return bfail(KB_ERR_ARG, "batch shape: segment table overflow");
+  cudaStreamSynchronize(B->stream);
+  bool ok = true;
+  ok &= cudaMemcpy(B->d_segb, seg_b.data(), sizeof(int) * seg_b.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(B->d_segi0, seg_i0.data(), sizeof(int) * seg_i0.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(B->d_segfirst, seg_first.data(), sizeof(int) * B->n, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(B->d_nseg, nseg.data(), sizeof(int) * B->n, cudaMemcpyHostToDevice) == cudaSuccess;
+  const int smem = var->smem(B->d.sst_max, B->d.nu4_max);
+  ok &= cudaFuncSetAttribute(var->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, var->smem_max) ==
+        cudaSuccess;
+  int per = 0, dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  ok &= cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, var->fn, threads, smem) == cudaSuccess;
+  if (!ok || per < 1) {
+    cudaGetLastError();
+    return bfail(KB_ERR_CUDA, "batch shape: segment tables or kernel attributes refused");
+  }
+  B->nseg = (long)seg_b.size();
+  B->d.nseg_all = (int)B->nseg;
+  B->seg = seg;
+  B->seg_t = threads;
+  B->persist = persist ? 1 : 0;
+  B->seg_fn = var->fn;
+  B->seg_smem = smem;
+  B->seg_grid = persist ? (int)std::min<long>(B->nseg, (long)sms * per) : (int)B->nseg;
+  if (B->pool && persist) B->seg_grid = sms * per;  // fixed, whatever the membership
+  if (B->graph) {
+    cudaGraphExecDestroy(B->graph);
+    B->graph = nullptr;
+  }
   return KB_OK;
 }
 
@@ -867,8 +504,8 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   long cells = 0, elems = 0, faces = 0, vels = 0;
   B->nus.resize(n);
   B->dense_off.resize(n);
-  std::vector<int> seg_b, seg_i0, seg_first(n), nseg(n);
   long dense = 0;
+  long seg_cap = 0;
   for (int b = 0; b < n; ++b) {
     B->cell_off[b] = cells;
     B->elem_off[b] = elems;
@@ -883,15 +520,10 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
     faces += nx[b] + 1;
     vels += nu[b];
     dx[b] = (x1[b] - x0[b]) / nx[b];
-    seg_first[b] = (int)seg_b.size();
-    nseg[b] = (nx[b] + kb::SEG - 1) / kb::SEG;
-    for (int k = 0; k < nseg[b]; ++k) {
-      seg_b.push_back(b);
-      seg_i0.push_back(k * kb::SEG);
-    }
+    seg_cap += (nx[b] + 7) / 8;  // the shortest segment length the tuner offers
   }
   B->ndense = dense;
-  B->nseg = (long)seg_b.size();
+  B->seg_cap = seg_cap;
   B->ncell = cells;
   B->nelem = elems;
   B->nface = faces;
@@ -924,11 +556,11 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   BALLOC(d_ng, int, n);
   BALLOC(d_nu, int, n);
   BALLOC(d_nus, int, n);
-  BALLOC(d_segb, int, B->nseg);
-  BALLOC(d_segi0, int, B->nseg);
+  BALLOC(d_segb, int, B->seg_cap);
+  BALLOC(d_segi0, int, B->seg_cap);
   BALLOC(d_segfirst, int, n);
   BALLOC(d_nseg, int, n);
-  BALLOC(d_respart, double, B->nseg * 8);
+  BALLOC(d_respart, double, B->seg_cap * 8);
   BALLOC(d_vo, int, n);
   BALLOC(d_active, int, n);
   BALLOC(d_counter, int, 2);
@@ -972,11 +604,7 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   ok &= cudaMemcpy(d_ng, ngx, sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_nu, nu, sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_nus, B->nus.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
-  ok &= cudaMemcpy(d_segb, seg_b.data(), sizeof(int) * B->nseg, cudaMemcpyHostToDevice) == cudaSuccess;
-  ok &= cudaMemcpy(d_segi0, seg_i0.data(), sizeof(int) * B->nseg, cudaMemcpyHostToDevice) == cudaSuccess;
-  ok &= cudaMemcpy(d_segfirst, seg_first.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
-  ok &= cudaMemcpy(d_nseg, nseg.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
-  ok &= cudaMemset(d_respart, 0, sizeof(double) * B->nseg * 8) == cudaSuccess;
+  ok &= cudaMemset(d_respart, 0, sizeof(double) * B->seg_cap * 8) == cudaSuccess;
   ok &= cudaMemcpy(d_vo, vel_off.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_active, ones.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   ok &= cudaMemcpy(d_co, B->cell_off.data(), sizeof(long) * n, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -1007,6 +635,10 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   d.seg_i0 = d_segi0;
   d.seg_first = d_segfirst;
   d.nseg = d_nseg;
+  B->d_segb = d_segb;
+  B->d_segi0 = d_segi0;
+  B->d_segfirst = d_segfirst;
+  B->d_nseg = d_nseg;
   d.respart = d_respart;
   d.sst_max = 4;
   d.nu4_max = 4;
@@ -1049,19 +681,15 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb::k_batch_step<float, 256>, 256, 0);
   B->grid = std::min(n, std::max(1, sms * per));
-  // the segment kernel's dynamic shared memory limit, raised on this device
-  // once per batch here rather than at launch (launches may sit inside a
-  // stream capture, and batches may be driven from several host threads)
-  if (B->prec == KB_PREC_FP32 &&
-      cudaFuncSetAttribute(kb::k_batch_seg, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kb::SEG_SMEM_MAX) != cudaSuccess)
-    return fail_out(bfail(KB_ERR_CUDA, "kb_batch_create: shared-memory attribute refused"));
+  if (B->prec == KB_PREC_FP32 && (rc = batch_set_shape(B, 16, 128, 0)) != KB_OK)
+    return fail_out(rc);
   *out = B;
   return KB_OK;
 }
 
 extern "C" int kb_batch_upload(kb_batch_t* B, const double* w, const double* prim,
                                const double* h, const double* bq) {
+  if (B && B->pool) return bfail(KB_ERR_STATE, "pools move state per slot (kb_pool_add / kb_pool_download)");
   if (!B || !w || !prim || !h || !bq) return bfail(KB_ERR_ARG, "kb_batch_upload: null argument");
   std::vector<double> w4(B->ncell * 4, 0.0), p4(B->ncell * 4, 0.0);
   for (long c = 0; c < B->ncell; ++c)
@@ -1103,7 +731,40 @@ extern "C" int kb_batch_upload(kb_batch_t* B, const double* w, const double* pri
   return KB_OK;
 }
 
+extern "C" int kb_batch_init_equilibrium(kb_batch_t* B, const double* w, const double* prim) {
+  if (B && B->pool) return bfail(KB_ERR_STATE, "pools move state per slot (kb_pool_add / kb_pool_download)");
+  if (!B || !w || !prim) return bfail(KB_ERR_ARG, "kb_batch_init_equilibrium: null argument");
+  std::vector<double> w4(B->ncell * 4, 0.0), p4(B->ncell * 4, 0.0);
+  for (long c = 0; c < B->ncell; ++c)
+    for (int k = 0; k < 3; ++k) {
+      w4[c * 4 + k] = w[c * 3 + k];
+      p4[c * 4 + k] = prim[c * 3 + k];
+    }
+  if (cudaMemcpy(B->d.w, w4.data(), sizeof(double) * w4.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(B->d.prim, p4.data(), sizeof(double) * p4.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bfail(KB_ERR_CUDA, "kb_batch_init_equilibrium: copy failed");
+  int maxc = 1;
+  for (int b = 0; b < B->n; ++b) maxc = std::max(maxc, B->nx[b] + 2 * B->ng[b]);
+  const dim3 grid((unsigned)maxc, (unsigned)B->n);
+  if (B->prec == KB_PREC_FP64)
+    kb::k_batch_init_eq64<<<grid, 128, 0, B->stream>>>(B->d, (double*)B->h[0], (double*)B->bq[0],
+                                                       (double*)B->h[1], (double*)B->bq[1]);
+  else
+    kb::k_batch_init_eq32<<<grid, 128, 0, B->stream>>>(B->d, 0, (float*)B->h[0], (float*)B->bq[0],
+                                                       (float*)B->h[1], (float*)B->bq[1]);
+  B->launches++;
+  std::vector<int> ones(B->n, 1);
+  cudaMemcpyAsync((void*)B->d.active, ones.data(), sizeof(int) * B->n, cudaMemcpyHostToDevice, B->stream);
+  cudaMemsetAsync(B->d.status, 0, sizeof(int), B->stream);
+  if (cudaStreamSynchronize(B->stream) != cudaSuccess)
+    return bfail(KB_ERR_CUDA, std::string("kb_batch_init_equilibrium: ") +
+                                  cudaGetErrorString(cudaGetLastError()));
+  B->cur = 0;
+  return KB_OK;
+}
+
 extern "C" int kb_batch_download(kb_batch_t* B, double* w, double* prim, double* h, double* bq) {
+  if (B && B->pool) return bfail(KB_ERR_STATE, "pools move state per slot (kb_pool_add / kb_pool_download)");
   if (!B) return bfail(KB_ERR_ARG, "kb_batch_download: null handle");
   cudaStreamSynchronize(B->stream);
   if (w || prim) {
@@ -1142,6 +803,7 @@ extern "C" int kb_batch_download(kb_batch_t* B, double* w, double* prim, double*
 }
 
 extern "C" int kb_batch_timestep(kb_batch_t* B, double cfl, double* dt_out) {
+  if (B && B->pool) return bfail(KB_ERR_STATE, "pool time steps are set per slot by kb_pool_add");
   if (!B) return bfail(KB_ERR_ARG, "kb_batch_timestep: null handle");
   kb::k_batch_timestep<<<B->n, 256, 0, B->stream>>>(B->d, B->d_umax, cfl, (double*)B->d.dt);
   B->launches++;
@@ -1152,6 +814,7 @@ extern "C" int kb_batch_timestep(kb_batch_t* B, double cfl, double* dt_out) {
 }
 
 extern "C" int kb_batch_set_dt(kb_batch_t* B, const double* dt) {
+  if (B && B->pool) return bfail(KB_ERR_STATE, "pool time steps are set per slot by kb_pool_add");
   if (!B || !dt) return bfail(KB_ERR_ARG, "kb_batch_set_dt: null argument");
   if (cudaMemcpy((void*)B->d.dt, dt, sizeof(double) * B->n, cudaMemcpyHostToDevice) != cudaSuccess)
     return bfail(KB_ERR_CUDA, "kb_batch_set_dt failed");
@@ -1164,10 +827,14 @@ static int batch_kernels_per_step(const kb_batch* B) { return B->prec == KB_PREC
 
 static void batch_launch(kb_batch* B, int cur) {
   if (B->prec == KB_PREC_FP32) {  // fused segments (one pass over HBM)
-    const int smem = kb::seg_smem(B->d.sst_max, B->d.nu4_max);
-    kb::k_batch_seg<<<(unsigned)B->nseg, kb::SEG_T, smem, B->stream>>>(
-        B->d, (const float*)B->h[cur], (const float*)B->bq[cur], (float*)B->h[cur ^ 1],
-        (float*)B->bq[cur ^ 1]);
+    const float* hin = (const float*)B->h[cur];
+    const float* bin = (const float*)B->bq[cur];
+    float* hout = (float*)B->h[cur ^ 1];
+    float* bout = (float*)B->bq[cur ^ 1];
+    void* args[] = {(void*)&B->d, (void*)&hin, (void*)&bin, (void*)&hout, (void*)&bout};
+    if (B->seg_grid > 0)  // an empty pool has no segments
+      cudaLaunchKernel(B->seg_fn, dim3((unsigned)B->seg_grid), dim3((unsigned)B->seg_t), args,
+                       (size_t)B->seg_smem, B->stream);
     kb::k_batch_seg_res<<<(unsigned)((B->n + 3) / 4), 128, 0, B->stream>>>(B->d);
     return;
   }
@@ -1238,9 +905,234 @@ extern "C" int kb_batch_step(kb_batch_t* B, int32_t nsteps, double tol, double* 
   return KB_OK;
 }
 
+extern "C" int kb_batch_set_tuning(kb_batch_t* B, const int32_t* params, int32_t n) {
+  if (!B || !params || n < 1) return bfail(KB_ERR_ARG, "kb_batch_set_tuning: null argument");
+  if (B->prec != KB_PREC_FP32) return KB_OK;  // the FP64 comparator has one shape
+  const int seg = params[0] > 0 ? params[0] : 16;
+  const int thr = n > 1 && params[1] > 0 ? params[1] : 128;
+  const int per = n > 2 ? params[2] : 0;
+  return batch_set_shape(B, seg, thr, per);
+}
+
+extern "C" int kb_batch_get_tuning(kb_batch_t* B, int32_t* params, int32_t n) {
+  if (!B || !params) return bfail(KB_ERR_ARG, "kb_batch_get_tuning: null argument");
+  const int32_t v[3] = {B->seg, B->seg_t, B->persist};
+  for (int k = 0; k < n && k < 3; ++k) params[k] = v[k];
+  return KB_OK;
+}
+
 extern "C" int kb_batch_info(kb_batch_t* B, int64_t* elems, int64_t* launches) {
   if (!B) return bfail(KB_ERR_ARG, "kb_batch_info: null handle");
   if (elems) *elems = B->nelem;
   if (launches) *launches = B->launches;
+  return KB_OK;
+}
+
+// ----------------------------------------------------------------- pool
+// Continuous batching of 1D2F1V solves: a pool of instance slots with
+// capacity fixed at creation; a request joins between steps (kb_pool_add
+// places it in free cell / element / velocity ranges, builds its equilibrium
+// state on the device and computes its time step) and leaves between steps
+// (kb_pool_remove frees its ranges); kb_batch_step advances every resident
+// instance with the same fused launch per step.  Only the segment tables and
+// the per-slot scalars change on a join or leave (small host-to-device
+// copies); the step graph is re-captured at the next step.
+
+static long range_alloc(std::map<long, long>& fr, long n) {
+  for (auto it = fr.begin(); it != fr.end(); ++it) {
+    if (it->second >= n) {
+      const long off = it->first, len = it->second;
+      fr.erase(it);
+      if (len > n) fr[off + n] = len - n;
+      return off;
+    }
+  }
+  return -1;
+}
+
+static void range_free(std::map<long, long>& fr, long off, long n) {
+  auto it = fr.emplace(off, n).first;
+  auto nx = std::next(it);
+  if (nx != fr.end() && it->first + it->second == nx->first) {
+    it->second += nx->second;
+    fr.erase(nx);
+  }
+  if (it != fr.begin()) {
+    auto pv = std::prev(it);
+    if (pv->first + pv->second == it->first) {
+      pv->second += it->second;
+      fr.erase(it);
+    }
+  }
+}
+
+extern "C" int kb_pool_create(const kb_config_t* base, int32_t max_instances, int64_t max_cells,
+                              int32_t max_nu, kb_batch_t** out) {
+  if (!base || !out || max_instances < 1 || max_cells < 3 * (int64_t)max_instances || max_nu < 1)
+    return bfail(KB_ERR_ARG, "kb_pool_create: null argument or empty capacity");
+  if (base->dim != 1 || base->nf == 1) return bfail(KB_ERR_CONFIG, "pooled solves are 1D2F1V");
+  if (base->precision != KB_PREC_FP32) return bfail(KB_ERR_CONFIG, "pooled solves use the FP32 split form");
+  if (base->flux != KB_FLUX_KFVS) return bfail(KB_ERR_CONFIG, "pooled solves use KFVS");
+  if (base->bc[0] != KB_BC_FIX || base->bc[1] != KB_BC_FIX)
+    return bfail(KB_ERR_CONFIG, "pooled solves use fixed boundaries");
+  if (max_nu > kb::SEG_MAXNU) return bfail(KB_ERR_CONFIG, "pooled solves have at most 256 velocities");
+  // placeholder instances of max_nu velocities and max_cells cells in all
+  // size the arrays (cells x max_nu distribution values, n x max_nu
+  // velocities); their slots are then released
+  const int n = max_instances;
+  std::vector<int32_t> nx(n, 3), ng(n, 0), nu(n, max_nu);
+  nx[0] = (int32_t)(max_cells - 3 * (int64_t)(n - 1));
+  std::vector<double> x0(n, 0.0), x1(n, 1.0), um(n, 1.0), mu(n, base->mu_ref);
+  std::vector<double> uu((size_t)n * max_nu, 0.0), ww((size_t)n * max_nu, 1.0);
+  kb_config_t c = *base;
+  c.nu = max_nu;
+  kb_batch_t* B = nullptr;
+  int rc = kb_batch_create(&c, n, nx.data(), ng.data(), nu.data(), x0.data(), x1.data(),
+                           um.data(), mu.data(), uu.data(), ww.data(), &B);
+  if (rc != KB_OK) return rc;
+  B->pool = true;
+  B->used.assign(n, 0);
+  B->free_cells[0] = B->ncell;
+  B->free_elems[0] = B->nelem;
+  B->free_vels[0] = B->nvel;
+  B->vel_off_h.assign(n, 0);
+  std::vector<int> zeros(n, 0);
+  cudaMemcpy((void*)B->d.active, zeros.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+  for (int b = 0; b < n; ++b) B->nx[b] = 0;
+  rc = batch_set_shape(B, 16, 128, 1);
+  if (rc != KB_OK) {
+    kb_batch_destroy(B);
+    return rc;
+  }
+  *out = B;
+  return KB_OK;
+}
+
+template <typename T>
+static bool put1(const T* dev, int b, T v) {
+  return cudaMemcpy((void*)(dev + b), &v, sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess;
+}
+
+extern "C" int kb_pool_add(kb_batch_t* B, int32_t nx, int32_t ngx, int32_t nu, double x0, double x1,
+                           double umax, double mu_ref, const double* u, const double* wts,
+                           const double* w, const double* prim, double cfl, int32_t* slot,
+                           double* dt_out) {
+  if (!B || !B->pool || !u || !wts || !w || !prim || !slot) return bfail(KB_ERR_ARG, "kb_pool_add: null argument");
+  if (nx < 3 || ngx < 0 || ngx > 2 || nu < 1 || nu > (int)B->d.nu4_max || !(x1 > x0) || !(cfl > 0.0))
+    return bfail(KB_ERR_CONFIG, "kb_pool_add: invalid instance");
+  int b = -1;
+  for (int k = 0; k < B->n && b < 0; ++k)
+    if (!B->used[k]) b = k;
+  if (b < 0) return bfail(KB_ERR_NOMEM, "kb_pool_add: no free slot");
+  const long nxt = nx + 2 * ngx, nus = (nu + 3) / 4 * 4;
+  const long co = range_alloc(B->free_cells, nxt);
+  const long eo = co < 0 ? -1 : range_alloc(B->free_elems, nxt * nus);
+  const long vo = eo < 0 ? -1 : range_alloc(B->free_vels, nu);
+  if (vo < 0) {
+    if (eo >= 0) range_free(B->free_elems, eo, nxt * nus);
+    if (co >= 0) range_free(B->free_cells, co, nxt);
+    return bfail(KB_ERR_NOMEM, "kb_pool_add: the pool's cell or velocity capacity is used up");
+  }
+  cudaStreamSynchronize(B->stream);
+  B->used[b] = 1;
+  B->nx[b] = nx;
+  B->ng[b] = ngx;
+  B->nu[b] = nu;
+  B->nus[b] = (int)nus;
+  B->cell_off[b] = co;
+  B->elem_off[b] = eo;
+  B->vel_off_h[b] = vo;
+  const double dx = (x1 - x0) / nx;
+  bool ok = put1(B->d.nx, b, (int)nx) && put1(B->d.ng, b, (int)ngx) && put1(B->d.nu, b, (int)nu) &&
+            put1(B->d.nus, b, (int)nus) && put1(B->d.cell_off, b, co) && put1(B->d.elem_off, b, eo) &&
+            put1(B->d.vel_off, b, (int)vo) && put1(B->d.dx, b, dx) && put1(B->d.mu, b, mu_ref) &&
+            put1((const double*)B->d_umax, b, umax);
+  std::vector<float> uf(nu), ul(nu), wf(nu);
+  for (int k = 0; k < nu; ++k) {
+    uf[k] = float(u[k]);
+    ul[k] = float(u[k] - (double)uf[k]);
+    wf[k] = float(wts[k]);
+  }
+  ok &= cudaMemcpy((void*)(B->d.u + vo), u, sizeof(double) * nu, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy((void*)(B->d.wt + vo), wts, sizeof(double) * nu, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy((void*)(B->d.uf + vo), uf.data(), sizeof(float) * nu, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy((void*)(B->d.ul + vo), ul.data(), sizeof(float) * nu, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy((void*)(B->d.wtf + vo), wf.data(), sizeof(float) * nu, cudaMemcpyHostToDevice) == cudaSuccess;
+  std::vector<double> w4(nxt * 4, 0.0), p4(nxt * 4, 0.0);
+  for (long c = 0; c < nxt; ++c)
+    for (int k = 0; k < 3; ++k) {
+      w4[c * 4 + k] = w[c * 3 + k];
+      p4[c * 4 + k] = prim[c * 3 + k];
+    }
+  ok &= cudaMemcpy(B->d.w + co * 4, w4.data(), sizeof(double) * w4.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+  ok &= cudaMemcpy(B->d.prim + co * 4, p4.data(), sizeof(double) * p4.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+  if (!ok) return bfail(KB_ERR_CUDA, "kb_pool_add: copy failed");
+  kb::k_batch_init_eq32<<<dim3((unsigned)nxt, 1), 128, 0, B->stream>>>(
+      B->d, b, (float*)B->h[0], (float*)B->bq[0], (float*)B->h[1], (float*)B->bq[1]);
+  kb::k_batch_timestep<<<1, 256, 0, B->stream>>>(B->d, B->d_umax, cfl, (double*)B->d.dt, b);
+  B->launches += 2;
+  double dt = 0.0;
+  ok &= cudaStreamSynchronize(B->stream) == cudaSuccess;
+  ok &= cudaMemcpy(&dt, B->d.dt + b, sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess;
+  ok &= put1((const int*)B->d.active, b, 1);
+  const double zero4[4] = {0, 0, 0, 0};
+  ok &= cudaMemcpy(B->d.residual + (long)b * 4, zero4, sizeof(zero4), cudaMemcpyHostToDevice) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    return bfail(KB_ERR_CUDA, "kb_pool_add: device set-up failed");
+  }
+  int rc = batch_set_shape(B, B->seg, B->seg_t, B->persist);
+  if (rc != KB_OK) return rc;
+  *slot = b;
+  if (dt_out) *dt_out = dt;
+  return KB_OK;
+}
+
+extern "C" int kb_pool_remove(kb_batch_t* B, int32_t slot) {
+  if (!B || !B->pool || slot < 0 || slot >= B->n || !B->used[slot])
+    return bfail(KB_ERR_ARG, "kb_pool_remove: no such slot");
+  cudaStreamSynchronize(B->stream);
+  const long nxt = B->nx[slot] + 2 * B->ng[slot];
+  range_free(B->free_cells, B->cell_off[slot], nxt);
+  range_free(B->free_elems, B->elem_off[slot], nxt * B->nus[slot]);
+  range_free(B->free_vels, B->vel_off_h[slot], B->nu[slot]);
+  B->used[slot] = 0;
+  B->nx[slot] = 0;
+  if (!put1((const int*)B->d.active, slot, 0)) return bfail(KB_ERR_CUDA, "kb_pool_remove: copy failed");
+  return batch_set_shape(B, B->seg, B->seg_t, B->persist);
+}
+
+extern "C" int kb_pool_download(kb_batch_t* B, int32_t slot, double* w, double* prim, double* h,
+                                double* bq) {
+  if (!B || !B->pool || slot < 0 || slot >= B->n || !B->used[slot])
+    return bfail(KB_ERR_ARG, "kb_pool_download: no such slot");
+  cudaStreamSynchronize(B->stream);
+  const long nxt = B->nx[slot] + 2 * B->ng[slot], co = B->cell_off[slot];
+  const int nu = B->nu[slot], nus = B->nus[slot];
+  bool ok = true;
+  if (w || prim) {
+    std::vector<double> a4(nxt * 4);
+    for (int which = 0; which < 2; ++which) {
+      double* dst = which == 0 ? w : prim;
+      if (!dst) continue;
+      ok &= cudaMemcpy(a4.data(), (which == 0 ? B->d.w : B->d.prim) + co * 4, sizeof(double) * a4.size(),
+                       cudaMemcpyDeviceToHost) == cudaSuccess;
+      for (long c = 0; c < nxt; ++c)
+        for (int k = 0; k < 3; ++k) dst[c * 3 + k] = a4[c * 4 + k];
+    }
+  }
+  const long ne = nxt * nus, eo = B->elem_off[slot];
+  std::vector<double> stage(ne);
+  for (int which = 0; which < 2; ++which) {
+    double* dst = which == 0 ? h : bq;
+    if (!dst) continue;
+    const float* src = (const float*)(which == 0 ? B->h[B->cur] : B->bq[B->cur]) + eo;
+    kb::k_batch_back<float><<<(unsigned)((ne + 255) / 256), 256, 0, B->stream>>>(B->d_stage, src, ne);
+    B->launches++;
+    ok &= cudaStreamSynchronize(B->stream) == cudaSuccess;
+    ok &= cudaMemcpy(stage.data(), B->d_stage, sizeof(double) * ne, cudaMemcpyDeviceToHost) == cudaSuccess;
+    for (long c = 0; c < nxt; ++c) std::memcpy(dst + c * nu, &stage[c * nus], sizeof(double) * nu);
+  }
+  if (!ok) return bfail(KB_ERR_CUDA, "kb_pool_download: copy failed");
   return KB_OK;
 }

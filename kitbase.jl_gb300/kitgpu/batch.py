@@ -22,11 +22,14 @@ _BATCH_SIGS = {
     "kb_batch_destroy": [ctypes.c_void_p],
     "kb_batch_upload": [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_double)] * 4,
     "kb_batch_download": [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_double)] * 4,
+    "kb_batch_init_equilibrium": [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_double)] * 2,
     "kb_batch_timestep": [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ctypes.c_double)],
     "kb_batch_set_dt": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)],
     "kb_batch_step": [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
                       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int32)],
     "kb_batch_info": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)],
+    "kb_batch_set_tuning": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32],
+    "kb_batch_get_tuning": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32],
 }
 
 
@@ -85,6 +88,7 @@ class Batch:
         if not self.KS:
             raise ValueError("empty batch")
         base = kb_config(self.KS[0], precision)
+        self.prec = precision
         self.n = len(self.KS)
         nx = np.array([K.ps.nx for K in self.KS], dtype=np.int32)
         ng = np.array([K.ps.ng for K in self.KS], dtype=np.int32)
@@ -135,14 +139,28 @@ class Batch:
         self.active[:] = 1
         return w, p, h, b
 
+    def init_initial(self):
+        """init_fvm's equilibrium state of every instance, h and b built on
+        the device (kb_batch_init_equilibrium): only w and prim cross the bus,
+        and the FP32 split form starts from its own FP32 Maxwellian."""
+        from .solver import initial_cells
+        parts = [initial_cells(K) for K in self.KS]
+        w = np.ascontiguousarray(np.concatenate([p[0] for p in parts]))
+        p = np.ascontiguousarray(np.concatenate([p[1] for p in parts]))
+        N.check(self.lib.kb_batch_init_equilibrium(self.h, N.ptr(w), N.ptr(p)))
+        self.active[:] = 1
+        return w, p
+
     def timestep(self):
         dt = np.zeros(self.n)
         N.check(self.lib.kb_batch_timestep(self.h, float(self.KS[0].set.cfl), N.ptr(dt)))
+        self.dt = dt
         return dt
 
     def set_dt(self, dt):
         dt = np.ascontiguousarray(dt, dtype=np.float64)
         N.check(self.lib.kb_batch_set_dt(self.h, N.ptr(dt)))
+        self.dt = dt
 
     def step(self, nsteps, tol=0.0):
         act = np.zeros(self.n, dtype=np.int32)
@@ -157,6 +175,15 @@ class Batch:
         while self.steps < max_steps and self.active.any():
             self.step(min(chunk, max_steps - self.steps), tol)
         return int(self.active.sum())
+
+    def upload(self, states):
+        """Per-instance states (dicts with w, prim, h, b as download() returns)."""
+        w = np.ascontiguousarray(np.concatenate([x["w"] for x in states]))
+        p = np.ascontiguousarray(np.concatenate([x["prim"] for x in states]))
+        h = np.ascontiguousarray(np.concatenate([x["h"].ravel() for x in states]))
+        b = np.ascontiguousarray(np.concatenate([x["b"].ravel() for x in states]))
+        N.check(self.lib.kb_batch_upload(self.h, N.ptr(w), N.ptr(p), N.ptr(h), N.ptr(b)))
+        self.active[:] = 1
 
     def download(self):
         ncell = int(self.cell_off[-1])
@@ -175,6 +202,17 @@ class Batch:
                             b=b[e0:e1].reshape(-1, nuk)))
         return out
 
+    def set_tuning(self, seg=16, threads=128, persist=0):
+        """Shape of the FP32 step kernel: cells per segment, threads per CTA,
+        persistent grid (kb_batch_set_tuning)."""
+        arr = (ctypes.c_int32 * 3)(int(seg), int(threads), int(persist))
+        N.check(self.lib.kb_batch_set_tuning(self.h, arr, 3))
+
+    def tuning(self):
+        arr = (ctypes.c_int32 * 3)()
+        N.check(self.lib.kb_batch_get_tuning(self.h, arr, 3))
+        return dict(seg=arr[0], threads=arr[1], persist=arr[2])
+
     def launches(self):
         e, l = ctypes.c_int64(), ctypes.c_int64()
         N.check(self.lib.kb_batch_info(self.h, ctypes.byref(e), ctypes.byref(l)))
@@ -182,3 +220,120 @@ class Batch:
 
     def cell_velocity_points(self):
         return int(np.sum(self.nx.astype(np.int64) * self.nu))
+
+
+_POOL_SIGS = {
+    "kb_pool_create": [ctypes.POINTER(N.KbConfig), ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                       ctypes.POINTER(ctypes.c_void_p)],
+    "kb_pool_add": [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                    ctypes.c_double, ctypes.c_double, ctypes.c_double] + [ctypes.POINTER(ctypes.c_double)] * 4
+    + [ctypes.c_double, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)],
+    "kb_pool_remove": [ctypes.c_void_p, ctypes.c_int32],
+    "kb_pool_download": [ctypes.c_void_p, ctypes.c_int32] + [ctypes.POINTER(ctypes.c_double)] * 4,
+}
+
+
+def _pool_lib():
+    lib = _lib()
+    for name, args in _POOL_SIGS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    return lib
+
+
+def poolable(KS):
+    """A solve the pool can hold: 1D2F1V, KFVS, fixed boundaries, van Leer,
+    at most 256 velocities (the batch kernel's coverage)."""
+    return (KS.dim == 1 and KS.nf == 2 and KS.set.flux == "kfvs" and KS.vs.nu <= 256
+            and list(KS.set.boundary)[:2] == ["fix", "fix"] and KS.set.interpOrder == 2)
+
+
+def pool_key(KS):
+    """Gas constants and collision model a pool's instances share."""
+    g = KS.gas
+    return (g.K, g.gamma, g.omega, g.Pr, KS.set.collision)
+
+
+class Pool:
+    """Continuous batching of 1D solves (kb_pool_*): a resident FP32-split
+    batch with fixed capacity that solves join (`add`) and leave (`remove`)
+    between steps; `step` advances every resident solve with one fused launch
+    per step (two steps per replayed CUDA graph)."""
+
+    def __init__(self, base_KS, max_instances=64, max_cells=64 * 2052, max_nu=256):
+        self.lib = _pool_lib()
+        self.key = pool_key(base_KS)
+        cfg = kb_config(base_KS, "fp32")
+        self.n = int(max_instances)
+        h = ctypes.c_void_p()
+        N.check(self.lib.kb_pool_create(ctypes.byref(cfg), self.n, int(max_cells), int(max_nu),
+                                        ctypes.byref(h)))
+        self.h = h
+        self.max_cells = int(max_cells)
+        self.slots = {}  # slot -> KS
+        self.residual = np.zeros((self.n, 4))
+        self.active = np.zeros(self.n, dtype=np.int32)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.kb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, KS):
+        """Place one solve (its init_fvm equilibrium state); returns (slot, dt)."""
+        from .solver import initial_cells
+        if pool_key(KS) != self.key or not poolable(KS):
+            raise ValueError("this solve does not fit the pool")
+        w, p = initial_cells(KS)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        u = np.ascontiguousarray(KS.vs.u, dtype=np.float64)
+        wt = np.ascontiguousarray(KS.vs.weights, dtype=np.float64)
+        slot, dt = ctypes.c_int32(), ctypes.c_double()
+        N.check(self.lib.kb_pool_add(self.h, KS.ps.nx, KS.ps.ng, KS.vs.nu, KS.ps.x0, KS.ps.x1,
+                                     KS.vs.u1, KS.gas.mu_ref, N.ptr(u), N.ptr(wt), N.ptr(w),
+                                     N.ptr(p), float(KS.set.cfl), ctypes.byref(slot),
+                                     ctypes.byref(dt)))
+        self.slots[slot.value] = KS
+        self.active[slot.value] = 1
+        return slot.value, dt.value
+
+    def remove(self, slot):
+        N.check(self.lib.kb_pool_remove(self.h, int(slot)))
+        self.slots.pop(int(slot), None)
+        self.active[slot] = 0
+
+    def download(self, slot, want=("w", "prim", "h", "b")):
+        KS = self.slots[int(slot)]
+        nc = KS.ps.nx + 2 * KS.ps.ng
+        out = {k: (np.zeros((nc, 3)) if k in ("w", "prim") else np.zeros((nc, KS.vs.nu)))
+               for k in want}
+        N.check(self.lib.kb_pool_download(self.h, int(slot), N.ptr(out.get("w")),
+                                          N.ptr(out.get("prim")), N.ptr(out.get("h")),
+                                          N.ptr(out.get("b"))))
+        return out
+
+    def step(self, nsteps, tol=0.0):
+        """nsteps steps of every resident solve; a solve whose residual falls
+        below tol stops (state carried).  Returns the residuals [n][3]."""
+        act = np.zeros(self.n, dtype=np.int32)
+        N.check(self.lib.kb_batch_step(self.h, int(nsteps), float(tol), N.ptr(self.residual),
+                                       act.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+        self.active = act
+        return self.residual[:, :3]
+
+    def set_tuning(self, seg=16, threads=128, persist=1):
+        arr = (ctypes.c_int32 * 3)(int(seg), int(threads), int(persist))
+        N.check(self.lib.kb_batch_set_tuning(self.h, arr, 3))
+
+    def launches(self):
+        e, l = ctypes.c_int64(), ctypes.c_int64()
+        N.check(self.lib.kb_batch_info(self.h, ctypes.byref(e), ctypes.byref(l)))
+        return l.value

@@ -1,13 +1,19 @@
 """Continuous-batching service for a stream of DVM solves.
 
-Requests arrive over time (Poisson); each admitted request owns a libkitgpu
-handle with its own CUDA stream, so the steps of all resident requests run
-concurrently on the GPU.  The loop admits queued requests whenever a slot and
-the HBM budget allow, enqueues a chunk of steps for every resident request
-(kb_step_async), polls completions (kb_query) and retires a request when its
-residual (reference definition, src/Solver/solver_update.jl:86-88) falls below
-the tolerance or it reaches its step limit; its final state is downloaded and
-its memory returned to the budget before the next admission.
+Requests arrive over time (Poisson).  1D requests that the batch kernel
+covers (1D2F1V, KFVS, fixed boundaries) join a resident pool (batch.Pool,
+kb_pool_*): one fused launch per step advances every resident 1D request,
+requests join and leave between chunks of steps, and a request's result does
+not depend on who else shares the launch.  Every other request (the 2D
+cavities) owns a libkitgpu handle with its own CUDA stream, so its steps run
+concurrently with the pool and with each other.  The loop admits queued
+requests whenever a slot and the HBM budget allow, advances the pool by a
+chunk, enqueues a chunk for every idle handle (kb_step_async), polls
+completions (kb_query) and retires a request when its residual (reference
+definition, src/Solver/solver_update.jl:86-88) falls below the tolerance or
+it reaches its step limit; its final state is downloaded and its memory
+returned to the budget before the next admission.  A request's step limit
+should be a multiple of the chunk: steps are counted in whole chunks.
 
 The mixed stream: 60 % 1D Sod tubes (cells log-uniform in [64, 2048],
 velocities in [32, 256]) and 40 % 2D lid-driven cavities (cells log-uniform
@@ -20,6 +26,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import batch as KBATCH
 from .setup import solver_set
 from .solver import Handle, initial_cells, kb_config, wall_states
 
@@ -95,36 +102,82 @@ def estimate_bytes(cfg, precision):
     return 4 * ncell * ((nvel + 3) // 4 * 4) * esz + ncell * 1024 + nface * 512 + (1 << 20)
 
 
+def pool_bytes(max_cells, max_nu=256):
+    """Device bytes of a 1D pool: FP32 h, b (two buffers each) and the FP64
+    staging array over max_cells x max_nu values, plus per-cell state."""
+    return max_cells * max_nu * (4 * 4 + 8) + max_cells * 512 + (8 << 20)
+
+
 @dataclass
 class Server:
     precision: str = "fp32"
     hbm_budget: int = 64 << 30
     max_slots: int = 64
     chunk: int = 20
+    pool_1d: bool = True          # 1D requests share one fused launch (FP32 only)
+    pool_cells: int = None        # cell capacity of the pool; None: from the HBM budget
     done: list = field(default_factory=list)
 
     def run(self, requests, time_scale=1.0, keep_results=False, on_retire=None):
         """Serve `requests` (sorted by arrival).  Arrival times are honoured in
         wall time divided by time_scale.  Returns summary metrics."""
         pending = sorted(requests, key=lambda r: r.arrival)
-        queue, active = [], []
+        if self.pool_cells is None:  # a quarter of the budget, at most 64 slots of 2048 cells
+            self.pool_cells = int(min(self.max_slots * 2052,
+                                      max(4096, self.hbm_budget // 4 // (256 * 24))))
+        queue, active, pooled = [], [], []
         used = 0
+        pool = None
+        self.pool_launches = 0
         t0 = time.perf_counter()
         cv_total = 0
         i = 0
-        while i < len(pending) or queue or active:
+
+        def retire(r, state):
+            nonlocal used
+            r.finished = (time.perf_counter() - t0) * time_scale
+            if keep_results:
+                r.result = state
+            self.done.append(r)
+            if on_retire:
+                on_retire(r)
+
+        while i < len(pending) or queue or active or pooled:
             now = (time.perf_counter() - t0) * time_scale
             while i < len(pending) and pending[i].arrival <= now:
                 queue.append(pending[i])
                 i += 1
             # admission: FIFO while a slot and the HBM budget allow
-            while queue and len(active) < self.max_slots:
+            while queue and len(active) + len(pooled) < self.max_slots:
                 r = queue[0]
+                KS = solver_set(r.config)
+                use_pool = (self.pool_1d and self.precision == "fp32" and KBATCH.poolable(KS)
+                            and (pool is None or KBATCH.pool_key(KS) == pool.key)
+                            and KS.ps.nx + 2 * KS.ps.ng <= self.pool_cells)
+                if use_pool and pool is None:
+                    need = pool_bytes(self.pool_cells)
+                    if used + need > self.hbm_budget and (active or pooled):
+                        break
+                    pool = KBATCH.Pool(KS, max_instances=self.max_slots, max_cells=self.pool_cells)
+                    used += need
+                if use_pool:
+                    try:
+                        r.slot, r.dt = pool.add(KS)
+                    except Exception:
+                        if not pooled:
+                            raise
+                        break  # pool capacity used up: wait for a retirement
+                    queue.pop(0)
+                    r.handle = None
+                    r.bytes = 0
+                    r.cv_per_step = KS.ps.nx * KS.vs.nu
+                    r.admitted = (time.perf_counter() - t0) * time_scale
+                    pooled.append(r)
+                    continue
                 need = estimate_bytes(r.config, self.precision)
-                if used + need > self.hbm_budget and active:
+                if used + need > self.hbm_budget and (active or pooled):
                     break
                 queue.pop(0)
-                KS = solver_set(r.config)
                 vs = KS.vs
                 if KS.dim == 1:
                     h = Handle(kb_config(KS, self.precision), vs.u, None, vs.weights)
@@ -146,13 +199,31 @@ class Server:
                 used += need
                 active.append(r)
                 r.inflight = 0
-            # enqueue a chunk for every idle resident request
+            # enqueue a chunk for every idle resident handle
             for r in active:
                 if r.inflight == 0:
                     n = min(self.chunk, r.max_steps - r.steps)
                     r.handle.step_async(r.dt, n)
                     r.inflight = n
-            # poll completions
+            # one chunk of the pool: every resident 1D request in each launch
+            if pooled:
+                n = self.chunk
+                l0 = pool.launches()
+                res = pool.step(n, min(r.tol for r in pooled))
+                self.pool_launches += pool.launches() - l0
+                still = []
+                for r in pooled:
+                    r.steps += n
+                    cv_total += n * r.cv_per_step
+                    r.residual = res[r.slot].copy()
+                    if r.steps >= r.max_steps or float(np.max(r.residual)) < r.tol:
+                        state = pool.download(r.slot, ("w", "prim")) if keep_results else None
+                        pool.remove(r.slot)
+                        retire(r, state)
+                    else:
+                        still.append(r)
+                pooled = still
+            # poll completions of the handles
             still = []
             for r in active:
                 ready, res = r.handle.query()
@@ -164,28 +235,26 @@ class Server:
                 r.inflight = 0
                 r.residual = res
                 if r.steps >= r.max_steps or float(np.max(res)) < r.tol:
-                    if keep_results:
-                        r.result = r.handle.download(("w", "prim"))
-                    r.finished = (time.perf_counter() - t0) * time_scale
+                    state = r.handle.download(("w", "prim")) if keep_results else None
                     r.handle.close()
                     r.handle = None
                     used -= r.bytes
-                    self.done.append(r)
-                    if on_retire:
-                        on_retire(r)
+                    retire(r, state)
                 else:
                     still.append(r)
             active = still
-            if not active and not queue and i < len(pending):
+            if not active and not pooled and not queue and i < len(pending):
                 # idle until the next arrival
                 wait = (pending[i].arrival - now) / time_scale
                 if wait > 0:
                     time.sleep(min(wait, 0.01))
         wall = time.perf_counter() - t0
+        if pool is not None:
+            pool.close()
         lat = np.array([r.latency for r in self.done if r.latency is not None]) / time_scale
         return dict(requests=len(self.done), wall_s=wall, cv_updates=cv_total,
                     throughput=cv_total / wall if wall > 0 else 0.0,
                     p50_s=float(np.percentile(lat, 50)) if len(lat) else None,
                     p99_s=float(np.percentile(lat, 99)) if len(lat) else None,
                     precision=self.precision, max_slots=self.max_slots,
-                    hbm_budget=self.hbm_budget)
+                    hbm_budget=self.hbm_budget, pool_launches=self.pool_launches)

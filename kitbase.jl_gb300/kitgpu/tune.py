@@ -95,3 +95,51 @@ def autotune(handle, dt, steps=2, use_cache=True, verbose=False):
     timings = {"march": {"tx%d-bs%d-ry%d" % k: v for k, v in res_march.items()},
                "moments": {"ts%d" % k: v for k, v in res_mom.items()}}
     return best, timings
+
+
+# Shapes of the fused FP32 batch step kernel (kb_batch_set_tuning): cells per
+# segment x threads per CTA, each with one CTA per segment or a persistent
+# grid of as many CTAs as fit on the GPU.
+BATCH_SHAPES = ((8, 64), (16, 64), (16, 128), (16, 256), (32, 128), (32, 256))
+BATCH_PERSIST = (0, 1)
+
+
+def batch_signature(batch):
+    n = batch.n
+    cv = batch.cell_velocity_points()
+    size = "small" if cv < 1 << 20 else ("medium" if cv < 1 << 24 else "large")
+    return "batch-n%d-nu%d-c%s-%s" % (n, int(batch.nu.max()), batch.KS[0].set.collision, size)
+
+
+def autotune_batch(batch, steps=100, use_cache=True, verbose=False):
+    """Pick the fastest shape of the FP32 batch step for `batch` by timing
+    `steps` graph-replayed steps of each candidate on the live state
+    (kb_batch_step returns after synchronising the batch's stream; the search
+    advances the state).  Returns the chosen dict and the per-candidate ms
+    per step."""
+    import time
+    if batch.prec != "fp32":
+        return None, None
+    key = batch_signature(batch)
+    cache = _load() if use_cache else {}
+    if use_cache and key in cache:
+        best = cache[key]
+        batch.set_tuning(**best)
+        return best, None
+    res = {}
+    for (seg, thr), per in itertools.product(BATCH_SHAPES, BATCH_PERSIST):
+        batch.set_tuning(seg=seg, threads=thr, persist=per)
+        batch.step(4)  # graph capture of this shape, warm-up
+        t0 = time.perf_counter()
+        batch.step(steps)
+        res[(seg, thr, per)] = 1e3 * (time.perf_counter() - t0) / steps
+        if verbose:
+            print("batch seg=%d threads=%d persist=%d: %.4f ms" % (seg, thr, per, res[(seg, thr, per)]),
+                  flush=True)
+    seg, thr, per = min(res, key=res.get)
+    best = dict(seg=seg, threads=thr, persist=per)
+    batch.set_tuning(**best)
+    if use_cache:
+        cache[key] = best
+        _save(cache)
+    return best, {"seg%d-t%d-p%d" % k: v for k, v in res.items()}

@@ -38,3 +38,57 @@ def test_admission_respects_budget(gpu_lib):
     m = srv.run(reqs, on_retire=on_retire)
     assert m["requests"] == len(reqs)
     assert all(r.finished >= r.admitted >= r.arrival - 1e-9 for r in srv.done)
+
+
+def test_pooled_1d_requests_share_launches(gpu_lib):
+    """The 1D requests of a stream are advanced together by the pool's fused
+    launches: far fewer pool launches than pooled request-steps."""
+    reqs = S.mixed_stream(rate=400.0, duration=0.05, seed=11, max_steps=40, tol=1e-12, scale=0.08)
+    n1d = sum(1 for r in reqs if r.config["space"] == "1d2f1v")
+    assert n1d >= 3
+    srv = S.Server(precision="fp32", max_slots=8, chunk=8, hbm_budget=1 << 30)
+    m = srv.run(reqs)
+    assert m["requests"] == len(reqs)
+    assert 0 < m["pool_launches"] < n1d * 40 * 2
+
+
+def test_pool_join_leave_and_accuracy(gpu_lib):
+    """Solves join a pool while others run and leave it: each result equals
+    the same solve alone in a pool bit for bit, stays within 1e-5 of the
+    plain FP64 single solve (rho, U, T), and freed slots are reused."""
+    from kitgpu import batch as KB
+    from cases import rho_u_t_error, sod
+    cfgs = [sod(nx=60, nu=40), sod(nx=37, nu=33), sod(nx=90, nu=64), sod(nx=16, nu=7)]
+    sets = [kitgpu.solver_set(c) for c in cfgs]
+
+    def alone(KS, n):
+        p = KB.Pool(KS, max_instances=1, max_cells=256)
+        slot, dt = p.add(KS)
+        p.step(n)
+        out = p.download(slot)
+        p.close()
+        return out, dt
+
+    pool = KB.Pool(sets[0], max_instances=3, max_cells=256)
+    s0, dt0 = pool.add(sets[0])
+    pool.step(10)
+    s1, dt1 = pool.add(sets[1])      # joins a running pool
+    pool.step(10)
+    a0 = pool.download(s0)
+    pool.remove(s0)                  # leaves; its ranges are reused below
+    s2, dt2 = pool.add(sets[2])
+    s3, dt3 = pool.add(sets[3])
+    pool.step(20)
+    a1, a2, a3 = pool.download(s1), pool.download(s2), pool.download(s3)
+    for (got, KS, n, dt) in ((a0, sets[0], 20, dt0), (a1, sets[1], 30, dt1), (a2, sets[2], 20, dt2),
+                             (a3, sets[3], 20, dt3)):
+        ref, dtr = alone(KS, n)
+        assert dtr == dt
+        for k in ("w", "prim", "h", "b"):
+            assert np.array_equal(got[k], ref[k]), k
+        ctr, face = kitgpu.init_fvm(KS, "fp64")
+        assert kitgpu.timestep(KS, ctr, 0.0) == pytest.approx(dt, rel=1e-14)
+        ctr.handle.step(dt, n)
+        single = ctr.handle.download()
+        assert max(rho_u_t_error(got["prim"], single["prim"])) < 1e-5
+    pool.close()
