@@ -522,7 +522,7 @@ def batch_block(args, peak):
         bt = KB.Batch(sets, prec)
         bt.init_initial()
         bt.timestep()
-        tuned = None
+        tuned, timings = None, None
         if prec == "fp32":
             # kernel shape from the project autotuner (the search advances
             # the state, so the batch restarts from its initial state)
@@ -561,6 +561,8 @@ def batch_block(args, peak):
                                      "unconverged": left, "instances": bt.n,
                                      "below_1e-6": int(np.sum(r < 1e-6))}
             out["fp32"]["tuning"] = bt.tuning()
+            if timings:
+                out["fp32"]["tuning_ms_per_step"] = timings
         bt.close()
     # steady convergence of both forms on the same sample of instances and
     # step cap: the rate of approach to the steady shock, not the storage
