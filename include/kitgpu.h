@@ -312,6 +312,38 @@ int kb_pool_remove(kb_batch_t* b, int32_t slot);
 int kb_pool_download(kb_batch_t* b, int32_t slot, double* w, double* prim, double* hdist,
                      double* bdist);
 
+/* ----------------------------------------------------------- unstructured
+ * 2D2F2V on a triangle mesh: evolve! US2F (src/Solver/solver_evolution.jl:
+ * 945-1035), update! US2F (src/Solver/solver_update.jl:414-471) with the
+ * triangle step! (src/Solver/step_2f.jl:256-326), update_boundary! US2F
+ * (src/Solver/update_boundary.jl:575-594) and the unstructured timestep
+ * (src/Solver/solver_main.jl:398-420).  First-order KFVS, BGK or Shakhov,
+ * FP64 or the FP32 split form; cfg supplies dim = 2, nu, nv, collision,
+ * precision, umax, vmax and the gas (K, gamma, mu_ref, omega, Pr), with
+ * flux = KFVS and interp_order = 1 (other choices: KB_ERR_CONFIG).  Mesh
+ * arrays (0-based): face_cells [nface][2] (-1: no cell), cell_faces and
+ * cell_neighbors [ncell][3], cell_type [ncell] (0 stepped, 1 fixed, 3 set to
+ * the mean of its two neighbours after each step; 2, a Maxwell wall cell, is
+ * refused: the reference's call for it matches no method), face normals
+ * [nface][2] pointing from the first to the second cell, face lengths, cell
+ * areas and the smallest centre-to-edge distance of each cell; u, v, weights
+ * the velocity grid (nu*nv).  State: w, prim [ncell][4], h, b [ncell][nu*nv]. */
+typedef struct kb_us kb_us_t;
+int kb_us_create(const kb_config_t* cfg, int32_t ncell, int32_t nface, const int32_t* face_cells,
+                 const int32_t* cell_faces, const int32_t* cell_neighbors, const int32_t* cell_type,
+                 const double* face_n, const double* face_len, const double* cell_area,
+                 const double* cell_mindx, const double* u, const double* v,
+                 const double* weights, kb_us_t** out);
+int kb_us_destroy(kb_us_t* us);
+int kb_us_upload(kb_us_t* us, const double* w, const double* prim, const double* hdist,
+                 const double* bdist);
+int kb_us_download(kb_us_t* us, double* w, double* prim, double* hdist, double* bdist);
+int kb_us_timestep(kb_us_t* us, double cfl, double sim_time, double max_time, double* dt_out);
+/* nsteps steps with a fixed dt; residual (host, 4 doubles, may be NULL)
+ * receives the last step's residual (src/Solver/solver_update.jl:465-467). */
+int kb_us_step(kb_us_t* us, double dt, int32_t nsteps, double* residual);
+int kb_us_info(kb_us_t* us, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,7 +33,8 @@ def test_library_exports_every_declared_symbol():
 
 def test_signatures_cover_header():
     from kitgpu import batch
-    known = set(N.SIGNATURES) | set(batch._BATCH_SIGS) | set(batch._POOL_SIGS)
+    from kitgpu import unstruct
+    known = set(N.SIGNATURES) | set(batch._BATCH_SIGS) | set(batch._POOL_SIGS) | set(unstruct._US_SIGS)
     for name in header_symbols():
         if name in ("kb_version", "kb_last_error"):
             continue

@@ -1,0 +1,91 @@
+"""Unstructured meshes on the host (no GPU): gmsh 4.1 round trip, the
+connectivity and geometry kitgpu builds against the oracle's independent
+construction, and the configurations the device solver refuses before any
+CUDA call."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from kitgpu import _native as N
+from kitgpu import unstruct as US
+import oracle_us as OU
+
+
+def test_gmsh_round_trip(tmp_path):
+    P, T = US.rectangle_mesh(5, 4, jitter=0.2)
+    path = str(tmp_path / "m.msh")
+    US.write_gmsh(path, P, T)
+    P2, T2 = US.read_gmsh(path)
+    assert np.array_equal(P2, P) and np.array_equal(T2, T)
+
+
+@pytest.mark.parametrize("bc", ["fix", "extra"])
+def test_connectivity_and_geometry(bc):
+    P, T = US.rectangle_mesh(7, 5, x1=2.0, jitter=0.25)
+    m = US.build_mesh(P, T, boundary=bc)
+    nbf = int((m.face_cells[:, 1] == -1).sum())
+    assert nbf == 2 * (7 + 5)
+    assert m.nface == (3 * m.ncell + nbf) // 2
+    assert abs(m.cell_area.sum() - 2.0) < 1e-12
+    for f in range(m.nface):  # normals point from the first to the second cell
+        c1, c2 = m.face_cells[f]
+        if c2 >= 0:
+            assert m.face_n[f] @ (m.cell_center[c2] - m.cell_center[c1]) > 0
+    # closed cells: the oriented face normals times lengths sum to ~0 (the
+    # normals are (|d| + 1e-6)-scaled, as the reference's unit_normal)
+    for c in range(m.ncell):
+        s = np.zeros(2)
+        for j in range(3):
+            f = m.cell_faces[c, j]
+            sg = 1.0 if (m.face_cells[f, 0] == c and m.face_cells[f, 1] != -1) else -1.0
+            s += sg * m.face_n[f] * m.face_len[f]
+        assert np.abs(s).max() < 1e-5
+    nn = (m.cell_neighbors != -1).sum(axis=1)
+    if bc == "fix":
+        assert np.array_equal(m.cell_type, np.where(nn < 3, 1, 0))
+    else:  # single-neighbour corners stay fixed: the two-neighbour mean needs two
+        assert np.array_equal(m.cell_type, np.select([nn < 2, nn == 2], [1, 3], 0))
+    # the oracle's own construction agrees cell by cell
+    o = OU.UnstructOracle(P, T, m.cell_type, [0.0], [0.0], [1.0], 1.0, 5 / 3, 1e-3, 0.72, 1.0, "bgk")
+    assert np.allclose(o.area, m.cell_area, rtol=1e-15, atol=0)
+    assert np.allclose(o.center, m.cell_center, rtol=1e-15, atol=1e-15)
+    assert np.allclose(o.dx.min(axis=1), m.cell_dx.min(axis=1), rtol=1e-14)
+    for c in range(m.ncell):
+        for j in range(3):
+            f = m.cell_faces[c, j]
+            sg = 1.0 if (m.face_cells[f, 0] == c and m.face_cells[f, 1] != -1) else -1.0
+            assert o.dirc[c, j] == sg
+
+
+def _create(mesh, cell_type=None, **kw):
+    lib = US._lib()
+    c = N.KbConfig()
+    c.dim, c.nx, c.ny, c.nu, c.nv = 2, mesh.ncell, 1, 4, 4
+    c.flux, c.collision, c.interp_order, c.precision = 0, 0, 1, 0
+    c.K, c.gamma, c.mu_ref, c.omega, c.Pr = 1.0, 5 / 3, 1e-3, 0.72, 1.0
+    for k, v in kw.items():
+        setattr(c, k, v)
+    keep = US.mesh_arrays(mesh)
+    if cell_type is not None:
+        keep[3] = np.ascontiguousarray(cell_type, dtype=np.int32)
+    vel = [np.zeros(16), np.zeros(16), np.ones(16)]
+    P = ctypes.POINTER(ctypes.c_int32)
+    h = ctypes.c_void_p()
+    return lib.kb_us_create(ctypes.byref(c), mesh.ncell, mesh.nface,
+                            *[a.ctypes.data_as(P) for a in keep[:4]],
+                            *[N.ptr(a) for a in keep[4:] + vel], ctypes.byref(h))
+
+
+@pytest.mark.parametrize("kw", [dict(interp_order=2), dict(flux=1), dict(flux=2), dict(nf=1), dict(dim=1)],
+                         ids=["second-order", "kcu", "ugks", "1f", "1d"])
+def test_refused_configurations(kw):
+    m = US.build_mesh(*US.rectangle_mesh(3, 3))
+    assert _create(m, **kw) == -2
+    assert N.load().kb_last_error()
+
+
+def test_maxwell_wall_cells_refused():
+    m = US.build_mesh(*US.rectangle_mesh(3, 3))
+    assert _create(m, cell_type=np.where(m.cell_type == 1, 2, m.cell_type)) == -2
+    assert b"no method" in N.load().kb_last_error()
