@@ -441,6 +441,8 @@ def run_ours(args):
         blocks["batch"] = batch_block(args, peak)
     if not args.no_serve:
         blocks["serve"] = serve_block(args)
+    if not args.no_unstruct:
+        blocks["unstructured"] = unstruct_block(args, peak)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -608,6 +610,120 @@ def batch_block(args, peak):
     return out
 
 
+def unstruct_block(args, peak):
+    """Unstructured 2D2F2V on a triangle mesh (a jittered triangulation of the
+    unit square, n x n quads split in two), the reference's unstructured
+    velocity grid and gas (test/t1_2f.txt: 16 x 16 velocities on [-5, 5]^2,
+    Kn 0.075, Pr 1, inK 1, KFVS, BGK, first order) with extrapolated boundary
+    cells, from a seeded smooth state.  FP32 split and plain FP64 step rates
+    (CUDA events on the solve's stream), the step's HBM roofline fraction,
+    end to end through the C ABI, the FP32 L-inf against FP64 after the same
+    steps, and the oracle's CPU rate on a small mesh."""
+    import torch
+    from kitgpu import tune
+    from kitgpu import unstruct as US
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    n = args.us_n
+    P, T = US.rectangle_mesh(n, n, jitter=0.2, seed=11)
+    m = US.build_mesh(P, T, boundary="extra")
+
+    def prim_at(x, y):
+        r2 = (x - 0.4) ** 2 + (y - 0.6) ** 2
+        return np.array([1.0 + 0.4 * np.exp(-r2 / 0.03), 0.2 * np.sin(3 * y), -0.1 * np.cos(2 * x),
+                         1.0 / (1.0 + 0.3 * np.exp(-r2 / 0.05))])
+
+    KS = US.unstruct_solver_set(m, prim_at=prim_at)
+    init = US.initial_cells(KS)
+    nvel = KS.vs.nu * KS.vs.nv
+    nstep_cells = int((m.cell_type == 0).sum())
+    cv = m.ncell * nvel
+    out = {"workload": "unstructured 2D2F2V, %d triangles (%dx%d jittered quads), %d stepped; "
+                       "16x16 velocities on [-5,5]^2, KFVS + BGK, Kn=0.075, first order, "
+                       "extrapolated boundary cells" % (m.ncell, n, n, nstep_cells),
+           "cells": m.ncell, "velocities": nvel, "cell_velocity_per_step": cv}
+    for prec, K in (("fp32", max(args.steps, 50)), ("fp64", max(2, min(args.steps, 10)))):
+        hd = US.init_fvm(KS, prec)
+        dt = hd.timestep()
+        # stepped cells per CTA from the project autotuner (advances the
+        # state, which is re-uploaded before timing)
+        best, tim = tune.autotune_unstruct(hd, dt, steps=10, use_cache=not args.retune)
+        hd.upload(*init)
+        hd.step(dt, args.warmup)
+        stream = torch.cuda.ExternalStream(hd.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = hd.launches()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        hd.step(dt, K)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / K
+        esz = 4 if prec == "fp32" else 8
+        alg = 4.0 * esz * nstep_cells * nvel  # read h, b + write h, b of the stepped cells
+        ach = alg / (ms / 1e3) / 1e9
+        r = {"value": cv / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": K,
+             "gpu_launches": hd.launches() - n0, "cells_per_cta": hd.tuning(),
+             "tuning_ms_per_step": tim,
+             "roofline": {"bound": "hbm", "kernel": "k_us_step (whole step: k_us_step + boundary means)",
+                          "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                          "algorithmic_bytes_per_step": alg}}
+        # end to end: host FP64 state in, K steps, state out through the C ABI
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hd.upload(*init)
+        hd.step(dt, K)
+        hd.download()
+        el = time.perf_counter() - t0
+        nb = sum(a.nbytes for a in init)
+        r["e2e"] = {"value": cv * K / el, "unit": UNIT, "h2d_bytes_per_step": nb / K,
+                    "d2h_bytes_per_step": nb / K}
+        hd.close()
+        out[prec] = r
+    # FP32 against FP64 after the same number of steps
+    Ke = 20
+    st = {}
+    for prec in ("fp32", "fp64"):
+        hd = US.init_fvm(KS, prec)
+        dt = hd.timestep()
+        hd.step(dt, Ke)
+        st[prec] = hd.download()
+        hd.close()
+    e = prim_errors(st["fp32"]["prim"], st["fp64"]["prim"])
+    out["linf_fp32_vs_fp64"] = {"steps": Ke, "rho": e[0], "U": e[1], "T": e[2]}
+    out["speedup_fp32_vs_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    # the oracle (numpy restatement, one host thread) on a 24 x 24-quad mesh
+    if not args.no_cpu:
+        import oracle_us as OU
+        Ps, Ts = US.rectangle_mesh(24, 24, jitter=0.2, seed=11)
+        ms_ = US.build_mesh(Ps, Ts, boundary="extra")
+        KSs = US.unstruct_solver_set(ms_, prim_at=prim_at)
+        vs, gs = KSs.vs, KSs.gas
+        orc = OU.UnstructOracle(Ps, Ts, ms_.cell_type, vs.flat(vs.u), vs.flat(vs.v), vs.flat(vs.weights),
+                                gs.K, gs.gamma, gs.mu_ref, gs.omega, gs.Pr, "bgk")
+        orc.set_state(*US.initial_cells(KSs))
+        dt = orc.timestep(KSs.set.cfl, 0.0, KSs.set.maxTime, vs.u1, vs.v1)
+        t0 = time.perf_counter()
+        ks = 0
+        while time.perf_counter() - t0 < 10.0:
+            orc.step(dt, 1)
+            ks += 1
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": ms_.ncell * nvel * ks / el, "unit": UNIT, "cores": 1,
+                               "kind": "port", "sample": "%d steps of the numpy oracle on %d triangles"
+                                                         % (ks, ms_.ncell)}
+    return out
+
+
+def run_unstruct(args):
+    import torch
+    torch.cuda.set_device(0)
+    import kitgpu
+    kitgpu.load()
+    out = unstruct_block(args, measured_peaks()[0])
+    print(json.dumps({"metric": METRIC, "workload": "unstructured", "result": out}), flush=True)
+    return 0
+
+
 def run_batch(args):
     import torch
     import kitgpu
@@ -668,7 +784,10 @@ def main():
     ap.add_argument("--no-error", action="store_true")
     ap.add_argument("--err-steps", type=int, default=40)
     ap.add_argument("--retune", action="store_true", help="ignore the autotuner cache")
-    ap.add_argument("--workload", choices=("quadrant", "batch", "serve"), default="quadrant")
+    ap.add_argument("--workload", choices=("quadrant", "batch", "serve", "unstructured"),
+                    default="quadrant")
+    ap.add_argument("--us-n", type=int, default=384, help="unstructured mesh: n x n quads, 2 n^2 triangles")
+    ap.add_argument("--no-unstruct", action="store_true")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--max-steady", type=int, default=40000)
     ap.add_argument("--loop-sample", type=int, default=64)
@@ -695,6 +814,8 @@ def main():
         return run_batch(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "unstructured":
+        return run_unstruct(args)
     return run_ours(args)
 
 

@@ -318,7 +318,11 @@ int kb_pool_download(kb_batch_t* b, int32_t slot, double* w, double* prim, doubl
  * triangle step! (src/Solver/step_2f.jl:256-326), update_boundary! US2F
  * (src/Solver/update_boundary.jl:575-594) and the unstructured timestep
  * (src/Solver/solver_main.jl:398-420).  First-order KFVS, BGK or Shakhov,
- * FP64 or the FP32 split form; cfg supplies dim = 2, nu, nv, collision,
+ * FP64 or the FP32 split form.  cfg->nf = 1 gives 2D1F2V (evolve! US1F
+ * :872-947, update! US1F src/Solver/solver_update.jl:359-403, the 2D1F2V
+ * triangle step! src/Solver/step_1f.jl:228-285, update_boundary! US1F
+ * src/Solver/update_boundary.jl:546-566): BGK only, b held at zero.
+ * cfg supplies dim = 2, nf, nu, nv, collision,
  * precision, umax, vmax and the gas (K, gamma, mu_ref, omega, Pr), with
  * flux = KFVS and interp_order = 1 (other choices: KB_ERR_CONFIG).  Mesh
  * arrays (0-based): face_cells [nface][2] (-1: no cell), cell_faces and
@@ -343,6 +347,14 @@ int kb_us_timestep(kb_us_t* us, double cfl, double sim_time, double max_time, do
  * receives the last step's residual (src/Solver/solver_update.jl:465-467). */
 int kb_us_step(kb_us_t* us, double dt, int32_t nsteps, double* residual);
 int kb_us_info(kb_us_t* us, int64_t* launches);
+/* Kernel shape of the step: stepped cells per CTA (1..32; 0 = the default,
+ * as many as fit 32 KB of per-velocity flux sums).  No reference
+ * counterpart (launch tuning). */
+int kb_us_set_tuning(kb_us_t* us, int32_t cells_per_cta);
+int kb_us_get_tuning(kb_us_t* us, int32_t* cells_per_cta);
+/* The CUDA stream (cudaStream_t) the solve's kernels run on, for timing
+ * with events or ordering the caller's own work; no reference counterpart. */
+int kb_us_stream(kb_us_t* us, void** stream);
 
 #ifdef __cplusplus
 }

@@ -6,17 +6,33 @@
 // src/Solver/update_boundary.jl:575-594; timestep for unstructured cells,
 // src/Solver/solver_main.jl:398-420).
 //
-// Cells and faces are gathered through index tables, so each step is three
-// kernels: one CTA per face forms the first-order KFVS fluxes fh, fb of every
-// velocity (stored per face) and their moments fw; one CTA per stepped cell
-// applies the triangle update (w from the three faces' fw with their
-// orientation signs, then the BGK / Shakhov relaxation of h, b from the three
-// faces' fh, fb, in place); one CTA walks the extrapolated boundary cells in
-// cell order and sets each to the mean of its two neighbours.  The plain
-// form computes in FP64 throughout; the FP32 split form stores h, b and the
-// face fluxes in FP32 and keeps fw, w, prim and all moments in FP64.
+// One fused kernel per step, one CTA per stepped cell: the CTA reads its own
+// h, b and its three neighbours' (gathered through the index tables), forms
+// the first-order KFVS flux of each of its three faces for every velocity and
+// the faces' moments fw (block sums), updates w and prim, and relaxes h, b
+// with the fluxes formed again in a second sweep (the neighbours' values are
+// then in L1).  The face fluxes are never stored: each interior face is
+// formed by both of its cells, with the same inputs, the same operation
+// order (explicitly rounded operations, no contraction) and the same
+// velocity partition of the block sums, so both sides see bit-identical fw
+// and the update stays conservative.  New h, b go to the other buffer of a
+// ping-pong pair (neighbours must read the old state); fixed cells hold the
+// same values in both.  The extrapolated boundary cells are then set in
+// dependency levels (see kb_us_create) that reproduce the reference's
+// sequential cell-order loop.  The plain form computes in FP64 throughout;
+// the FP32 split form stores h, b and forms the per-velocity arithmetic in
+// FP32, with the block sums in compensated double-float and fw, w, prim, tau
+// in FP64.  DRAM traffic per step is one read and one write of the stepped
+// cells' h, b (the neighbours' re-reads hit L2 for meshes numbered with
+// locality), 16 B per cell-velocity in the FP32 form.
+// 2D1F2V (cfg->nf = 1: evolve! / update! / update_boundary! US1F, the
+// 2D1F2V triangle step!, src/Solver/step_1f.jl:228-285) runs the same
+// kernels with b held at zero and its equilibrium K / (2 lambda) M replaced
+// by 0, which reduces every term to the 1F formula (flux_kfvs! 1F2V,
+// src/Flux/flux_kfvs.jl:615-650).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -27,36 +43,383 @@
 namespace kb {
 
 struct UsDev {
-  int ncell, nface, nvel, vstride, coll, navg;
+  int ncell, nface, nvel, vstride, coll, nstep, navg;
   const int* face_cells;     // [nface][2], -1 where no cell
   const int* cell_faces;     // [ncell][3]
   const int* cell_nb;        // [ncell][3], -1 where no cell
   const int* cell_type;      // [ncell]: 0 stepped, 1 fixed, 3 mean of two neighbours
-  const int* avg_list;       // type-3 cells in cell order [navg]
+  const int* step_list;      // type-0 cells [nstep]
+  const int* avg_list;       // type-3 cells by dependency level [navg]
   const double* face_n;      // [nface][2]
   const double* face_len;    // [nface]
+  const float4* face_geo;    // [nface] FP32 n1, n2, len, |n|^2 (the FP32 form)
   const double* cell_area;   // [ncell]
   const double* cell_mindx;  // [ncell] smallest centre-to-edge distance
-  const double* u;
+  const double* u;           // velocity grid, FP64
   const double* v;
   const double* wt;
+  const float* uf;           // and its FP32 copies for the FP32 form
+  const float* vf;
+  const float* wtf;
   double* w;      // [ncell][4]
   double* prim;   // [ncell][4]
-  void* h;        // [ncell][vstride]
-  void* b;
-  void* fh;       // [nface][vstride]
-  void* fb;
-  double* fw;     // [nface][4] global frame
   double* cres;   // [ncell][8]: (w - w_old)^2, |w| of the last step
   double* tmax;   // [1]
   double* residual;  // [4]
   int* status;
-  double K, gamma, mu_ref, omega, Pr, umax, vmax;
+  double K, Kb, gamma, mu_ref, omega, Pr, umax, vmax;  // Kb = K (2F) or 0 (1F: b absent)
 };
 
 constexpr int US_T = 128;
+constexpr int US_W = US_T / 32;
+constexpr int US_BLK = 8;  // velocities summed plainly before a compensated flush
 
-// fixed-order tree sum over the CTA (deterministic)
+// explicitly rounded arithmetic (never contracted), so that both cells of a
+// face form its flux and moments bit-identically
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double rfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// Per cell and velocity, the signed sums over the cell's three faces of
+// the first-order KFVS fluxes (flux_kfvs! 2F2V / 1F2V of first-order states,
+// src/Flux/flux_kfvs.jl:615-700; heaviside(0) = 1):
+//   Dh = sum_j sg_j fh_j,  Db = sum_j sg_j fb_j,  Dn = sum_j sg_j |n_j|^2 fh_j
+// with sg_j = +1 where the normal points out of the cell.  The reference
+// forms each face's moments fw in the face frame (vn, vt) and rotates them
+// back (global_frame, src/Geometry/geo_general.jl:6-26); with its normals of
+// length |n| = |d| / (|d| + 1e-6) that equals |n|^2 times the global-frame
+// moments, so the cell's sum_j sg_j fw_j is
+//   (sum w Dh, sum u w Dn, sum v w Dn, (sum c^2 w Dn + sum w Db) / 2).
+// Each face flux is formed with explicitly rounded operations (never
+// contracted) from the same inputs in both of its cells, so both see the
+// same per-velocity values.
+template <typename R>
+struct UsFace {
+  R n1, n2, a, l;  // flux = ((a vn) s) l: FP64 a = dt, l = len; FP32 a = dt len, l = 1
+  R sg, sgn;       // sg and sg |n|^2
+  int nb;          // the other cell
+  bool left;       // the cell is the face's first cell
+};
+
+template <typename R>
+__device__ __forceinline__ void us_flux(const UsFace<R>& F, R u, R v, R hc, R bc, R hn, R bn,
+                                        R& fh, R& fb) {
+  const R vn = rfma(u, F.n1, rmul(v, F.n2));
+  const bool own = (vn >= R(0)) == F.left;
+  const R hs = own ? hc : hn, bs = own ? bc : bn;
+  const R av = rmul(F.a, vn);
+  if (sizeof(R) == 8) {
+    fh = rmul(rmul(av, hs), F.l);
+    fb = rmul(rmul(av, bs), F.l);
+  } else {
+    fh = rmul(av, hs);
+    fb = rmul(av, bs);
+  }
+}
+
+constexpr int US_CB = 32;   // most cells of one CTA (one lane each in the cell phase)
+constexpr int US_NM = 8;    // block sums per cell: 5 moments, 2 heat-flux sums, 1 spare
+constexpr int US_NP = 16;   // per-cell parameters of the relaxation
+
+// warp reduce-scatter of 8 per-lane partial sums (FP64, or double-float in
+// the FP32 form): three halving exchanges leave lane l with the partial of
+// sum (l >> 2) & 7 over its 8-lane group, two more finish it; lanes with
+// (l & 3) == 0 then hold the 8 totals.
+__device__ __forceinline__ double us_merge(double a, double b) { return a + b; }
+__device__ __forceinline__ DF us_merge(DF a, DF b) { return df_merge(a, b); }
+__device__ __forceinline__ double us_shfl(double a, int m) { return __shfl_xor_sync(0xffffffffu, a, m); }
+__device__ __forceinline__ DF us_shfl(DF a, int m) { return df_shfl_xor(a, m); }
+__device__ __forceinline__ double us_value(double a) { return a; }
+__device__ __forceinline__ double us_value(DF a) { return (double)a.hi + (double)a.lo; }
+template <typename V>
+__device__ __forceinline__ double us_reduce8(const V (&x)[8], int lane) {
+  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+  V y[4], z[2];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) y[k] = us_merge(b4 ? x[k + 4] : x[k], us_shfl(b4 ? x[k] : x[k + 4], 16));
+#pragma unroll
+  for (int k = 0; k < 2; ++k) z[k] = us_merge(b3 ? y[k + 2] : y[k], us_shfl(b3 ? y[k] : y[k + 2], 8));
+  V t = us_merge(b2 ? z[1] : z[0], us_shfl(b2 ? z[0] : z[1], 4));
+  t = us_merge(t, us_shfl(t, 2));
+  t = us_merge(t, us_shfl(t, 1));
+  return us_value(t);
+}
+
+template <typename R> struct Vec2;
+template <> struct Vec2<float> { using T = float2; };
+template <> struct Vec2<double> { using T = double2; };
+
+// One CTA of US_T threads steps cb consecutive cells of the step list:
+// (1) each warp takes cells wid, wid + 4, ..., forms Dh, Db (kept in shared
+// memory, two velocities per lane and iteration) and the cell's velocity
+// sums (blocked, compensated in the FP32 form); (2) warp 0 does each cell's
+// FP64 algebra on its own lane (w update, conserve_prim, residual partials,
+// tau, equilibrium and Shakhov parameters); (3) the warps relax h, b of
+// their cells.  The FP32 form takes its face geometry from an FP32 table and
+// evaluates the cell's transcendentals in FP32 (GB300 runs FP64 at a small
+// fraction of the FP32 rate, so per-cell FP64 work is kept to the lane-per-
+// cell phase).
+template <typename R, bool SHAK>
+__global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? 6 : 3)
+    k_us_step(UsDev d, double dt, int cb, const R* __restrict__ hin,
+                                                  const R* __restrict__ bin, R* __restrict__ hout,
+                                                  R* __restrict__ bout) {
+  using R2 = typename Vec2<R>::T;
+  constexpr bool FAST = sizeof(R) == 4;
+  extern __shared__ __align__(16) unsigned char us_smem[];
+  double* S = (double*)us_smem;                  // [cb][US_NM]
+  R* P = (R*)(S + cb * US_NM);                   // [cb][US_NP] (room for doubles)
+  R* D = (R*)(S + cb * (US_NM + US_NP));         // [cb][2][vstride]: Dh, Db
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int c0 = blockIdx.x * cb;
+  const int nloc = min(cb, d.nstep - c0);
+  const R2* U2 = (const R2*)(FAST ? (const void*)d.uf : (const void*)d.u);
+  const R2* V2 = (const R2*)(FAST ? (const void*)d.vf : (const void*)d.v);
+  const R2* W2 = (const R2*)(FAST ? (const void*)d.wtf : (const void*)d.wt);
+  const long vs = d.vstride;
+  const int np = d.vstride >> 1;
+  constexpr bool shak = SHAK;
+  const R rdt = R(dt);
+
+  // (1) face fluxes and velocity sums
+  for (int i = wid; i < nloc; i += US_W) {
+    const int c = d.step_list[c0 + i];
+    UsFace<R> F[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int f = d.cell_faces[3 * c + j];
+      const int L = d.face_cells[2 * f], Rc = d.face_cells[2 * f + 1];
+      const R sg = L == c ? R(1) : R(-1);
+      if (FAST) {
+        const float4 g = d.face_geo[f];  // n1, n2, len, |n|^2
+        F[j].n1 = R(g.x);
+        F[j].n2 = R(g.y);
+        F[j].a = rmul(rdt, R(g.z));
+        F[j].l = R(1);
+        F[j].sgn = sg * R(g.w);
+      } else {
+        const double n1 = d.face_n[2 * f], n2 = d.face_n[2 * f + 1];
+        F[j].n1 = R(n1);
+        F[j].n2 = R(n2);
+        F[j].a = R(dt);
+        F[j].l = R(d.face_len[f]);
+        F[j].sgn = sg * R(n1 * n1 + n2 * n2);
+      }
+      F[j].sg = sg;
+      F[j].left = L == c;
+      F[j].nb = L == c ? Rc : L;
+    }
+    const R2* Hc = (const R2*)(hin + (long)c * vs);
+    const R2* Bc = (const R2*)(bin + (long)c * vs);
+    const R2* H0 = (const R2*)(hin + (long)F[0].nb * vs);
+    const R2* B0 = (const R2*)(bin + (long)F[0].nb * vs);
+    const R2* H1 = (const R2*)(hin + (long)F[1].nb * vs);
+    const R2* B1 = (const R2*)(bin + (long)F[1].nb * vs);
+    const R2* H2 = (const R2*)(hin + (long)F[2].nb * vs);
+    const R2* B2 = (const R2*)(bin + (long)F[2].nb * vs);
+    R Uo = R(0), Vo = R(0);
+    if (shak) {
+      Uo = R(d.prim[4L * c + 1]);
+      Vo = R(d.prim[4L * c + 2]);
+    }
+    R2* Dh = (R2*)(D + (long)i * 2 * vs);
+    R2* Db = (R2*)(D + (long)i * 2 * vs + vs);
+    R pp[US_NM];
+    Acc<R> acc[US_NM];
+#pragma unroll
+    for (int k = 0; k < US_NM; ++k) pp[k] = R(0);
+    int blk = 0;
+    for (int q = lane; q < np; q += 32) {
+      const R2 u2 = U2[q], v2 = V2[q], w2 = W2[q];
+      const R2 hc2 = Hc[q], bc2 = Bc[q];
+      const R2 h0 = H0[q], b0 = B0[q], h1 = H1[q], b1 = B1[q], h2 = H2[q], b2 = B2[q];
+      R2 dh2, db2;
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const R u = e ? u2.y : u2.x, vv = e ? v2.y : v2.x, om = e ? w2.y : w2.x;
+        const R hc = e ? hc2.y : hc2.x, bc = e ? bc2.y : bc2.x;
+        R fh0, fb0, fh1, fb1, fh2, fb2;
+        us_flux(F[0], u, vv, hc, bc, e ? h0.y : h0.x, e ? b0.y : b0.x, fh0, fb0);
+        us_flux(F[1], u, vv, hc, bc, e ? h1.y : h1.x, e ? b1.y : b1.x, fh1, fb1);
+        us_flux(F[2], u, vv, hc, bc, e ? h2.y : h2.x, e ? b2.y : b2.x, fh2, fb2);
+        const R dh = F[0].sg * fh0 + F[1].sg * fh1 + F[2].sg * fh2;
+        const R db = F[0].sg * fb0 + F[1].sg * fb1 + F[2].sg * fb2;
+        const R dn = F[0].sgn * fh0 + F[1].sgn * fh1 + F[2].sgn * fh2;
+        if (e) { dh2.y = dh; db2.y = db; } else { dh2.x = dh; db2.x = db; }
+        const R wn = om * dn;
+        pp[0] += om * dh;
+        pp[1] += u * wn;
+        pp[2] += vv * wn;
+        pp[3] += (u * u + vv * vv) * wn;
+        pp[4] += om * db;
+        if (shak) {  // heat_flux 2F2V of the old state (src/Theory/theory_moments.jl:567-578)
+          const R cu = u - Uo, cv = vv - Vo;
+          const R t = om * ((cu * cu + cv * cv) * hc + bc);
+          pp[5] += cu * t;
+          pp[6] += cv * t;
+        }
+      }
+      Dh[q] = dh2;
+      Db[q] = db2;
+      if (++blk == US_BLK) {
+#pragma unroll
+        for (int k = 0; k < US_NM; ++k) {
+          acc[k].add(pp[k]);
+          pp[k] = R(0);
+        }
+        blk = 0;
+      }
+    }
+    decltype(acc[0].s) x[US_NM];
+#pragma unroll
+    for (int k = 0; k < US_NM; ++k) {
+      acc[k].add(pp[k]);
+      x[k] = acc[k].s;
+    }
+    const double t = us_reduce8(x, lane);
+    if ((lane & 3) == 0) S[i * US_NM + (lane >> 2)] = t;
+  }
+  __syncthreads();
+
+  // (2) the cell algebra, one lane per cell (step! 2D2F2V on a triangle,
+  // src/Solver/step_2f.jl:256-326; 2D1F2V src/Solver/step_1f.jl:228-285)
+  if (wid == 0 && lane < nloc) {
+    const int c = d.step_list[c0 + lane];
+    const double* Sc = S + lane * US_NM;
+    double* w = d.w + 4L * c;
+    double* p = d.prim + 4L * c;
+    const double rho_o = p[0], U_o = p[1], V_o = p[2], lam_o = p[3];
+    const double ia = 1.0 / d.cell_area[c];
+    const double A[4] = {Sc[0], Sc[1], Sc[2], 0.5 * (Sc[3] + Sc[4])};
+    double wo[4], pn[4];
+    double* cr = d.cres + 8L * c;
+    for (int k = 0; k < 4; ++k) {
+      wo[k] = w[k];
+      w[k] -= A[k] * ia;
+    }
+    conserve_prim<FAST>(w, 4, d.gamma, pn);
+    for (int k = 0; k < 4; ++k) {
+      p[k] = pn[k];
+      cr[k] = (w[k] - wo[k]) * (w[k] - wo[k]);
+      cr[4 + k] = fabs(w[k]);
+    }
+    if (!(pn[0] > 0.0) || !(pn[3] > 0.0) || !isfinite(pn[0]) || !isfinite(pn[3])) atomicOr(d.status, 1);
+    const double k = dt / vhs_time<FAST>(pn[0], pn[3], d.mu_ref, d.omega);
+    R* Pc = P + lane * US_NP;
+    Pc[0] = R(pn[0] * (pn[3] / PI));  // Maxwellian amplitude
+    Pc[1] = R(pn[1]);
+    Pc[2] = R(pn[2]);
+    Pc[3] = R(pn[3]);
+    Pc[4] = R(d.Kb / (2.0 * pn[3]));  // B / H
+    Pc[5] = R(k);
+    Pc[6] = R(1.0 / (1.0 + k));
+    Pc[7] = R(ia);
+    if (shak) {  // shakhov 2F2V of the old state (src/Theory/theory_equilibrium.jl:227-238)
+      const double sfac = 0.8 * (1.0 - d.Pr) * (lam_o * lam_o) / rho_o;
+      Pc[8] = R(sfac * 0.5 * Sc[5]);
+      Pc[9] = R(sfac * 0.5 * Sc[6]);
+      Pc[10] = R(rho_o * (lam_o / PI));
+      Pc[11] = R(d.Kb / (2.0 * lam_o));
+      Pc[12] = R(lam_o);
+      Pc[13] = R(U_o);
+      Pc[14] = R(V_o);
+    }
+  }
+  __syncthreads();
+
+  // (3) relaxation of h, b
+  const R Km5 = R(d.Kb - 5.0), Km3 = R(d.Kb - 3.0);
+  for (int i = wid; i < nloc; i += US_W) {
+    const int c = d.step_list[c0 + i];
+    const R* Pc = P + i * US_NP;
+    const R rn = Pc[0], U = Pc[1], V = Pc[2], lam = Pc[3], cB = Pc[4];
+    const R kk = Pc[5], i1k = Pc[6], ia = Pc[7];
+    R fq0 = R(0), fq1 = R(0), orn = R(0), ocB = R(0), olam = R(0), Uo = R(0), Vo = R(0);
+    if (shak) {
+      fq0 = Pc[8];
+      fq1 = Pc[9];
+      orn = Pc[10];
+      ocB = Pc[11];
+      olam = Pc[12];
+      Uo = Pc[13];
+      Vo = Pc[14];
+    }
+    const R2* Hc = (const R2*)(hin + (long)c * vs);
+    const R2* Bc = (const R2*)(bin + (long)c * vs);
+    const R2* Dh = (const R2*)(D + (long)i * 2 * vs);
+    const R2* Db = (const R2*)(D + (long)i * 2 * vs + vs);
+    R2* Ho = (R2*)(hout + (long)c * vs);
+    R2* Bo = (R2*)(bout + (long)c * vs);
+    for (int q = lane; q < np; q += 32) {
+      const R2 u2 = U2[q], v2 = V2[q], hc2 = Hc[q], bc2 = Bc[q], dh2 = Dh[q], db2 = Db[q];
+      R2 ho, bo;
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const R u = e ? u2.y : u2.x, vv = e ? v2.y : v2.x;
+        const R du = u - U, dv = vv - V;
+        R MH = rn * mexp(-lam * (du * du + dv * dv));
+        R MB = MH * cB;
+        if (shak) {
+          const R cu = u - Uo, cv = vv - Vo, c2 = cu * cu + cv * cv;
+          const R MHo = orn * mexp(-olam * c2), MBo = MHo * ocB;
+          const R fq = fq0 * cu + fq1 * cv;
+          const R tl = R(2) * olam * c2;
+          MH += fq * (tl + Km5) * MHo;
+          MB += fq * (tl + Km3) * MBo;
+        }
+        const R hn = ((e ? hc2.y : hc2.x) - (e ? dh2.y : dh2.x) * ia + kk * MH) * i1k;
+        const R bn = ((e ? bc2.y : bc2.x) - (e ? db2.y : db2.x) * ia + kk * MB) * i1k;
+        if (e) { ho.y = hn; bo.y = bn; } else { ho.x = hn; bo.x = bn; }
+      }
+      Ho[q] = ho;
+      Bo[q] = bo;
+    }
+  }
+}
+
+// update_boundary! US2F (src/Solver/update_boundary.jl:575-594) for the
+// extrapolated cells of one dependency level: each becomes the mean of its
+// first two neighbours.  The reference runs this loop in cell order, so a
+// cell sees the new value of an earlier extrapolated neighbour and the old
+// value of a later one; levels are built so that the earlier ones are done
+// and the later ones not yet, and a later one's old h, b are read from the
+// input buffer (its output slot is written in a later level).
+template <typename R>
+__global__ void __launch_bounds__(US_T) k_us_avg(UsDev d, int first, const R* __restrict__ hin,
+                                                 const R* __restrict__ bin, R* hout, R* bout) {
+  const int c = d.avg_list[first + blockIdx.x];
+  int id[2] = {c, c}, m = 0;
+  for (int j = 0; j < 3; ++j)
+    if (d.cell_nb[3 * c + j] != -1 && m < 2) id[m++] = d.cell_nb[3 * c + j];
+  if (threadIdx.x == 0) {
+    double* w = d.w + 4L * c;
+    for (int k = 0; k < 4; ++k) w[k] = 0.5 * (d.w[4L * id[0] + k] + d.w[4L * id[1] + k]);
+    double pn[4];
+    conserve_prim<false>(w, 4, d.gamma, pn);
+    for (int k = 0; k < 4; ++k) d.prim[4L * c + k] = pn[k];
+  }
+  const long vs = d.vstride;
+  const bool old0 = d.cell_type[id[0]] == 3 && id[0] > c, old1 = d.cell_type[id[1]] == 3 && id[1] > c;
+  const R* H0 = (old0 ? hin : hout) + id[0] * vs;
+  const R* B0 = (old0 ? bin : bout) + id[0] * vs;
+  const R* H1 = (old1 ? hin : hout) + id[1] * vs;
+  const R* B1 = (old1 ? bin : bout) + id[1] * vs;
+  R* H = hout + (long)c * vs;
+  R* B = bout + (long)c * vs;
+  for (int v = threadIdx.x; v < d.nvel; v += US_T) {
+    H[v] = R(0.5) * (H0[v] + H1[v]);
+    B[v] = R(0.5) * (B0[v] + B1[v]);
+  }
+}
+
+// residual of update! US2F: sqrt(sum (w - w_old)^2 * ncell) / (sum |w| + 1e-7)
+// over the stepped cells (src/Solver/solver_update.jl:465-467); chunked sums
+// in cell order, then a fixed tree (deterministic)
 __device__ __forceinline__ double us_block_sum(double x, double* red) {
   red[threadIdx.x] = x;
   __syncthreads();
@@ -69,192 +432,6 @@ __device__ __forceinline__ double us_block_sum(double x, double* red) {
   return r;
 }
 
-// flux_kfvs! 2F2V (src/Flux/flux_kfvs.jl:654-700) of first-order face states
-// with flux_conserve! (src/Theory/theory_moments.jl:409-414), then
-// global_frame (src/Geometry/geo_general.jl:6-26).  Faces without two cells
-// are not used by any stepped cell and carry zero flux.
-template <typename R>
-__global__ void __launch_bounds__(US_T) k_us_face(UsDev d, double dt) {
-  __shared__ double red[US_T];
-  const int f = blockIdx.x;
-  const int cl = d.face_cells[2 * f], cr = d.face_cells[2 * f + 1];
-  R* Fh = (R*)d.fh + (long)f * d.vstride;
-  R* Fb = (R*)d.fb + (long)f * d.vstride;
-  if (cl < 0 || cr < 0) {
-    for (int v = threadIdx.x; v < d.nvel; v += US_T) {
-      Fh[v] = R(0);
-      Fb[v] = R(0);
-    }
-    if (threadIdx.x < 4) d.fw[4 * f + threadIdx.x] = 0.0;
-    return;
-  }
-  const double n1 = d.face_n[2 * f], n2 = d.face_n[2 * f + 1], len = d.face_len[f];
-  const R* HL = (const R*)d.h + (long)cl * d.vstride;
-  const R* BL = (const R*)d.b + (long)cl * d.vstride;
-  const R* HR = (const R*)d.h + (long)cr * d.vstride;
-  const R* BR = (const R*)d.b + (long)cr * d.vstride;
-  double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  for (int v = threadIdx.x; v < d.nvel; v += US_T) {
-    const double u = d.u[v], vv = d.v[v];
-    const double vn = __dadd_rn(__dmul_rn(u, n1), __dmul_rn(vv, n2));
-    const double vt = __dsub_rn(__dmul_rn(vv, n1), __dmul_rn(u, n2));
-    const bool up = vn >= 0.0;  // heaviside(0) = 1
-    R fh, fb;
-    if (sizeof(R) == 8) {
-      const double hs = up ? (double)HL[v] : (double)HR[v];
-      const double bs = up ? (double)BL[v] : (double)BR[v];
-      fh = R(__dmul_rn(__dmul_rn(__dmul_rn(dt, vn), hs), len));
-      fb = R(__dmul_rn(__dmul_rn(__dmul_rn(dt, vn), bs), len));
-    } else {
-      const float hs = up ? (float)HL[v] : (float)HR[v];
-      const float bs = up ? (float)BL[v] : (float)BR[v];
-      const float tl = float(dt * len * vn);
-      fh = R(tl * hs);
-      fb = R(tl * bs);
-    }
-    Fh[v] = fh;
-    Fb[v] = fb;
-    const double om = d.wt[v];
-    const double wf = om * (double)fh;
-    s[0] += wf;
-    s[1] += vn * wf;
-    s[2] += vt * wf;
-    s[3] += (vn * vn + vt * vt) * wf;
-    s[4] += om * (double)fb;
-  }
-  double S[5];
-#pragma unroll
-  for (int k = 0; k < 5; ++k) S[k] = us_block_sum(s[k], red);
-  if (threadIdx.x == 0) {
-    const double l1 = S[1], l2 = S[2];
-    d.fw[4 * f + 0] = S[0];
-    d.fw[4 * f + 1] = l1 * n1 - l2 * n2;
-    d.fw[4 * f + 2] = l1 * n2 + l2 * n1;
-    d.fw[4 * f + 3] = 0.5 * (S[3] + S[4]);
-  }
-}
-
-// step! 2D2F2V on a triangle (src/Solver/step_2f.jl:256-326) for the cells
-// update! US2F steps (cellType 0, src/Solver/solver_update.jl:428-462); the
-// orientation sign of face j is +1 when the face normal points out of the
-// cell (the cell is the first of the face's two cells) and -1 otherwise.
-template <typename R>
-__global__ void __launch_bounds__(US_T) k_us_cell(UsDev d, double dt) {
-  __shared__ double red[US_T];
-  __shared__ double sh[16];
-  const int c = blockIdx.x;
-  double* cr = d.cres + 8L * c;
-  if (d.cell_type[c] != 0) {
-    if (threadIdx.x < 8) cr[threadIdx.x] = 0.0;
-    return;
-  }
-  int fj[3];
-  double sg[3];
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    fj[j] = d.cell_faces[3 * c + j];
-    // a boundary face's normal points into its only cell
-    sg[j] = (d.face_cells[2 * fj[j]] == c && d.face_cells[2 * fj[j] + 1] != -1) ? 1.0 : -1.0;
-  }
-  const double area = d.cell_area[c];
-  double* w = d.w + 4L * c;
-  double* p = d.prim + 4L * c;
-  const double rho_o = p[0], U_o = p[1], V_o = p[2], lam_o = p[3];
-  R* H = (R*)d.h + (long)c * d.vstride;
-  R* B = (R*)d.b + (long)c * d.vstride;
-  const bool shak = d.coll == COLL_SHAKHOV;
-  double q0 = 0.0, q1 = 0.0;
-  if (shak) {  // heat_flux 2F2V of the old state (src/Theory/theory_moments.jl:567-578)
-    double a0 = 0.0, a1 = 0.0;
-    for (int v = threadIdx.x; v < d.nvel; v += US_T) {
-      const double cu = d.u[v] - U_o, cv = d.v[v] - V_o, om = d.wt[v];
-      const double c2 = cu * cu + cv * cv, hv = (double)H[v], bv = (double)B[v];
-      a0 += om * cu * c2 * hv + om * cu * bv;
-      a1 += om * cv * c2 * hv + om * cv * bv;
-    }
-    q0 = 0.5 * us_block_sum(a0, red);
-    q1 = 0.5 * us_block_sum(a1, red);
-  }
-  __syncthreads();  // every thread has read the old prim before thread 0 replaces it
-  if (threadIdx.x == 0) {
-    double wo[4];
-    for (int k = 0; k < 4; ++k) wo[k] = w[k];
-    for (int k = 0; k < 4; ++k)
-      w[k] -= (d.fw[4 * fj[0] + k] * sg[0] + d.fw[4 * fj[1] + k] * sg[1] +
-               d.fw[4 * fj[2] + k] * sg[2]) / area;
-    double pn[4];
-    conserve_prim<false>(w, 4, d.gamma, pn);
-    for (int k = 0; k < 4; ++k) {
-      p[k] = pn[k];
-      cr[k] = (w[k] - wo[k]) * (w[k] - wo[k]);
-      cr[4 + k] = fabs(w[k]);
-    }
-    if (!(pn[0] > 0.0) || !(pn[3] > 0.0) || !isfinite(pn[0]) || !isfinite(pn[3])) atomicOr(d.status, 1);
-    const double tau = d.mu_ref * 2.0 * pow(pn[3], 1.0 - d.omega) / pn[0];
-    for (int k = 0; k < 4; ++k) sh[k] = pn[k];
-    sh[4] = dt / tau;
-  }
-  __syncthreads();
-  const double rho = sh[0], U = sh[1], V = sh[2], lam = sh[3], k = sh[4];
-  const double rn = rho * (lam / PI), cB = d.K / (2.0 * lam);
-  const double orn = rho_o * (lam_o / PI), ocB = d.K / (2.0 * lam_o);
-  const double sfac = 0.8 * (1.0 - d.Pr) * (lam_o * lam_o) / rho_o;
-  const R* F0h = (const R*)d.fh + (long)fj[0] * d.vstride;
-  const R* F1h = (const R*)d.fh + (long)fj[1] * d.vstride;
-  const R* F2h = (const R*)d.fh + (long)fj[2] * d.vstride;
-  const R* F0b = (const R*)d.fb + (long)fj[0] * d.vstride;
-  const R* F1b = (const R*)d.fb + (long)fj[1] * d.vstride;
-  const R* F2b = (const R*)d.fb + (long)fj[2] * d.vstride;
-  for (int v = threadIdx.x; v < d.nvel; v += US_T) {
-    const double u = d.u[v], vv = d.v[v];
-    const double du = u - U, dv = vv - V;
-    double MH = rn * exp(-lam * (du * du + dv * dv));
-    double MB = MH * cB;
-    if (shak) {
-      const double cu = u - U_o, cv = vv - V_o, c2 = cu * cu + cv * cv;
-      const double MHo = orn * exp(-lam_o * c2), MBo = MHo * ocB;
-      const double fq = sfac * (cu * q0 + cv * q1);
-      MH += fq * (2.0 * lam_o * c2 + d.K - 5.0) * MHo;
-      MB += fq * (2.0 * lam_o * c2 + d.K - 3.0) * MBo;
-    }
-    const double dh = ((double)F0h[v] * sg[0] + (double)F1h[v] * sg[1] + (double)F2h[v] * sg[2]) / area;
-    const double db = ((double)F0b[v] * sg[0] + (double)F1b[v] * sg[1] + (double)F2b[v] * sg[2]) / area;
-    H[v] = R(((double)H[v] - dh + k * MH) / (1.0 + k));
-    B[v] = R(((double)B[v] - db + k * MB) / (1.0 + k));
-  }
-}
-
-// update_boundary! US2F (src/Solver/update_boundary.jl:575-594): each
-// extrapolated cell becomes the mean of its two neighbours, in cell order
-// (a later cell sees the new value of an earlier one), one CTA in sequence.
-template <typename R>
-__global__ void __launch_bounds__(US_T) k_us_avg(UsDev d) {
-  for (int a = 0; a < d.navg; ++a) {
-    const int c = d.avg_list[a];
-    int id[2] = {c, c}, m = 0;
-    for (int j = 0; j < 3; ++j)
-      if (d.cell_nb[3 * c + j] != -1 && m < 2) id[m++] = d.cell_nb[3 * c + j];
-    if (threadIdx.x == 0) {
-      double* w = d.w + 4L * c;
-      for (int k = 0; k < 4; ++k) w[k] = 0.5 * (d.w[4L * id[0] + k] + d.w[4L * id[1] + k]);
-      double pn[4];
-      conserve_prim<false>(w, 4, d.gamma, pn);
-      for (int k = 0; k < 4; ++k) d.prim[4L * c + k] = pn[k];
-    }
-    R* H = (R*)d.h;
-    R* B = (R*)d.b;
-    const long o = (long)c * d.vstride, o0 = (long)id[0] * d.vstride, o1 = (long)id[1] * d.vstride;
-    for (int v = threadIdx.x; v < d.nvel; v += US_T) {
-      H[o + v] = R(0.5 * ((double)H[o0 + v] + (double)H[o1 + v]));
-      B[o + v] = R(0.5 * ((double)B[o0 + v] + (double)B[o1 + v]));
-    }
-    __syncthreads();
-  }
-}
-
-// residual of update! US2F: sqrt(sum (w - w_old)^2 * ncell) / (sum |w| + 1e-7)
-// over the stepped cells (src/Solver/solver_update.jl:465-467); chunked sums
-// in cell order, then a fixed tree (deterministic)
 __global__ void __launch_bounds__(US_T) k_us_residual(UsDev d) {
   __shared__ double red[US_T];
   const int per = (d.ncell + US_T - 1) / US_T;
@@ -290,14 +467,19 @@ __global__ void k_us_tmax(UsDev d) {
     atomicMax((unsigned long long*)d.tmax, (unsigned long long)__double_as_longlong(red[0]));
 }
 
+// FP64 host rows [ncell][nvel] <-> device rows [ncell][vstride] (both
+// buffers of the ping-pong pair on upload)
 template <typename R>
-__global__ void k_us_in(R* dst, const double* src, long ncell, int nvel, int vstride) {
+__global__ void k_us_in(R* dst0, R* dst1, const double* src, int nvel, int vstride) {
   const long c = blockIdx.x;
-  for (int v = threadIdx.x; v < vstride; v += blockDim.x)
-    dst[c * vstride + v] = v < nvel ? R(src[c * nvel + v]) : R(0);
+  for (int v = threadIdx.x; v < vstride; v += blockDim.x) {
+    const R x = v < nvel ? R(src[c * nvel + v]) : R(0);
+    dst0[c * vstride + v] = x;
+    dst1[c * vstride + v] = x;
+  }
 }
 template <typename R>
-__global__ void k_us_out(double* dst, const R* src, long ncell, int nvel, int vstride) {
+__global__ void k_us_out(double* dst, const R* src, int nvel, int vstride) {
   const long c = blockIdx.x;
   for (int v = threadIdx.x; v < nvel; v += blockDim.x) dst[c * nvel + v] = (double)src[c * vstride + v];
 }
@@ -311,6 +493,12 @@ struct kb_us {
   std::vector<void*> allocs;
   int64_t launches = 0;
   double* stage = nullptr;
+  void* h[2] = {nullptr, nullptr};  // ping-pong pairs; cur holds the state
+  void* b[2] = {nullptr, nullptr};
+  int cur = 0;
+  std::vector<int> level_first;  // avg_list offsets of the dependency levels (+ end)
+  int cb = 1;                    // stepped cells per CTA
+  size_t smem = 0;               // dynamic shared memory of the step kernel
 };
 
 static int usfail(int code, const std::string& m) {
@@ -324,6 +512,74 @@ static int usalloc(kb_us* U, void** p, size_t bytes) {
     return usfail(KB_ERR_NOMEM, "unstructured solve: cudaMalloc failed");
   }
   U->allocs.push_back(*p);
+  return KB_OK;
+}
+
+// Dependency levels of the extrapolated (type-3) cells.  update_boundary!
+// sets them one after another in cell order, each from its first two
+// neighbours, so a cell c that reads an earlier type-3 cell must come after
+// it and one that reads a later type-3 cell must come before it (it sees the
+// old value).  Both constraints point from the lower to the higher cell
+// index, so levels by longest path in index order make every level free of
+// such pairs, and running the levels in order reproduces the loop.
+static std::vector<int> us_levels(int ncell, const int32_t* cell_nb, const int32_t* cell_type,
+                                  std::vector<int>& order, std::vector<int>& first) {
+  std::vector<int> lvl(ncell, 0), minl(ncell, 1);
+  int top = 0;
+  for (int c = 0; c < ncell; ++c) {
+    if (cell_type[c] != 3) continue;
+    int ids[2], m = 0;
+    for (int j = 0; j < 3 && m < 2; ++j)
+      if (cell_nb[3 * c + j] != -1) ids[m++] = cell_nb[3 * c + j];
+    int l = minl[c];
+    for (int k = 0; k < m; ++k)
+      if (cell_type[ids[k]] == 3 && ids[k] < c) l = std::max(l, lvl[ids[k]] + 1);
+    lvl[c] = l;
+    for (int k = 0; k < m; ++k)
+      if (cell_type[ids[k]] == 3 && ids[k] > c) minl[ids[k]] = std::max(minl[ids[k]], l + 1);
+    top = std::max(top, l);
+  }
+  first.assign(top + 2, 0);
+  for (int c = 0; c < ncell; ++c)
+    if (cell_type[c] == 3) first[lvl[c] + 1]++;
+  for (int l = 1; l <= top + 1; ++l) first[l] += first[l - 1];
+  order.assign(first[top + 1], 0);
+  std::vector<int> pos(first.begin(), first.end());
+  for (int c = 0; c < ncell; ++c)
+    if (cell_type[c] == 3) order[pos[lvl[c]]++] = c;
+  // level 0 is empty (levels start at 1)
+  first.erase(first.begin());
+  return lvl;
+}
+
+// Cells per CTA of the step kernel and its shared memory: the per-velocity
+// flux sums of cb cells (2 nvel values each) plus the per-cell sums and
+// parameters.  cb = 0 picks the largest count up to 32 within 32 KB of flux
+// sums (at least one cell).
+static int us_set_cells_per_cta(kb_us* U, int cb) {
+  const kb::UsDev& d = U->d;
+  const size_t esz = U->prec == KB_PREC_FP64 ? 8 : 4;
+  const size_t per = 2 * (size_t)d.vstride * esz;
+  if (cb == 0) cb = (int)std::max<size_t>(1, std::min<size_t>(kb::US_CB, (32u << 10) / per));
+  if (cb < 1 || cb > kb::US_CB) return usfail(KB_ERR_ARG, "cells per CTA must be 1 .. 32");
+  const size_t smem = (sizeof(double) * (kb::US_NM + kb::US_NP) + per) * cb;
+  int dev = 0, maxs = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (smem > (size_t)maxs)
+    return usfail(KB_ERR_CONFIG, "velocity grid too large for the unstructured step's shared memory");
+  const bool sk = d.coll == KB_COLL_SHAKHOV;
+  const void* fn = U->prec == KB_PREC_FP64 ? (sk ? (const void*)kb::k_us_step<double, true>
+                                                 : (const void*)kb::k_us_step<double, false>)
+                                           : (sk ? (const void*)kb::k_us_step<float, true>
+                                                 : (const void*)kb::k_us_step<float, false>);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return usfail(KB_ERR_CUDA, "kb_us: cudaFuncSetAttribute failed");
+  }
+  U->cb = cb;
+  U->smem = smem;
   return KB_OK;
 }
 
@@ -345,7 +601,11 @@ extern "C" int kb_us_create(const kb_config_t* cfg, int32_t ncell, int32_t nface
   if (!cfg || !out || !face_cells || !cell_faces || !cell_nb || !cell_type || !face_n ||
       !face_len || !cell_area || !cell_mindx || !u || !v || !weights || ncell < 1 || nface < 3)
     return usfail(KB_ERR_ARG, "kb_us_create: null argument or empty mesh");
-  if (cfg->dim != 2 || cfg->nf == 1) return usfail(KB_ERR_CONFIG, "unstructured solves are 2D2F2V");
+  if (cfg->dim != 2) return usfail(KB_ERR_CONFIG, "unstructured solves are 2D (2D2F2V or 2D1F2V)");
+  if (cfg->nf == 1 && cfg->collision != KB_COLL_BGK)
+    return usfail(KB_ERR_CONFIG,
+                  "2D1F2V unstructured solves are BGK: the reference's triangle step! for 2D1F2V reads "
+                  "h and b, which it does not have, under Shakhov");
   if (cfg->flux != KB_FLUX_KFVS)
     return usfail(KB_ERR_CONFIG, "unstructured solves use KFVS (evolve! US2F computes fluxes for :kfvs only)");
   if (cfg->interp_order != 1)
@@ -361,7 +621,7 @@ extern "C" int kb_us_create(const kb_config_t* cfg, int32_t ncell, int32_t nface
     if (face_cells[2 * f] < 0 || face_cells[2 * f] >= ncell || face_cells[2 * f + 1] < -1 ||
         face_cells[2 * f + 1] >= ncell)
       return usfail(KB_ERR_ARG, "face_cells out of range");
-  std::vector<int> avg;
+  std::vector<int> steps;
   for (int c = 0; c < ncell; ++c) {
     const int t = cell_type[c];
     if (t == 2)
@@ -375,26 +635,34 @@ extern "C" int kb_us_create(const kb_config_t* cfg, int32_t ncell, int32_t nface
       if (f < 0 || f >= nface) return usfail(KB_ERR_ARG, "cell_faces out of range");
       if (face_cells[2 * f] != c && face_cells[2 * f + 1] != c)
         return usfail(KB_ERR_ARG, "cell_faces and face_cells disagree");
-      if (cell_nb[3 * c + j] < -1 || cell_nb[3 * c + j] >= ncell)
-        return usfail(KB_ERR_ARG, "cell_neighbors out of range");
-      nb += cell_nb[3 * c + j] >= 0;
+      const int n = cell_nb[3 * c + j];
+      if (n < -1 || n >= ncell) return usfail(KB_ERR_ARG, "cell_neighbors out of range");
+      if (n != (face_cells[2 * f] == c ? face_cells[2 * f + 1] : face_cells[2 * f]))
+        return usfail(KB_ERR_ARG, "cell_neighbors and face_cells disagree");
+      nb += n >= 0;
     }
-    if (t == 0 && nb != 3) return usfail(KB_ERR_CONFIG, "a stepped cell (type 0) needs three neighbours");
-    if (t == 3) {
-      if (nb < 2) return usfail(KB_ERR_CONFIG, "an extrapolated cell (type 3) needs two neighbours");
-      avg.push_back(c);
+    if (t == 0) {
+      if (nb != 3) return usfail(KB_ERR_CONFIG, "a stepped cell (type 0) needs three neighbours");
+      steps.push_back(c);
     }
+    if (t == 3 && nb < 2)
+      return usfail(KB_ERR_CONFIG, "an extrapolated cell (type 3) needs two neighbours");
   }
+  std::vector<int> avg, first;
+  us_levels(ncell, cell_nb, cell_type, avg, first);
   kb_us* U = new kb_us();
   kb::UsDev& d = U->d;
   U->prec = cfg->precision;
+  U->level_first = first;
   d.ncell = ncell;
   d.nface = nface;
   d.nvel = cfg->nu * cfg->nv;
   d.vstride = (d.nvel + 3) / 4 * 4;
   d.coll = cfg->collision;
+  d.nstep = (int)steps.size();
   d.navg = (int)avg.size();
   d.K = cfg->K;
+  d.Kb = cfg->nf == 1 ? 0.0 : cfg->K;
   d.gamma = cfg->gamma;
   d.mu_ref = cfg->mu_ref;
   d.omega = cfg->omega;
@@ -413,33 +681,55 @@ extern "C" int kb_us_create(const kb_config_t* cfg, int32_t ncell, int32_t nface
 #define USALLOC(dst, T, count)                                                        \
   if ((rc = usalloc(U, &p, sizeof(T) * (size_t)(count))) != KB_OK) return bail(rc); \
   dst = (T*)p;
-  int *fc, *cf, *nbp, *ct, *al, *st;
+  int *fc, *cf, *nbp, *ct, *sl, *al, *st;
   double *fn, *fl, *ca, *cm, *du, *dv, *dw, *tm, *res;
+  float *fu, *fv, *fwt;
+  float4* geo;
   USALLOC(fc, int, 2 * nface);
   USALLOC(cf, int, 3 * ncell);
   USALLOC(nbp, int, 3 * ncell);
   USALLOC(ct, int, ncell);
+  USALLOC(sl, int, steps.size() + 1);
   USALLOC(al, int, avg.size() + 1);
   USALLOC(st, int, 1);
   USALLOC(fn, double, 2 * nface);
   USALLOC(fl, double, nface);
   USALLOC(ca, double, ncell);
   USALLOC(cm, double, ncell);
-  USALLOC(du, double, d.nvel);
-  USALLOC(dv, double, d.nvel);
-  USALLOC(dw, double, d.nvel);
+  USALLOC(du, double, d.vstride);
+  USALLOC(dv, double, d.vstride);
+  USALLOC(dw, double, d.vstride);
+  USALLOC(fu, float, d.vstride);
+  USALLOC(fv, float, d.vstride);
+  USALLOC(fwt, float, d.vstride);
+  USALLOC(geo, float4, nface);
   USALLOC(tm, double, 1);
   USALLOC(res, double, 4);
   USALLOC(d.w, double, 4L * ncell);
   USALLOC(d.prim, double, 4L * ncell);
-  USALLOC(d.fw, double, 4L * nface);
   USALLOC(d.cres, double, 8L * ncell);
   USALLOC(U->stage, double, (long)ncell * d.nvel);
 #undef USALLOC
-  for (void** q : {&d.h, &d.b})
+  for (void** q : {&U->h[0], &U->h[1], &U->b[0], &U->b[1]})
     if ((rc = usalloc(U, q, esz * (size_t)ncell * d.vstride)) != KB_OK) return bail(rc);
-  for (void** q : {&d.fh, &d.fb})
-    if ((rc = usalloc(U, q, esz * (size_t)nface * d.vstride)) != KB_OK) return bail(rc);
+  // velocity grid padded to vstride with zero weights (the padding carries
+  // no moment), in FP64 and FP32
+  const size_t VS = d.vstride;
+  std::vector<double> f64(3 * VS, 0.0);
+  std::vector<float> f32(3 * VS, 0.0f);
+  for (int k = 0; k < d.nvel; ++k) {
+    f64[k] = u[k];
+    f64[VS + k] = v[k];
+    f64[2 * VS + k] = weights[k];
+    f32[k] = (float)u[k];
+    f32[VS + k] = (float)v[k];
+    f32[2 * VS + k] = (float)weights[k];
+  }
+  std::vector<float4> g32(nface);
+  for (int f = 0; f < nface; ++f) {
+    const double n1 = face_n[2 * f], n2 = face_n[2 * f + 1];
+    g32[f] = make_float4((float)n1, (float)n2, (float)face_len[f], (float)(n1 * n1 + n2 * n2));
+  }
   bool ok = true;
   auto up = [&](void* dst, const void* src, size_t bytes) {
     ok &= cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -448,30 +738,41 @@ extern "C" int kb_us_create(const kb_config_t* cfg, int32_t ncell, int32_t nface
   up(cf, cell_faces, sizeof(int) * 3 * ncell);
   up(nbp, cell_nb, sizeof(int) * 3 * ncell);
   up(ct, cell_type, sizeof(int) * ncell);
+  if (!steps.empty()) up(sl, steps.data(), sizeof(int) * steps.size());
   if (!avg.empty()) up(al, avg.data(), sizeof(int) * avg.size());
   up(fn, face_n, sizeof(double) * 2 * nface);
   up(fl, face_len, sizeof(double) * nface);
   up(ca, cell_area, sizeof(double) * ncell);
   up(cm, cell_mindx, sizeof(double) * ncell);
-  up(du, u, sizeof(double) * d.nvel);
-  up(dv, v, sizeof(double) * d.nvel);
-  up(dw, weights, sizeof(double) * d.nvel);
+  up(du, f64.data(), sizeof(double) * VS);
+  up(dv, f64.data() + VS, sizeof(double) * VS);
+  up(dw, f64.data() + 2 * VS, sizeof(double) * VS);
+  up(fu, f32.data(), sizeof(float) * VS);
+  up(fv, f32.data() + VS, sizeof(float) * VS);
+  up(fwt, f32.data() + 2 * VS, sizeof(float) * VS);
+  up(geo, g32.data(), sizeof(float4) * nface);
   ok &= cudaMemset(st, 0, sizeof(int)) == cudaSuccess;
   ok &= cudaMemset(d.cres, 0, sizeof(double) * 8L * ncell) == cudaSuccess;
   if (!ok) return bail(usfail(KB_ERR_CUDA, "kb_us_create: copy failed"));
+  if ((rc = us_set_cells_per_cta(U, 0)) != KB_OK) return bail(rc);
   d.face_cells = fc;
   d.cell_faces = cf;
   d.cell_nb = nbp;
   d.cell_type = ct;
+  d.step_list = sl;
   d.avg_list = al;
   d.status = st;
   d.face_n = fn;
   d.face_len = fl;
+  d.face_geo = geo;
   d.cell_area = ca;
   d.cell_mindx = cm;
   d.u = du;
   d.v = dv;
   d.wt = dw;
+  d.uf = fu;
+  d.vf = fv;
+  d.wtf = fwt;
   d.tmax = tm;
   d.residual = res;
   *out = U;
@@ -482,19 +783,23 @@ extern "C" int kb_us_upload(kb_us_t* U, const double* w, const double* prim, con
                             const double* b) {
   if (!U || !w || !prim || !h || !b) return usfail(KB_ERR_ARG, "kb_us_upload: null argument");
   const kb::UsDev& d = U->d;
-  bool ok = cudaMemcpy(d.w, w, sizeof(double) * 4L * d.ncell, cudaMemcpyHostToDevice) == cudaSuccess &&
+  bool ok = cudaStreamSynchronize(U->stream) == cudaSuccess &&
+            cudaMemcpy(d.w, w, sizeof(double) * 4L * d.ncell, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(d.prim, prim, sizeof(double) * 4L * d.ncell, cudaMemcpyHostToDevice) == cudaSuccess;
   for (int k = 0; k < 2 && ok; ++k) {
     ok &= cudaMemcpy(U->stage, k == 0 ? h : b, sizeof(double) * (size_t)d.ncell * d.nvel,
                      cudaMemcpyHostToDevice) == cudaSuccess;
-    void* dst = k == 0 ? d.h : d.b;
+    void** dst = k == 0 ? U->h : U->b;
     if (U->prec == KB_PREC_FP64)
-      kb::k_us_in<double><<<d.ncell, 128, 0, U->stream>>>((double*)dst, U->stage, d.ncell, d.nvel, d.vstride);
+      kb::k_us_in<double><<<d.ncell, 128, 0, U->stream>>>((double*)dst[0], (double*)dst[1], U->stage,
+                                                          d.nvel, d.vstride);
     else
-      kb::k_us_in<float><<<d.ncell, 128, 0, U->stream>>>((float*)dst, U->stage, d.ncell, d.nvel, d.vstride);
+      kb::k_us_in<float><<<d.ncell, 128, 0, U->stream>>>((float*)dst[0], (float*)dst[1], U->stage,
+                                                         d.nvel, d.vstride);
     U->launches++;
     ok &= cudaStreamSynchronize(U->stream) == cudaSuccess;
   }
+  U->cur = 0;
   ok &= cudaMemset(d.status, 0, sizeof(int)) == cudaSuccess;
   if (!ok) return usfail(KB_ERR_CUDA, "kb_us_upload failed");
   return KB_OK;
@@ -509,11 +814,11 @@ extern "C" int kb_us_download(kb_us_t* U, double* w, double* prim, double* h, do
   for (int k = 0; k < 2 && ok; ++k) {
     double* dst = k == 0 ? h : b;
     if (!dst) continue;
-    const void* src = k == 0 ? d.h : d.b;
+    const void* src = k == 0 ? U->h[U->cur] : U->b[U->cur];
     if (U->prec == KB_PREC_FP64)
-      kb::k_us_out<double><<<d.ncell, 128, 0, U->stream>>>(U->stage, (const double*)src, d.ncell, d.nvel, d.vstride);
+      kb::k_us_out<double><<<d.ncell, 128, 0, U->stream>>>(U->stage, (const double*)src, d.nvel, d.vstride);
     else
-      kb::k_us_out<float><<<d.ncell, 128, 0, U->stream>>>(U->stage, (const float*)src, d.ncell, d.nvel, d.vstride);
+      kb::k_us_out<float><<<d.ncell, 128, 0, U->stream>>>(U->stage, (const float*)src, d.nvel, d.vstride);
     U->launches++;
     ok &= cudaStreamSynchronize(U->stream) == cudaSuccess;
     ok &= cudaMemcpy(dst, U->stage, sizeof(double) * (size_t)d.ncell * d.nvel, cudaMemcpyDeviceToHost) ==
@@ -539,20 +844,38 @@ extern "C" int kb_us_timestep(kb_us_t* U, double cfl, double sim_time, double ma
   return KB_OK;
 }
 
+template <typename R>
+static void us_enqueue_step(kb_us* U, double dt) {
+  const kb::UsDev& d = U->d;
+  const R* hin = (const R*)U->h[U->cur];
+  const R* bin = (const R*)U->b[U->cur];
+  R* hout = (R*)U->h[U->cur ^ 1];
+  R* bout = (R*)U->b[U->cur ^ 1];
+  if (d.nstep) {
+    const int grid = (d.nstep + U->cb - 1) / U->cb;
+    if (d.coll == KB_COLL_SHAKHOV)
+      kb::k_us_step<R, true><<<grid, kb::US_T, U->smem, U->stream>>>(d, dt, U->cb, hin, bin, hout, bout);
+    else
+      kb::k_us_step<R, false><<<grid, kb::US_T, U->smem, U->stream>>>(d, dt, U->cb, hin, bin, hout, bout);
+    U->launches++;
+  }
+  for (size_t l = 0; l + 1 < U->level_first.size(); ++l) {
+    const int n = U->level_first[l + 1] - U->level_first[l];
+    if (n == 0) continue;
+    kb::k_us_avg<R><<<n, kb::US_T, 0, U->stream>>>(d, U->level_first[l], hin, bin, hout, bout);
+    U->launches++;
+  }
+  U->cur ^= 1;
+}
+
 extern "C" int kb_us_step(kb_us_t* U, double dt, int32_t nsteps, double* residual) {
   if (!U || nsteps < 0) return usfail(KB_ERR_ARG, "kb_us_step: bad argument");
   const kb::UsDev& d = U->d;
   for (int s = 0; s < nsteps; ++s) {
-    if (U->prec == KB_PREC_FP64) {
-      kb::k_us_face<double><<<d.nface, kb::US_T, 0, U->stream>>>(d, dt);
-      kb::k_us_cell<double><<<d.ncell, kb::US_T, 0, U->stream>>>(d, dt);
-      if (d.navg) kb::k_us_avg<double><<<1, kb::US_T, 0, U->stream>>>(d);
-    } else {
-      kb::k_us_face<float><<<d.nface, kb::US_T, 0, U->stream>>>(d, dt);
-      kb::k_us_cell<float><<<d.ncell, kb::US_T, 0, U->stream>>>(d, dt);
-      if (d.navg) kb::k_us_avg<float><<<1, kb::US_T, 0, U->stream>>>(d);
-    }
-    U->launches += d.navg ? 3 : 2;
+    if (U->prec == KB_PREC_FP64)
+      us_enqueue_step<double>(U, dt);
+    else
+      us_enqueue_step<float>(U, dt);
   }
   kb::k_us_residual<<<1, kb::US_T, 0, U->stream>>>(d);
   U->launches++;
@@ -568,5 +891,23 @@ extern "C" int kb_us_step(kb_us_t* U, double dt, int32_t nsteps, double* residua
 extern "C" int kb_us_info(kb_us_t* U, int64_t* launches) {
   if (!U || !launches) return usfail(KB_ERR_ARG, "kb_us_info: null argument");
   *launches = U->launches;
+  return KB_OK;
+}
+
+extern "C" int kb_us_set_tuning(kb_us_t* U, int32_t cells_per_cta) {
+  if (!U) return usfail(KB_ERR_ARG, "kb_us_set_tuning: null handle");
+  if (cudaStreamSynchronize(U->stream) != cudaSuccess) return usfail(KB_ERR_CUDA, "kb_us_set_tuning");
+  return us_set_cells_per_cta(U, cells_per_cta);
+}
+
+extern "C" int kb_us_get_tuning(kb_us_t* U, int32_t* cells_per_cta) {
+  if (!U || !cells_per_cta) return usfail(KB_ERR_ARG, "kb_us_get_tuning: null argument");
+  *cells_per_cta = U->cb;
+  return KB_OK;
+}
+
+extern "C" int kb_us_stream(kb_us_t* U, void** stream) {
+  if (!U || !stream) return usfail(KB_ERR_ARG, "kb_us_stream: null argument");
+  *stream = (void*)U->stream;
   return KB_OK;
 }

@@ -143,3 +143,44 @@ def autotune_batch(batch, steps=100, use_cache=True, verbose=False):
         cache[key] = best
         _save(cache)
     return best, {"seg%d-t%d-p%d" % k: v for k, v in res.items()}
+
+
+US_CELLS_PER_CTA = (4, 8, 12, 16, 24, 32)
+
+
+def unstruct_signature(hd):
+    size = "small" if hd.ncell < 4096 else ("medium" if hd.ncell < 65536 else "large")
+    return "us-v%d-c%d-p%d-%s" % (hd.nvel, hd.cfg.collision, hd.cfg.precision, size)
+
+
+def autotune_unstruct(hd, dt, steps=20, use_cache=True, verbose=False):
+    """Pick the fastest stepped-cells-per-CTA shape of the unstructured step
+    for handle `hd` (kitgpu.unstruct.UnstructHandle) by timing `steps` steps of
+    each candidate on the live state (kb_us_step returns after synchronising
+    the solve's stream; the search advances the state).  Returns the chosen
+    count and the per-candidate ms per step."""
+    import time
+    key = unstruct_signature(hd)
+    cache = _load() if use_cache else {}
+    if use_cache and key in cache:
+        best = cache[key]["cells_per_cta"]
+        hd.set_tuning(best)
+        return best, None
+    res = {}
+    for cb in US_CELLS_PER_CTA:
+        try:
+            hd.set_tuning(cb)
+        except N.KitGPUError:
+            continue  # more shared memory than a CTA may have
+        hd.step(dt, 2)
+        t0 = time.perf_counter()
+        hd.step(dt, steps)
+        res[cb] = 1e3 * (time.perf_counter() - t0) / steps
+        if verbose:
+            print("unstructured cells/CTA=%d: %.4f ms" % (cb, res[cb]), flush=True)
+    best = min(res, key=res.get)
+    hd.set_tuning(best)
+    if use_cache:
+        cache[key] = {"cells_per_cta": best}
+        _save(cache)
+    return best, {"cb%d" % k: v for k, v in res.items()}

@@ -1,4 +1,4 @@
-"""Unstructured 2D2F2V (triangle meshes) on the GPU: host side.
+"""Unstructured 2D2F2V and 2D1F2V (triangle meshes) on the GPU: host side.
 
 The reference builds an `UnstructPSpace` (src/Geometry/geo_unstruct.jl:10-38)
 from a gmsh file with FiniteMesh.jl 0.3 (`read_mesh`, `mesh_connectivity_2D`;
@@ -31,6 +31,13 @@ Only first-order, KFVS is covered: the reference's US2F `evolve!` computes
 fluxes for `mode == :kfvs` only, and its second-order slopes divide by the
 x / y offsets of neighbouring cell centres (reconstruct4!,
 src/Reconstruction/reconstruction.jl:217-235), which vanish on general meshes.
+
+2D1F2V (space "2d1f2v": `evolve!` / `update!` / `update_boundary!` US1F,
+src/Solver/solver_evolution.jl:872-947, src/Solver/solver_update.jl:359-403,
+src/Solver/update_boundary.jl:546-566, with the 2D1F2V triangle `step!`,
+src/Solver/step_1f.jl:228-285) runs on the same device solver with b held at
+zero; it is BGK only, since that `step!` reads h and b, which a 1F cell
+does not have, under Shakhov.
 """
 import ctypes
 import math
@@ -175,50 +182,49 @@ def build_mesh(points, cells, boundary="fix"):
     points = np.asarray(points, dtype=np.float64)
     cells = np.asarray(cells, dtype=np.int64)
     nc = len(cells)
-    edge_id = {}
-    fp, fc = [], []
-    cf = np.zeros((nc, 3), dtype=np.int64)
-    for c in range(nc):
-        for j in range(3):
-            a, b = int(cells[c, j]), int(cells[c, (j + 1) % 3])
-            key = (min(a, b), max(a, b))
-            f = edge_id.get(key)
-            if f is None:
-                f = len(fp)
-                edge_id[key] = f
-                fp.append((a, b))
-                fc.append([c, -1])
-            else:
-                if fc[f][1] != -1:
-                    raise ValueError("edge %s shared by more than two triangles" % (key,))
-                fc[f][1] = c
-            cf[c, j] = f
-    fp = np.array(fp, dtype=np.int64)
-    fc = np.array(fc, dtype=np.int64)
-    nb = np.full((nc, 3), -1, dtype=np.int64)
-    for c in range(nc):
-        for j in range(3):
-            f = cf[c, j]
-            nb[c, j] = fc[f, 1] if fc[f, 0] == c else fc[f, 0]
-    center = np.array([(points[t[0]] + points[t[1]] + points[t[2]]) / 3.0 for t in cells])
-    area = np.array([0.5 * abs((points[t[1], 0] - points[t[0], 0]) * (points[t[2], 1] - points[t[0], 1])
-                               - (points[t[2], 0] - points[t[0], 0]) * (points[t[1], 1] - points[t[0], 1]))
-                     for t in cells])
-    cdx = np.array([[point_distance(center[c], points[cells[c, j]], points[cells[c, (j + 1) % 3]])
-                     for j in range(3)] for c in range(nc)])
-    fcen = 0.5 * (points[fp[:, 0]] + points[fp[:, 1]])
-    flen = np.array([math.sqrt((points[a, 0] - points[b, 0]) ** 2 + (points[a, 1] - points[b, 1]) ** 2)
-                     for a, b in fp])
-    fn = np.zeros((len(fp), 2))
-    for f, (a, b) in enumerate(fp):
-        n = unit_normal(points[a], points[b])
-        if fc[f, 1] != -1:
-            n0 = center[fc[f, 1]] - center[fc[f, 0]]
-        else:
-            n0 = center[fc[f, 0]] - fcen[f]
-        if n[0] * n0[0] + n[1] * n0[1] < 0:
-            n = -n
-        fn[f] = n
+    # edge k = 3 c + j joins (cells[c, j], cells[c, j + 1]); faces are the
+    # distinct edges numbered by their first appearance in k
+    ea = cells.reshape(-1)
+    eb = cells[:, [1, 2, 0]].reshape(-1)
+    key = np.minimum(ea, eb) * (int(ea.max(initial=0)) + 1 if nc else 1) + np.maximum(ea, eb)
+    _, first, inv, cnt = np.unique(key, return_index=True, return_inverse=True, return_counts=True)
+    if (cnt > 2).any():
+        raise ValueError("an edge is shared by more than two triangles")
+    order = np.argsort(first, kind="stable")          # unique-key slot -> face order
+    rank = np.empty_like(order)
+    rank[order] = np.arange(len(order))
+    edge_face = rank[inv.reshape(-1)]                 # edge k -> face
+    cf = edge_face.reshape(nc, 3)
+    fk = first[order]                                 # first edge of each face
+    fp = np.stack([ea[fk], eb[fk]], axis=1)
+    fc = np.full((len(fk), 2), -1, dtype=np.int64)
+    fc[:, 0] = fk // 3
+    k = np.arange(3 * nc)
+    second = k[k != fk[edge_face]]
+    fc[edge_face[second], 1] = second // 3
+    nb = np.where(fc[cf, 0] == np.arange(nc)[:, None], fc[cf, 1], fc[cf, 0])
+    P0, P1, P2 = points[cells[:, 0]], points[cells[:, 1]], points[cells[:, 2]]
+    center = (P0 + P1 + P2) / 3.0
+    area = 0.5 * np.abs((P1[:, 0] - P0[:, 0]) * (P2[:, 1] - P0[:, 1])
+                        - (P2[:, 0] - P0[:, 0]) * (P1[:, 1] - P0[:, 1]))
+    # point_distance of the centre to each edge (src/Geometry/geo_general.jl:260-267)
+    A, B = points[ea].reshape(nc, 3, 2), points[eb].reshape(nc, 3, 2)
+    x0, y0 = center[:, None, 0], center[:, None, 1]
+    x1, y1, x2, y2 = A[..., 0], A[..., 1], B[..., 0], B[..., 1]
+    cdx = np.abs((x2 - x1) * (y1 - y0) - (x1 - x0) * (y2 - y1)) / np.sqrt(
+        (x2 - x1) ** 2 + (y2 - y1) ** 2 + 1e-6)
+    pa, pb = points[fp[:, 0]], points[fp[:, 1]]
+    fcen = 0.5 * (pa + pb)
+    flen = np.sqrt((pa[:, 0] - pb[:, 0]) ** 2 + (pa[:, 1] - pb[:, 1]) ** 2)
+    # unit_normal (src/Geometry/geo_general.jl:230-235), turned towards the
+    # second cell, or into the cell at a boundary face
+    d = pb - pa
+    ln = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + 1e-6
+    fn = np.stack([-d[:, 1] / ln, d[:, 0] / ln], axis=1)
+    inner = fc[:, 1] != -1
+    n0 = np.where(inner[:, None], center[np.where(inner, fc[:, 1], 0)] - center[fc[:, 0]],
+                  center[fc[:, 0]] - fcen)
+    fn[fn[:, 0] * n0[:, 0] + fn[:, 1] * n0[:, 1] < 0] *= -1.0
     ctype = np.zeros(nc, dtype=np.int64)
     bnd = (nb == -1).any(axis=1)
     if boundary == "fix":
@@ -250,15 +256,18 @@ class UnstructSolverSet:
 
 def unstruct_solver_set(mesh, nu=16, nv=16, umax=5.0, vmax=5.0, vmesh="rectangle", Kn=0.075,
                         Pr=1.0, inK=1.0, omega=0.72, collision="bgk", cfl=0.8, maxTime=1.0,
-                        prim_at=None):
-    """The reference's unstructured test setup (test/t1_2f.txt: KFVS, first
-    order, 16 x 16 velocities on [-5, 5]^2, Kn 0.075, Pr 1, inK 1) on `mesh`;
-    prim_at(x, y) gives the initial primitive state (default: rest, lambda 1)."""
-    s = Setup(matter="gas", case="unstructured", space="2d2f2v", flux="kfvs",
+                        prim_at=None, space="2d2f2v"):
+    """The reference's unstructured test setup (test/t1_2f.txt, or
+    test/t1_1f.txt with space = "2d1f2v": KFVS, first order, 16 x 16
+    velocities on [-5, 5]^2, Kn 0.075, Pr 1, inK 1) on `mesh`; prim_at(x, y)
+    gives the initial primitive state (default: rest, lambda 1)."""
+    if space not in ("2d2f2v", "2d1f2v"):
+        raise ValueError("unstructured spaces: 2d2f2v or 2d1f2v, not %r" % space)
+    s = Setup(matter="gas", case="unstructured", space=space, flux="kfvs",
               collision=collision, interpOrder=1, limiter="vanleer", boundary=["fix"] * 4,
               cfl=cfl, maxTime=maxTime)
     vs = VSpace2D.build(-umax, umax, nu, -vmax, vmax, nv, type=vmesh)
-    gas = gas_property(space="2d2f2v", inK=inK, knudsen=Kn, prandtl=Pr, omega=omega)
+    gas = gas_property(space=space, inK=inK, knudsen=Kn, prandtl=Pr, omega=omega)
     if prim_at is None:
         def prim_at(x, y):
             return np.array([1.0, 0.0, 0.0, 1.0])
@@ -266,24 +275,24 @@ def unstruct_solver_set(mesh, nu=16, nv=16, umax=5.0, vmax=5.0, vmesh="rectangle
     def fw(x, y):
         return prim_conserve(prim_at(x, y), gas.gamma)
 
-    return UnstructSolverSet(s, mesh, vs, gas, fw)
+    return UnstructSolverSet(s, mesh, vs, gas, fw, nf=1 if space == "2d1f2v" else 2)
 
 
 def initial_cells(KS):
     """w, prim [nc, 4] and h, b [nc, nu*nv] of init_fvm on the cell centres
-    (src/Solver/solver_init.jl:594-610)."""
+    (src/Solver/solver_init.jl:594-610; 2D1F2V :512-522, with b = 0)."""
     vs, gas = KS.vs, KS.gas
     u, v = vs.flat(vs.u), vs.flat(vs.v)
-    W, P, H, B = [], [], [], []
-    for x, y in KS.ps.cell_center:
-        w = np.asarray(KS.ib_fw(x, y), dtype=np.float64)
-        p = conserve_prim(w, gas.gamma)
-        h = maxwellian(u, p, v)
-        W.append(w)
-        P.append(p)
-        H.append(h)
-        B.append(h * gas.K / 2.0 / p[-1])
-    return np.array(W), np.array(P), np.array(H), np.array(B)
+    W = np.array([np.asarray(KS.ib_fw(x, y), dtype=np.float64) for x, y in KS.ps.cell_center])
+    # conserve_prim and maxwellian (src/Theory/theory_macro.jl:185-206,
+    # src/Theory/theory_equilibrium.jl:8-25), over all cells at once
+    r, m1, m2, E = W[:, 0], W[:, 1], W[:, 2], W[:, 3]
+    lam = 0.5 * r / (gas.gamma - 1.0) / (E - 0.5 * (m1 * m1 + m2 * m2) / r)
+    P = np.stack([r, m1 / r, m2 / r, lam], axis=1)
+    H = (P[:, 0:1] * (P[:, 3:4] / np.pi)
+         * np.exp(-P[:, 3:4] * ((u[None, :] - P[:, 1:2]) ** 2 + (v[None, :] - P[:, 2:3]) ** 2)))
+    B = H * gas.K / 2.0 / P[:, 3:4] if KS.nf == 2 else np.zeros_like(H)
+    return W, P, H, B
 
 
 _D = ctypes.POINTER(ctypes.c_double)
@@ -297,6 +306,9 @@ _US_SIGS = {
     "kb_us_timestep": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double, _D],
     "kb_us_step": [ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, _D],
     "kb_us_info": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)],
+    "kb_us_stream": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)],
+    "kb_us_set_tuning": [ctypes.c_void_p, ctypes.c_int32],
+    "kb_us_get_tuning": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)],
 }
 
 
@@ -333,7 +345,7 @@ class UnstructHandle:
         c.umax, c.vmax = vs.u1, vs.v1
         c.K, c.gamma, c.mu_ref, c.omega, c.Pr = gas.K, gas.gamma, gas.mu_ref, gas.omega, gas.Pr
         c.x0, c.x1, c.y0, c.y1 = 0.0, 1.0, 0.0, 1.0
-        c.nf = 2
+        c.nf = KS.nf
         self.cfg = c
         self.nvel = vs.nu * vs.nv
         self.ncell = m.ncell
@@ -384,6 +396,21 @@ class UnstructHandle:
         r = np.zeros(4)
         N.check(self.lib.kb_us_step(self.h, float(dt), int(n), N.ptr(r)))
         return r
+
+    def set_tuning(self, cells_per_cta=0):
+        """Stepped cells per CTA of the step kernel (0: the default)."""
+        N.check(self.lib.kb_us_set_tuning(self.h, int(cells_per_cta)))
+
+    def tuning(self):
+        n = ctypes.c_int32()
+        N.check(self.lib.kb_us_get_tuning(self.h, ctypes.byref(n)))
+        return n.value
+
+    def stream(self):
+        """The cudaStream_t (as an int) the solve's kernels run on."""
+        st = ctypes.c_void_p()
+        N.check(self.lib.kb_us_stream(self.h, ctypes.byref(st)))
+        return st.value or 0
 
     def launches(self):
         n = ctypes.c_int64()

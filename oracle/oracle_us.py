@@ -24,6 +24,13 @@ Restated (file:line of the reference):
   (src/Solver/step_2f.jl:256-326), heat_flux 2F2V and shakhov 2F2V
   (src/Theory/theory_moments.jl:567-578, src/Theory/theory_equilibrium.jl:227-238);
 - update_boundary! US2F (src/Solver/update_boundary.jl:575-594).
+2D1F2V (nf = 1), written from the reference's 1F functions, not from the 2F
+code above:
+- evolve! US1F, KFVS branch (src/Solver/solver_evolution.jl:872-947) with
+  flux_kfvs! 1F2V (src/Flux/flux_kfvs.jl:615-650) and flux_conserve! 1F2V;
+- update! US1F (src/Solver/solver_update.jl:359-403) with the 2D1F2V triangle
+  step! (src/Solver/step_1f.jl:228-285; BGK, the only collision it can run);
+- update_boundary! US1F (src/Solver/update_boundary.jl:546-566).
 """
 import math
 
@@ -58,11 +65,14 @@ class UnstructOracle:
     """One unstructured solve: cells from (points, triangles); cell types 0
     (stepped), 1 (fixed), 3 (mean of its two neighbours)."""
 
-    def __init__(self, points, tris, cell_type, u, v, wt, K, gamma, mu_ref, omega, Pr, coll):
+    def __init__(self, points, tris, cell_type, u, v, wt, K, gamma, mu_ref, omega, Pr, coll, nf=2):
         P = np.asarray(points, dtype=np.float64)
         T = np.asarray(tris, dtype=np.int64)
         self.u, self.v, self.wt = (np.asarray(a, dtype=np.float64) for a in (u, v, wt))
         self.K, self.g, self.mu, self.om, self.Pr, self.coll = K, gamma, mu_ref, omega, Pr, coll
+        self.nf = nf
+        if nf == 1 and coll != "bgk":
+            raise ValueError("the 2D1F2V triangle step! runs BGK only")
         self.type = np.asarray(cell_type)
         nc = len(T)
         self.center = P[T].mean(axis=1)
@@ -123,6 +133,8 @@ class UnstructOracle:
         return dt if dt < tmax_time - t else tmax_time - t
 
     def evolve(self, dt):
+        if self.nf == 1:
+            return self._evolve_1f(dt)
         nv = len(self.u)
         self.fw = np.zeros((len(self.faces), 4))
         self.fh = np.zeros((len(self.faces), nv))
@@ -143,6 +155,8 @@ class UnstructOracle:
             self.fh[k], self.fb[k] = fh, fb
 
     def update(self, dt):
+        if self.nf == 1:
+            return self._update_1f(dt)
         sumR, sumA = np.zeros(4), np.zeros(4)
         u, v, wt, K, Pr = self.u, self.v, self.wt, self.K, self.Pr
         for c in range(self.ncell):
@@ -184,6 +198,56 @@ class UnstructOracle:
                 self.w[c] = 0.5 * (self.w[ids[0]] + self.w[ids[1]])
                 self.h[c] = 0.5 * (self.h[ids[0]] + self.h[ids[1]])
                 self.b[c] = 0.5 * (self.b[ids[0]] + self.b[ids[1]])
+                self.prim[c] = conserve_prim(self.w[c], self.g)
+        return res
+
+    # ------------------------------------------------------------ 2D1F2V
+
+    def _evolve_1f(self, dt):
+        """evolve! US1F: ff = (dt vn f - 0.5 dt^2 vn^2 sf) len with sf = 0
+        (first order), fw = (sum w ff, sum w vn ff, sum w vt ff,
+        0.5 sum w (vn^2 + vt^2) ff), rotated by global_frame."""
+        nv = len(self.u)
+        self.fw = np.zeros((len(self.faces), 4))
+        self.fh = np.zeros((len(self.faces), nv))
+        self.fb = np.zeros((len(self.faces), nv))
+        for k, (c1, c2, n, ln) in enumerate(self.faces):
+            if c2 < 0:
+                continue
+            vn = self.u * n[0] + self.v * n[1]
+            vt = self.v * n[0] - self.u * n[1]
+            delta = np.where(vn >= 0.0, 1.0, 0.0)
+            f = self.h[c1] * delta + self.h[c2] * (1.0 - delta)
+            ff = (dt * vn * f) * ln
+            a = np.sum(self.wt * ff)
+            bn = np.sum(self.wt * vn * ff)
+            bt = np.sum(self.wt * vt * ff)
+            e = 0.5 * np.sum(self.wt * (vn * vn + vt * vt) * ff)
+            self.fw[k] = [a, bn * n[0] - bt * n[1], bn * n[1] + bt * n[0], e]
+            self.fh[k] = ff
+
+    def _update_1f(self, dt):
+        sumR, sumA = np.zeros(4), np.zeros(4)
+        for c in range(self.ncell):
+            if self.type[c] not in (0, 2):
+                continue
+            fs, dc = self.cell_face[c], self.dirc[c]
+            w, p, f = self.w[c], self.prim[c], self.h[c]
+            w_old = w.copy()
+            w -= (self.fw[fs[0]] * dc[0] + self.fw[fs[1]] * dc[1] + self.fw[fs[2]] * dc[2]) / self.area[c]
+            p[:] = conserve_prim(w, self.g)
+            sumR += (w - w_old) ** 2
+            sumA += np.abs(w)
+            M = maxwellian(self.u, self.v, p)
+            tau = self.mu * 2.0 * p[3] ** (1.0 - self.om) / p[0]
+            f[:] = (f - (self.fh[fs[0]] * dc[0] + self.fh[fs[1]] * dc[1] + self.fh[fs[2]] * dc[2])
+                    / self.area[c] + dt / tau * M) / (1.0 + dt / tau)
+        res = np.sqrt(sumR * self.ncell) / (sumA + 1.e-7)
+        for c in range(self.ncell):
+            if self.type[c] == 3:
+                i1, i2 = [i for i in self.nb[c] if i != -1][:2]
+                self.w[c] = 0.5 * (self.w[i1] + self.w[i2])
+                self.h[c] = 0.5 * (self.h[i1] + self.h[i2])
                 self.prim[c] = conserve_prim(self.w[c], self.g)
         return res
 

@@ -3,6 +3,7 @@ connectivity and geometry kitgpu builds against the oracle's independent
 construction, and the configurations the device solver refuses before any
 CUDA call."""
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -77,8 +78,9 @@ def _create(mesh, cell_type=None, **kw):
                             *[N.ptr(a) for a in keep[4:] + vel], ctypes.byref(h))
 
 
-@pytest.mark.parametrize("kw", [dict(interp_order=2), dict(flux=1), dict(flux=2), dict(nf=1), dict(dim=1)],
-                         ids=["second-order", "kcu", "ugks", "1f", "1d"])
+@pytest.mark.parametrize("kw", [dict(interp_order=2), dict(flux=1), dict(flux=2),
+                                dict(nf=1, collision=1), dict(dim=1)],
+                         ids=["second-order", "kcu", "ugks", "1f-shakhov", "1d"])
 def test_refused_configurations(kw):
     m = US.build_mesh(*US.rectangle_mesh(3, 3))
     assert _create(m, **kw) == -2
@@ -89,3 +91,49 @@ def test_maxwell_wall_cells_refused():
     m = US.build_mesh(*US.rectangle_mesh(3, 3))
     assert _create(m, cell_type=np.where(m.cell_type == 1, 2, m.cell_type)) == -2
     assert b"no method" in N.load().kb_last_error()
+
+
+REF_MESH = os.path.join(os.environ.get("KITBASE_REF", "/root/reference"), "test", "t1.msh")
+
+
+@pytest.mark.skipif(not os.path.exists(REF_MESH), reason="the reference's test mesh is not present")
+def test_reference_test_mesh():
+    """The reference's own unstructured test mesh (test/t1.msh, gmsh 4.1,
+    read by test/test_unstructure.jl through t1_2f.txt) loads through
+    read_gmsh, builds a closed triangulation of [0, 0.1] x [0, 0.3], agrees
+    with the oracle's construction, and gives the step count that test takes
+    (nt = maxTime / dt with maxTime 0.001, cfl 0.8, 16 x 16 velocities on
+    [-5, 5]^2, a uniform gas at rest)."""
+    P, T = US.read_gmsh(REF_MESH)
+    assert P.shape == (403, 2) and T.shape == (724, 3)
+    for bc in ("fix", "extra"):
+        m = US.build_mesh(P, T, boundary=bc)
+        assert abs(m.cell_area.sum() - 0.03) < 1e-15
+        nbf = m.face_cells[:, 1] == -1
+        on_edge = ((np.abs(m.face_center[nbf, 0]) < 1e-12) | (np.abs(m.face_center[nbf, 0] - 0.1) < 1e-12)
+                   | (np.abs(m.face_center[nbf, 1]) < 1e-12) | (np.abs(m.face_center[nbf, 1] - 0.3) < 1e-12))
+        assert on_edge.all()
+    KS = US.unstruct_solver_set(m, maxTime=0.001)
+    vs, g = KS.vs, KS.gas
+    o = OU.UnstructOracle(P, T, m.cell_type, vs.flat(vs.u), vs.flat(vs.v), vs.flat(vs.weights),
+                          g.K, g.gamma, g.mu_ref, g.omega, g.Pr, "bgk")
+    assert np.allclose(o.dx.min(axis=1), m.cell_dx.min(axis=1), rtol=1e-14)
+    o.set_state(*US.initial_cells(KS))
+    dt = o.timestep(0.8, 0.0, 0.001, vs.u1, vs.v1)
+    assert int(0.001 // dt) == 6
+
+
+def test_1f_setup():
+    """2D1F2V: gamma from inK as heat_capacity_ratio gives it
+    (src/Struct/struct_property.jl:476-492), b zero in the initial cells, the
+    oracle refuses Shakhov as the device does."""
+    m = US.build_mesh(*US.rectangle_mesh(4, 4))
+    KS = US.unstruct_solver_set(m, nu=4, nv=4, space="2d1f2v", inK=0.0)
+    assert KS.nf == 1 and KS.gas.gamma == 2.0
+    w, p, h, b = US.initial_cells(KS)
+    assert np.all(b == 0.0) and np.all(h > 0.0)
+    with pytest.raises(ValueError):
+        OU.UnstructOracle(m.points, m.cells, m.cell_type, [0.0], [0.0], [1.0], 0.0, 2.0, 1e-3,
+                          0.72, 1.0, "shakhov", nf=1)
+    with pytest.raises(ValueError):
+        US.unstruct_solver_set(m, space="1d1f1v")
