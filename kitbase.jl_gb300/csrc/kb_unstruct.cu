@@ -42,17 +42,19 @@
 
 namespace kb {
 
+// FP64 face record of a stepped cell (32-byte aligned, one vector load pair)
+struct alignas(32) UsG64 {
+  double n1, n2, len, sgn;
+};
+
 struct UsDev {
   int ncell, nface, nvel, vstride, coll, nstep, navg;
-  const int* face_cells;     // [nface][2], -1 where no cell
-  const int* cell_faces;     // [ncell][3]
   const int* cell_nb;        // [ncell][3], -1 where no cell
   const int* cell_type;      // [ncell]: 0 stepped, 1 fixed, 3 mean of two neighbours
-  const int* step_list;      // type-0 cells [nstep]
+  const int4* step_rec;      // [nstep] stepped (type-0) cell, its neighbours over its faces 0..2
+  const float4* step_geo32;  // [nstep][3] per face: n1, n2, len, sg |n|^2 (FP32 form)
+  const UsG64* step_geo64;   // [nstep][3] the same in FP64
   const int* avg_list;       // type-3 cells by dependency level [navg]
-  const double* face_n;      // [nface][2]
-  const double* face_len;    // [nface]
-  const float4* face_geo;    // [nface] FP32 n1, n2, len, |n|^2 (the FP32 form)
   const double* cell_area;   // [ncell]
   const double* cell_mindx;  // [ncell] smallest centre-to-edge distance
   const double* u;           // velocity grid, FP64
@@ -63,7 +65,7 @@ struct UsDev {
   const float* wtf;
   double* w;      // [ncell][4]
   double* prim;   // [ncell][4]
-  double* cres;   // [ncell][8]: (w - w_old)^2, |w| of the last step
+  double* bres;   // [step CTAs][8]: sums of (w - w_old)^2, |w| over each CTA's cells, last step
   double* tmax;   // [1]
   double* residual;  // [4]
   int* status;
@@ -154,6 +156,71 @@ template <typename R> struct Vec2;
 template <> struct Vec2<float> { using T = float2; };
 template <> struct Vec2<double> { using T = double2; };
 
+// Packed FP32 pair arithmetic (one instruction for both velocities of a
+// lane's pair) and the base-2 exponential of a pre-scaled argument.
+__device__ __forceinline__ float2 p2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 p2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 p2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 p2sub(float2 a, float2 b) {
+  unsigned long long A = *reinterpret_cast<unsigned long long*>(&a);
+  unsigned long long B = *reinterpret_cast<unsigned long long*>(&b), C;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(C) : "l"(A), "l"(B));
+  return *reinterpret_cast<float2*>(&C);
+}
+__device__ __forceinline__ float2 p2s(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float us_ex2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float2 p2ex2(float2 a) { return make_float2(us_ex2(a.x), us_ex2(a.y)); }
+
+// Outward first-order KFVS flux of one face for a velocity pair, FP32 form:
+// with vo = u no1 + v no2 the normal velocity along the cell's outward
+// normal (sg n) and ao = (dt len) vo, the flux out of the cell is
+// max(ao, 0) h_cell + min(ao, 0) h_neighbour (heaviside(0) = 1 and a zero
+// normal velocity carries nothing).  Its neighbour forms exactly the
+// negated value (negation is exact), so both cells of a face agree bit for
+// bit.
+__device__ __forceinline__ void us_flux2(float no1, float no2, float a, float2 u2, float2 v2, float2 hc,
+                                         float2 bc, float2 hn, float2 bn, float2& fh, float2& fb) {
+  const float2 ao = p2mul(p2s(a), p2fma(u2, p2s(no1), p2mul(v2, p2s(no2))));
+  const float2 ap = make_float2(fmaxf(ao.x, 0.f), fmaxf(ao.y, 0.f));
+  const float2 am = make_float2(fminf(ao.x, 0.f), fminf(ao.y, 0.f));
+  fh = p2fma(ap, hc, p2mul(am, hn));
+  fb = p2fma(ap, bc, p2mul(am, bn));
+}
+
+// A stepped cell's face geometry: normal, length and sg |n|^2 (its sign is
+// the orientation: + where the cell is the face's first cell)
+template <typename R>
+struct UsGeo {
+  R n1, n2, len, sgn;
+};
+
+__device__ __forceinline__ void us_load_rec(const UsDev& d, int s, int4& rec, UsGeo<float> (&g)[3]) {
+  rec = __ldg(d.step_rec + s);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const float4 q = __ldg(d.step_geo32 + 3L * s + j);
+    g[j].n1 = q.x;
+    g[j].n2 = q.y;
+    g[j].len = q.z;
+    g[j].sgn = q.w;
+  }
+}
+__device__ __forceinline__ void us_load_rec(const UsDev& d, int s, int4& rec, UsGeo<double> (&g)[3]) {
+  rec = __ldg(d.step_rec + s);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const UsG64 q = d.step_geo64[3L * s + j];
+    g[j].n1 = q.n1;
+    g[j].n2 = q.n2;
+    g[j].len = q.len;
+    g[j].sgn = q.sgn;
+  }
+}
+
 // One CTA of US_T threads steps cb consecutive cells of the step list:
 // (1) each warp takes cells wid, wid + 4, ..., forms Dh, Db (kept in shared
 // memory, two velocities per lane and iteration) and the cell's velocity
@@ -165,7 +232,7 @@ template <> struct Vec2<double> { using T = double2; };
 // fraction of the FP32 rate, so per-cell FP64 work is kept to the lane-per-
 // cell phase).
 template <typename R, bool SHAK>
-__global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? 6 : 3)
+__global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? 5 : 3)
     k_us_step(UsDev d, double dt, int cb, const R* __restrict__ hin,
                                                   const R* __restrict__ bin, R* __restrict__ hout,
                                                   R* __restrict__ bout) {
@@ -186,34 +253,29 @@ __global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? 6 : 3)
   constexpr bool shak = SHAK;
   const R rdt = R(dt);
 
-  // (1) face fluxes and velocity sums
+  // (1) face fluxes and velocity sums.  Each stepped cell's record (the
+  // cell, its three neighbours, and per face n1, n2, len and sg |n|^2) is
+  // one contiguous read, fetched a cell ahead.
+  int4 rec = make_int4(0, 0, 0, 0);
+  UsGeo<R> geo[3];
+  if (wid < nloc) us_load_rec(d, c0 + wid, rec, geo);
   for (int i = wid; i < nloc; i += US_W) {
-    const int c = d.step_list[c0 + i];
+    const int c = rec.x;
     UsFace<R> F[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      const int f = d.cell_faces[3 * c + j];
-      const int L = d.face_cells[2 * f], Rc = d.face_cells[2 * f + 1];
-      const R sg = L == c ? R(1) : R(-1);
-      if (FAST) {
-        const float4 g = d.face_geo[f];  // n1, n2, len, |n|^2
-        F[j].n1 = R(g.x);
-        F[j].n2 = R(g.y);
-        F[j].a = rmul(rdt, R(g.z));
-        F[j].l = R(1);
-        F[j].sgn = sg * R(g.w);
-      } else {
-        const double n1 = d.face_n[2 * f], n2 = d.face_n[2 * f + 1];
-        F[j].n1 = R(n1);
-        F[j].n2 = R(n2);
-        F[j].a = R(dt);
-        F[j].l = R(d.face_len[f]);
-        F[j].sgn = sg * R(n1 * n1 + n2 * n2);
-      }
-      F[j].sg = sg;
-      F[j].left = L == c;
-      F[j].nb = L == c ? Rc : L;
+      F[j].n1 = geo[j].n1;
+      F[j].n2 = geo[j].n2;
+      F[j].a = FAST ? rmul(rdt, geo[j].len) : R(dt);
+      F[j].l = FAST ? R(1) : geo[j].len;
+      F[j].sgn = geo[j].sgn;
+      F[j].left = geo[j].sgn > R(0);
+      F[j].sg = F[j].left ? R(1) : R(-1);
     }
+    F[0].nb = rec.y;
+    F[1].nb = rec.z;
+    F[2].nb = rec.w;
+    if (i + US_W < nloc) us_load_rec(d, c0 + i + US_W, rec, geo);
     const R2* Hc = (const R2*)(hin + (long)c * vs);
     const R2* Bc = (const R2*)(bin + (long)c * vs);
     const R2* H0 = (const R2*)(hin + (long)F[0].nb * vs);
@@ -234,6 +296,59 @@ __global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? 6 : 3)
 #pragma unroll
     for (int k = 0; k < US_NM; ++k) pp[k] = R(0);
     int blk = 0;
+    if constexpr (FAST) {
+      float no[3][2], aa[3], nn[3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        no[j][0] = F[j].left ? F[j].n1 : -F[j].n1;
+        no[j][1] = F[j].left ? F[j].n2 : -F[j].n2;
+        aa[j] = F[j].a;
+        nn[j] = fabsf(F[j].sgn);
+      }
+      float2 Pk[US_NM];
+#pragma unroll
+      for (int k = 0; k < US_NM; ++k) Pk[k] = make_float2(0.f, 0.f);
+      const float2 Uo2 = p2s(Uo), Vo2 = p2s(Vo);
+      for (int q = lane; q < np; q += 32) {
+        const float2 u2 = U2[q], v2 = V2[q], w2 = W2[q];
+        const float2 hc2 = Hc[q], bc2 = Bc[q];
+        const float2 h0 = H0[q], b0 = B0[q], h1 = H1[q], b1 = B1[q], h2 = H2[q], b2 = B2[q];
+        float2 fh, fb, dh2, db2, dn2;
+        us_flux2(no[0][0], no[0][1], aa[0], u2, v2, hc2, bc2, h0, b0, fh, fb);
+        dh2 = fh;
+        db2 = fb;
+        dn2 = p2mul(p2s(nn[0]), fh);
+        us_flux2(no[1][0], no[1][1], aa[1], u2, v2, hc2, bc2, h1, b1, fh, fb);
+        dh2 = p2add(dh2, fh);
+        db2 = p2add(db2, fb);
+        dn2 = p2fma(p2s(nn[1]), fh, dn2);
+        us_flux2(no[2][0], no[2][1], aa[2], u2, v2, hc2, bc2, h2, b2, fh, fb);
+        dh2 = p2add(dh2, fh);
+        db2 = p2add(db2, fb);
+        dn2 = p2fma(p2s(nn[2]), fh, dn2);
+        Dh[q] = dh2;
+        Db[q] = db2;
+        const float2 wn = p2mul(w2, dn2);
+        Pk[0] = p2fma(w2, dh2, Pk[0]);
+        Pk[1] = p2fma(u2, wn, Pk[1]);
+        Pk[2] = p2fma(v2, wn, Pk[2]);
+        Pk[3] = p2fma(p2fma(u2, u2, p2mul(v2, v2)), wn, Pk[3]);
+        Pk[4] = p2fma(w2, db2, Pk[4]);
+        if (shak) {  // heat_flux 2F2V of the old state (src/Theory/theory_moments.jl:567-578)
+          const float2 cu = p2sub(u2, Uo2), cv = p2sub(v2, Vo2);
+          const float2 t = p2mul(w2, p2fma(p2fma(cu, cu, p2mul(cv, cv)), hc2, bc2));
+          Pk[5] = p2fma(cu, t, Pk[5]);
+          Pk[6] = p2fma(cv, t, Pk[6]);
+        }
+      }
+      // the pair partials (np / 32 pairs per lane) enter the compensated
+      // cross-lane sums
+#pragma unroll
+      for (int k = 0; k < US_NM; ++k) {
+        acc[k].add(Pk[k].x);
+        acc[k].add(Pk[k].y);
+      }
+    } else
     for (int q = lane; q < np; q += 32) {
       const R2 u2 = U2[q], v2 = V2[q], w2 = W2[q];
       const R2 hc2 = Hc[q], bc2 = Bc[q];
@@ -288,54 +403,60 @@ __global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? 6 : 3)
 
   // (2) the cell algebra, one lane per cell (step! 2D2F2V on a triangle,
   // src/Solver/step_2f.jl:256-326; 2D1F2V src/Solver/step_1f.jl:228-285)
-  if (wid == 0 && lane < nloc) {
-    const int c = d.step_list[c0 + lane];
-    const double* Sc = S + lane * US_NM;
-    double* w = d.w + 4L * c;
-    double* p = d.prim + 4L * c;
-    const double rho_o = p[0], U_o = p[1], V_o = p[2], lam_o = p[3];
-    const double ia = 1.0 / d.cell_area[c];
-    const double A[4] = {Sc[0], Sc[1], Sc[2], 0.5 * (Sc[3] + Sc[4])};
-    double wo[4], pn[4];
-    double* cr = d.cres + 8L * c;
-    for (int k = 0; k < 4; ++k) {
-      wo[k] = w[k];
-      w[k] -= A[k] * ia;
+  if (wid == 0) {
+    double rr[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (lane < nloc) {
+      const int c = d.step_rec[c0 + lane].x;
+      const double* Sc = S + lane * US_NM;
+      double* w = d.w + 4L * c;
+      double* p = d.prim + 4L * c;
+      const double rho_o = p[0], U_o = p[1], V_o = p[2], lam_o = p[3];
+      const double ia = 1.0 / d.cell_area[c];
+      const double A[4] = {Sc[0], Sc[1], Sc[2], 0.5 * (Sc[3] + Sc[4])};
+      double wo[4], pn[4];
+      for (int k = 0; k < 4; ++k) {
+        wo[k] = w[k];
+        w[k] -= A[k] * ia;
+      }
+      conserve_prim<FAST>(w, 4, d.gamma, pn);
+      for (int k = 0; k < 4; ++k) {
+        p[k] = pn[k];
+        rr[k] = (w[k] - wo[k]) * (w[k] - wo[k]);
+        rr[4 + k] = fabs(w[k]);
+      }
+      if (!(pn[0] > 0.0) || !(pn[3] > 0.0) || !isfinite(pn[0]) || !isfinite(pn[3])) atomicOr(d.status, 1);
+      const double k = dt / vhs_time<FAST>(pn[0], pn[3], d.mu_ref, d.omega);
+      R* Pc = P + lane * US_NP;
+      Pc[0] = R(pn[0] * (pn[3] / PI));  // Maxwellian amplitude
+      Pc[1] = R(pn[1]);
+      Pc[2] = R(pn[2]);
+      Pc[3] = R(pn[3]);
+      Pc[4] = R(d.Kb / (2.0 * pn[3]));  // B / H
+      Pc[5] = R(k);
+      Pc[6] = R(1.0 / (1.0 + k));
+      Pc[7] = R(ia);
+      if (shak) {  // shakhov 2F2V of the old state (src/Theory/theory_equilibrium.jl:227-238)
+        const double sfac = 0.8 * (1.0 - d.Pr) * (lam_o * lam_o) / rho_o;
+        Pc[8] = R(sfac * 0.5 * Sc[5]);
+        Pc[9] = R(sfac * 0.5 * Sc[6]);
+        Pc[10] = R(rho_o * (lam_o / PI));
+        Pc[11] = R(d.Kb / (2.0 * lam_o));
+        Pc[12] = R(lam_o);
+        Pc[13] = R(U_o);
+        Pc[14] = R(V_o);
+      }
     }
-    conserve_prim<FAST>(w, 4, d.gamma, pn);
-    for (int k = 0; k < 4; ++k) {
-      p[k] = pn[k];
-      cr[k] = (w[k] - wo[k]) * (w[k] - wo[k]);
-      cr[4 + k] = fabs(w[k]);
-    }
-    if (!(pn[0] > 0.0) || !(pn[3] > 0.0) || !isfinite(pn[0]) || !isfinite(pn[3])) atomicOr(d.status, 1);
-    const double k = dt / vhs_time<FAST>(pn[0], pn[3], d.mu_ref, d.omega);
-    R* Pc = P + lane * US_NP;
-    Pc[0] = R(pn[0] * (pn[3] / PI));  // Maxwellian amplitude
-    Pc[1] = R(pn[1]);
-    Pc[2] = R(pn[2]);
-    Pc[3] = R(pn[3]);
-    Pc[4] = R(d.Kb / (2.0 * pn[3]));  // B / H
-    Pc[5] = R(k);
-    Pc[6] = R(1.0 / (1.0 + k));
-    Pc[7] = R(ia);
-    if (shak) {  // shakhov 2F2V of the old state (src/Theory/theory_equilibrium.jl:227-238)
-      const double sfac = 0.8 * (1.0 - d.Pr) * (lam_o * lam_o) / rho_o;
-      Pc[8] = R(sfac * 0.5 * Sc[5]);
-      Pc[9] = R(sfac * 0.5 * Sc[6]);
-      Pc[10] = R(rho_o * (lam_o / PI));
-      Pc[11] = R(d.Kb / (2.0 * lam_o));
-      Pc[12] = R(lam_o);
-      Pc[13] = R(U_o);
-      Pc[14] = R(V_o);
-    }
+    // residual partials of update! (src/Solver/solver_update.jl:465-467)
+    // summed over the CTA's cells in a fixed order
+    const double t = us_reduce8(rr, lane);
+    if ((lane & 3) == 0) d.bres[8L * blockIdx.x + (lane >> 2)] = t;
   }
   __syncthreads();
 
   // (3) relaxation of h, b
   const R Km5 = R(d.Kb - 5.0), Km3 = R(d.Kb - 3.0);
   for (int i = wid; i < nloc; i += US_W) {
-    const int c = d.step_list[c0 + i];
+    const int c = d.step_rec[c0 + i].x;
     const R* Pc = P + i * US_NP;
     const R rn = Pc[0], U = Pc[1], V = Pc[2], lam = Pc[3], cB = Pc[4];
     const R kk = Pc[5], i1k = Pc[6], ia = Pc[7];
@@ -355,6 +476,26 @@ __global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? 6 : 3)
     const R2* Db = (const R2*)(D + (long)i * 2 * vs + vs);
     R2* Ho = (R2*)(hout + (long)c * vs);
     R2* Bo = (R2*)(bout + (long)c * vs);
+    if constexpr (FAST) {
+      const float nl = -float(LOG2E) * lam, onl = -float(LOG2E) * olam;
+      for (int q = lane; q < np; q += 32) {
+        const float2 u2 = U2[q], v2 = V2[q], hc2 = Hc[q], bc2 = Bc[q], dh2 = Dh[q], db2 = Db[q];
+        const float2 du = p2sub(u2, p2s(U)), dv = p2sub(v2, p2s(V));
+        float2 MH = p2mul(p2s(rn), p2ex2(p2mul(p2s(nl), p2fma(du, du, p2mul(dv, dv)))));
+        float2 MB = p2mul(p2s(cB), MH);
+        if (shak) {
+          const float2 cu = p2sub(u2, p2s(Uo)), cv = p2sub(v2, p2s(Vo));
+          const float2 c2 = p2fma(cu, cu, p2mul(cv, cv));
+          const float2 MHo = p2mul(p2s(orn), p2ex2(p2mul(p2s(onl), c2)));
+          const float2 fq = p2fma(p2s(fq0), cu, p2mul(p2s(fq1), cv));
+          const float2 tl = p2mul(p2s(2.f * olam), c2);
+          MH = p2fma(p2mul(fq, p2add(tl, p2s(Km5))), MHo, MH);
+          MB = p2fma(p2mul(fq, p2add(tl, p2s(Km3))), p2mul(p2s(ocB), MHo), MB);
+        }
+        Ho[q] = p2mul(p2fma(p2s(kk), MH, p2fma(dh2, p2s(-ia), hc2)), p2s(i1k));
+        Bo[q] = p2mul(p2fma(p2s(kk), MB, p2fma(db2, p2s(-ia), bc2)), p2s(i1k));
+      }
+    } else
     for (int q = lane; q < np; q += 32) {
       const R2 u2 = U2[q], v2 = V2[q], hc2 = Hc[q], bc2 = Bc[q], dh2 = Dh[q], db2 = Db[q];
       R2 ho, bo;
@@ -418,33 +559,22 @@ __global__ void __launch_bounds__(US_T) k_us_avg(UsDev d, int first, const R* __
 }
 
 // residual of update! US2F: sqrt(sum (w - w_old)^2 * ncell) / (sum |w| + 1e-7)
-// over the stepped cells (src/Solver/solver_update.jl:465-467); chunked sums
-// in cell order, then a fixed tree (deterministic)
-__device__ __forceinline__ double us_block_sum(double x, double* red) {
-  red[threadIdx.x] = x;
+// over the stepped cells (src/Solver/solver_update.jl:465-467) from the step
+// CTAs' partials: strided sums, then a fixed tree (deterministic)
+__global__ void __launch_bounds__(256) k_us_residual(UsDev d, int nblk) {
+  __shared__ double red[8][256];
+  double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int b = threadIdx.x; b < nblk; b += 256)
+    for (int k = 0; k < 8; ++k) a[k] += d.bres[8L * b + k];
+  for (int k = 0; k < 8; ++k) red[k][threadIdx.x] = a[k];
   __syncthreads();
-  for (int s = US_T / 2; s >= 1; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+  for (int s = 128; s >= 1; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int k = 0; k < 8; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s];
     __syncthreads();
   }
-  const double r = red[0];
-  __syncthreads();
-  return r;
-}
-
-__global__ void __launch_bounds__(US_T) k_us_residual(UsDev d) {
-  __shared__ double red[US_T];
-  const int per = (d.ncell + US_T - 1) / US_T;
-  const int c0 = threadIdx.x * per, c1 = min(d.ncell, c0 + per);
-  for (int k = 0; k < 4; ++k) {
-    double r = 0.0, a = 0.0;
-    for (int c = c0; c < c1; ++c) {
-      r += d.cres[8L * c + k];
-      a += d.cres[8L * c + 4 + k];
-    }
-    const double Rs = us_block_sum(r, red), As = us_block_sum(a, red);
-    if (threadIdx.x == 0) d.residual[k] = sqrt(Rs * d.ncell) / (As + 1.e-7);
-  }
+  if (threadIdx.x < 4)
+    d.residual[threadIdx.x] = sqrt(red[threadIdx.x][0] * d.ncell) / (red[4 + threadIdx.x][0] + 1.e-7);
 }
 
 // timestep for unstructured cells (src/Solver/solver_main.jl:398-420):
@@ -498,6 +628,7 @@ struct kb_us {
   int cur = 0;
   std::vector<int> level_first;  // avg_list offsets of the dependency levels (+ end)
   int cb = 1;                    // stepped cells per CTA
+  int nblk = 0;                  // CTAs of the last step launch (residual partial rows)
   size_t smem = 0;               // dynamic shared memory of the step kernel
 };
 
@@ -681,19 +812,19 @@ extern "C" int kb_us_create(const kb_config_t* cfg, int32_t ncell, int32_t nface
 #define USALLOC(dst, T, count)                                                        \
   if ((rc = usalloc(U, &p, sizeof(T) * (size_t)(count))) != KB_OK) return bail(rc); \
   dst = (T*)p;
-  int *fc, *cf, *nbp, *ct, *sl, *al, *st;
-  double *fn, *fl, *ca, *cm, *du, *dv, *dw, *tm, *res;
+  int *nbp, *ct, *al, *st;
+  int4* srec;
+  float4* sg32;
+  kb::UsG64* sg64;
+  double *ca, *cm, *du, *dv, *dw, *tm, *res;
   float *fu, *fv, *fwt;
-  float4* geo;
-  USALLOC(fc, int, 2 * nface);
-  USALLOC(cf, int, 3 * ncell);
   USALLOC(nbp, int, 3 * ncell);
   USALLOC(ct, int, ncell);
-  USALLOC(sl, int, steps.size() + 1);
+  USALLOC(srec, int4, steps.size() + 1);
+  USALLOC(sg32, float4, 3 * steps.size() + 1);
+  USALLOC(sg64, kb::UsG64, 3 * steps.size() + 1);
   USALLOC(al, int, avg.size() + 1);
   USALLOC(st, int, 1);
-  USALLOC(fn, double, 2 * nface);
-  USALLOC(fl, double, nface);
   USALLOC(ca, double, ncell);
   USALLOC(cm, double, ncell);
   USALLOC(du, double, d.vstride);
@@ -702,12 +833,11 @@ extern "C" int kb_us_create(const kb_config_t* cfg, int32_t ncell, int32_t nface
   USALLOC(fu, float, d.vstride);
   USALLOC(fv, float, d.vstride);
   USALLOC(fwt, float, d.vstride);
-  USALLOC(geo, float4, nface);
   USALLOC(tm, double, 1);
   USALLOC(res, double, 4);
   USALLOC(d.w, double, 4L * ncell);
   USALLOC(d.prim, double, 4L * ncell);
-  USALLOC(d.cres, double, 8L * ncell);
+  USALLOC(d.bres, double, 8L * std::max(1, (int)steps.size()));
   USALLOC(U->stage, double, (long)ncell * d.nvel);
 #undef USALLOC
   for (void** q : {&U->h[0], &U->h[1], &U->b[0], &U->b[1]})
@@ -725,23 +855,37 @@ extern "C" int kb_us_create(const kb_config_t* cfg, int32_t ncell, int32_t nface
     f32[VS + k] = (float)v[k];
     f32[2 * VS + k] = (float)weights[k];
   }
-  std::vector<float4> g32(nface);
-  for (int f = 0; f < nface; ++f) {
-    const double n1 = face_n[2 * f], n2 = face_n[2 * f + 1];
-    g32[f] = make_float4((float)n1, (float)n2, (float)face_len[f], (float)(n1 * n1 + n2 * n2));
+  // stepped-cell records: the cell, its neighbours, and per face n1, n2,
+  // len and sg |n|^2 with sg = +1 where the cell is the face's first cell
+  std::vector<int4> r4(steps.size());
+  std::vector<float4> g32(3 * steps.size());
+  std::vector<kb::UsG64> g64(3 * steps.size());
+  for (size_t k = 0; k < steps.size(); ++k) {
+    const int c = steps[k];
+    int nbj[3];
+    for (int j = 0; j < 3; ++j) {
+      const int f = cell_faces[3 * c + j];
+      const bool left = face_cells[2 * f] == c;
+      nbj[j] = left ? face_cells[2 * f + 1] : face_cells[2 * f];
+      const double n1 = face_n[2 * f], n2 = face_n[2 * f + 1];
+      const double sgn = (left ? 1.0 : -1.0) * (n1 * n1 + n2 * n2);
+      g32[3 * k + j] = make_float4((float)n1, (float)n2, (float)face_len[f], (float)sgn);
+      g64[3 * k + j] = kb::UsG64{n1, n2, face_len[f], sgn};
+    }
+    r4[k] = make_int4(c, nbj[0], nbj[1], nbj[2]);
   }
   bool ok = true;
   auto up = [&](void* dst, const void* src, size_t bytes) {
     ok &= cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
   };
-  up(fc, face_cells, sizeof(int) * 2 * nface);
-  up(cf, cell_faces, sizeof(int) * 3 * ncell);
   up(nbp, cell_nb, sizeof(int) * 3 * ncell);
   up(ct, cell_type, sizeof(int) * ncell);
-  if (!steps.empty()) up(sl, steps.data(), sizeof(int) * steps.size());
+  if (!steps.empty()) {
+    up(srec, r4.data(), sizeof(int4) * steps.size());
+    up(sg32, g32.data(), sizeof(float4) * g32.size());
+    up(sg64, g64.data(), sizeof(kb::UsG64) * g64.size());
+  }
   if (!avg.empty()) up(al, avg.data(), sizeof(int) * avg.size());
-  up(fn, face_n, sizeof(double) * 2 * nface);
-  up(fl, face_len, sizeof(double) * nface);
   up(ca, cell_area, sizeof(double) * ncell);
   up(cm, cell_mindx, sizeof(double) * ncell);
   up(du, f64.data(), sizeof(double) * VS);
@@ -750,21 +894,17 @@ extern "C" int kb_us_create(const kb_config_t* cfg, int32_t ncell, int32_t nface
   up(fu, f32.data(), sizeof(float) * VS);
   up(fv, f32.data() + VS, sizeof(float) * VS);
   up(fwt, f32.data() + 2 * VS, sizeof(float) * VS);
-  up(geo, g32.data(), sizeof(float4) * nface);
   ok &= cudaMemset(st, 0, sizeof(int)) == cudaSuccess;
-  ok &= cudaMemset(d.cres, 0, sizeof(double) * 8L * ncell) == cudaSuccess;
+  ok &= cudaMemset(d.bres, 0, sizeof(double) * 8L * std::max(1, (int)steps.size())) == cudaSuccess;
   if (!ok) return bail(usfail(KB_ERR_CUDA, "kb_us_create: copy failed"));
   if ((rc = us_set_cells_per_cta(U, 0)) != KB_OK) return bail(rc);
-  d.face_cells = fc;
-  d.cell_faces = cf;
   d.cell_nb = nbp;
   d.cell_type = ct;
-  d.step_list = sl;
+  d.step_rec = srec;
+  d.step_geo32 = sg32;
+  d.step_geo64 = sg64;
   d.avg_list = al;
   d.status = st;
-  d.face_n = fn;
-  d.face_len = fl;
-  d.face_geo = geo;
   d.cell_area = ca;
   d.cell_mindx = cm;
   d.u = du;
@@ -853,6 +993,7 @@ static void us_enqueue_step(kb_us* U, double dt) {
   R* bout = (R*)U->b[U->cur ^ 1];
   if (d.nstep) {
     const int grid = (d.nstep + U->cb - 1) / U->cb;
+    U->nblk = grid;
     if (d.coll == KB_COLL_SHAKHOV)
       kb::k_us_step<R, true><<<grid, kb::US_T, U->smem, U->stream>>>(d, dt, U->cb, hin, bin, hout, bout);
     else
@@ -877,7 +1018,7 @@ extern "C" int kb_us_step(kb_us_t* U, double dt, int32_t nsteps, double* residua
     else
       us_enqueue_step<float>(U, dt);
   }
-  kb::k_us_residual<<<1, kb::US_T, 0, U->stream>>>(d);
+  kb::k_us_residual<<<1, 256, 0, U->stream>>>(d, U->nblk);
   U->launches++;
   if (cudaStreamSynchronize(U->stream) != cudaSuccess)
     return usfail(KB_ERR_CUDA, std::string("kb_us_step: ") + cudaGetErrorString(cudaGetLastError()));
