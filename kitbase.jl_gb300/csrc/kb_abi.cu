@@ -302,6 +302,11 @@ int kb_create(const kb_config_t* cfg, const double* u, const double* v, const do
   ALLOC(h->s.fc, kb::FaceCoef32, h->nface);
   ALLOC(h->s.cc, kb::CellCoef32, h->ncell);
   ALLOC(h->s.blockres, double, (size_t)h->s.res_blocks * 16);
+  h->s.mpart = nullptr;
+  if (c.precision == KB_PREC_FP32 && g.D == 2) {
+    const size_t nbox = (size_t)(g.nvel + kb::KB_TMA_VBOX - 1) / kb::KB_TMA_VBOX;
+    ALLOC(h->s.mpart, float2, 2 * nbox * h->nface * 4);  // two warps per face and box
+  }
   ALLOC(h->s.residual, double, 4);
   ALLOC(h->s.status, int, 1);
   ALLOC(h->d_scalar, double, 8);
@@ -754,7 +759,7 @@ int kb_set_tuning(kb_handle_t* h, const int32_t* params, int32_t n) {
     if (k == kb::KB_TUNE_MARCH_TX) ok = p == 0 || p == 2 || p == 4;
     if (k == kb::KB_TUNE_MARCH_RY) ok = p >= 0 && p <= 4096;
     if (k == kb::KB_TUNE_MARCH_BS) ok = p == 0 || p == 64 || p == 128;
-    if (k == kb::KB_TUNE_MOM_TS) ok = p == 0 || p == 2 || p == 4;
+    if (k == kb::KB_TUNE_MOM_TS) ok = p == 0 || p == 2 || p == 4 || p == 8;
     if (!ok) return fail(KB_ERR_ARG, "kb_set_tuning: value out of range for parameter " + std::to_string(k));
   }
   for (int k = 0; k < n; ++k) h->s.tune[k] = params[k];

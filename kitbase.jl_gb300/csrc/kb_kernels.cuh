@@ -49,6 +49,8 @@ struct DevState {
   FaceCoef32* fc;   // [nface] FP32 coefficient blocks
   CellCoef32* cc;   // [ncell] FP32 cell coefficients
   double* blockres; // [nblocks][16] residual partials
+  float2* mpart;    // [velocity boxes][2][nface][4] pass-A partials of the row-ring form
+                    // (double-float hi, lo); null where that form is not offered
   double* residual; // [4]
   int* status;      // [1]
   // host pointer to the TMA descriptors (CUtensorMap) of the FP32 form (the
@@ -77,6 +79,9 @@ int launch_finish(DevState& s, cudaStream_t st);
 
 // Pass A (face moments, heat flux) and pass B (pointwise update), kb_march.cu.
 int launch_moments(DevState& s, cudaStream_t st);
+// Pass A of the 2D FP32 BGK step in one launch over row rings plus the
+// partial sum (kb_mom4.cu); returns the number of launches.
+int moments_ring(DevState& s, cudaStream_t st);
 int launch_march(DevState& s, double dt, cudaStream_t st);
 
 // Materialise face fluxes fh / fb (double) of the current state, and slopes.

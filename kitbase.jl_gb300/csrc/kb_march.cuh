@@ -1983,6 +1983,9 @@ static int mom_go(DevState& s, cudaStream_t st) {
 
 template <typename R, int D, int FLUX>
 static int mom_t(DevState& s, cudaStream_t st) {
+  // 8: both face directions in one launch over row rings (2D FP32, BGK)
+  if (sizeof(R) == 4 && D == 2 && s.tune[KB_TUNE_MOM_TS] == 8 && s.coll == COLL_BGK && s.mpart)
+    return moments_ring(s, st);
   if (s.tune[KB_TUNE_MOM_TS] == 2) return mom_go<R, D, FLUX, 2>(s, st);
   return mom_go<R, D, FLUX, TS_MOM>(s, st);
 }

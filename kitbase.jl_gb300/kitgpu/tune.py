@@ -22,7 +22,7 @@ CACHE = os.environ.get("KITGPU_TUNE_CACHE",
 MARCH_TX = (2, 4)
 MARCH_BS = (64, 128)
 MARCH_RY = (16, 32, 64)
-MOM_TS = (2, 4)
+MOM_TS = (2, 4, 8)  # faces per warp of the line form; 8: the row-ring form (2D FP32 BGK)
 
 
 def signature(handle):

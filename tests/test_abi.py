@@ -164,4 +164,5 @@ def test_unsupported_paths_raise():
 
 def test_tune_signature_and_options():
     from kitgpu import tune
-    assert set(tune.MARCH_TX) <= {2, 4} and set(tune.MOM_TS) <= {2, 4}
+    # the values kb_set_tuning accepts (8: the row-ring pass A)
+    assert set(tune.MARCH_TX) <= {2, 4} and set(tune.MOM_TS) <= {2, 4, 8}

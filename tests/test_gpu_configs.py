@@ -158,12 +158,14 @@ def test_cavity_full_fp32_split(gpu_lib, cavity_oracle):
     assert max(e) < TOL32 and eq < TOLQ32, (e, eq)
 
 
-def test_quadrant_128_fp32_split(gpu_lib):
+@pytest.mark.parametrize("mom_ts", [2, 8], ids=["pass-a-lines", "pass-a-ring"])
+def test_quadrant_128_fp32_split(gpu_lib, mom_ts):
     """Four-quadrant physics of the headline workload at 128^2 cells, FP32
-    split with the tuned launch shapes of the headline (4-column strips, two
-    velocities per thread, 64 rows, 2 faces per warp) against the oracle."""
+    split with the launch shapes of the headline (4-column strips, two
+    velocities per thread, 64 rows; pass A along lines with 2 faces per warp,
+    or over row rings) against the oracle."""
     KS, ctr, *faces, t = kitgpu.initialize(C3S, precision="fp32")
-    ctr.handle.set_tuning(4, 64, 64, 2)
+    ctr.handle.set_tuning(4, 64, 64, mom_ts)
     u, v, wt = O.vspace2d(-6.0, 6.0, 64, -6.0, 6.0, 64, "newton")
     assert np.array_equal(u, KS.vs.flat(KS.vs.u)) and np.array_equal(wt, KS.vs.flat(KS.vs.weights))
     c = kitgpu.kb_config(KS)

@@ -32,7 +32,7 @@ NX = NY = 512
 NV = 64
 
 
-SHAPES = [(4, 64, 64, 2), (0, 0, 0, 0)]  # march_tx, march_ry, march_bs, mom_ts
+SHAPES = [(4, 64, 64, 2), (0, 0, 0, 0), (4, 64, 64, 8)]  # march_tx, march_ry, march_bs, mom_ts
 
 
 def headline_cfg(vmesh="newton"):
@@ -59,7 +59,7 @@ def cells_w(prim, gamma):
     return np.stack([rho, rho * U, rho * V, E], axis=1)
 
 
-@pytest.mark.parametrize("shape", SHAPES, ids=["tuned", "default"])
+@pytest.mark.parametrize("shape", SHAPES, ids=["tuned", "default", "ring-pass-a"])
 def test_headline_size_uniform_equilibrium_is_a_fixed_point(gpu_lib, shape):
     KS, h = headline_handle(shape)
     try:
@@ -77,7 +77,7 @@ def test_headline_size_uniform_equilibrium_is_a_fixed_point(gpu_lib, shape):
         h.close()
 
 
-@pytest.mark.parametrize("shape", SHAPES, ids=["tuned", "default"])
+@pytest.mark.parametrize("shape", SHAPES, ids=["tuned", "default", "ring-pass-a"])
 def test_headline_size_mirror_symmetry(gpu_lib, shape):
     KS, h = headline_handle(shape, vmesh="rectangle")
     try:

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import kitgpu
+from kitgpu import _native as N
 from cases import cavity, oracle_for, quadrant, rel, rho_u_t_error, shock, sod
 
 pytestmark = pytest.mark.gpu
@@ -171,3 +172,51 @@ def test_init_equilibrium_matches_host_state(gpu_lib, name, cfg, prec):
     for k in ("w", "prim", "h", "b"):
         scale = np.max(np.abs(ref[k]))
         assert np.max(np.abs(got[k] - ref[k])) <= tol * scale + (6e-8 * np.abs(ref[k]).max() if prec == "fp32" else 0.0), k
+
+
+MOM_CASES = [
+    ("quadrant-ugks-bgk-extra", quadrant(nx=18, ny=17, nu=15, nv=12)),
+    ("quadrant-kcu-bgk-extra", quadrant(nx=13, ny=22, nu=12, nv=16, flux="kcu")),
+    ("cavity-kfvs-bgk-walls", cavity(nx=13, ny=11, nu=14, nv=16, flux="kfvs", coll="bgk")),
+    ("cavity-ugks-bgk-walls", cavity(nx=21, ny=19, nu=16, nv=14, flux="ugks", coll="bgk")),
+]
+
+
+def _fw_after_evolve(cfg, mom_ts):
+    KS, ctr, *faces, t = kitgpu.initialize(cfg, precision="fp32")
+    h = ctr.handle
+    h.set_tuning(march_ry=8, mom_ts=mom_ts)
+    dt = kitgpu.timestep(KS, ctr, 0.0)
+    kitgpu.step(KS, ctr, dt, 3)  # a state with gradients everywhere
+    h.reconstruct()
+    h.evolve(dt)
+    fw = np.zeros((h.nface, h.nw))
+    h.call("kb_download_faces", float(dt), N.ptr(fw), None, None)
+    return KS, ctr, dt, fw
+
+
+@pytest.mark.parametrize("name,cfg", MOM_CASES, ids=[c[0] for c in MOM_CASES])
+def test_fp32_moment_pass_forms_agree(gpu_lib, name, cfg):
+    """The one-launch row-ring form of pass A (mom_ts 8: both face directions
+    from one read of h, b, partial sums per velocity box) gives the face
+    moments fw of the two-launch form (x lines, then y lines) to FP32
+    summation order: within 2e-6 of each moment's largest magnitude, on
+    partial strips, odd velocity counts and Maxwell walls."""
+    _, _, _, fa = _fw_after_evolve(cfg, 4)
+    _, _, _, fb = _fw_after_evolve(cfg, 8)
+    scale = np.max(np.abs(fa), axis=0)
+    assert np.all(np.max(np.abs(fb - fa), axis=0) <= 2e-6 * scale), (np.max(np.abs(fb - fa), axis=0), scale)
+
+
+@pytest.mark.parametrize("name,cfg", MOM_CASES, ids=[c[0] for c in MOM_CASES])
+def test_fp32_ring_moment_pass_against_oracle(gpu_lib, name, cfg):
+    """30 FP32 steps with the row-ring pass A stay within 1e-5 of the FP64
+    oracle in rho, U, T."""
+    KS, ctr, *faces, t = kitgpu.initialize(cfg, precision="fp32")
+    ctr.handle.set_tuning(march_ry=8, mom_ts=8)
+    orc = oracle_for(KS)
+    dt = kitgpu.timestep(KS, ctr, 0.0)
+    kitgpu.step(KS, ctr, dt, 30)
+    orc.step(dt, 30)
+    e = rho_u_t_error(ctr.handle.download()["prim"], orc.get_state()[1])
+    assert max(e) < 1e-5, e
