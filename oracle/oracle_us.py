@@ -1,7 +1,10 @@
 """TEST INFRASTRUCTURE ONLY: FP64 CPU restatement of KitBase.jl's
 unstructured 2D2F2V DVM step (numpy, vectorised over the velocity grid; loops
 over faces and cells), the checker of kitgpu's kb_us_* solver.  Only tests/
-use it; the product never imports it.
+and bench.py's CPU baseline use it; the product never imports it.  use_c()
+moves the step to the multithreaded C restatement (kb_oracle_us.c) on the
+same mesh tables; the numpy and C forms are held to each other by
+tests/test_unstruct_mesh.py.
 
 PARITY UNPINNED: the reference cannot run here and its unstructured test
 (test/test_unstructure.jl) asserts nothing.  The mesh connectivity and
@@ -32,6 +35,7 @@ code above:
   step! (src/Solver/step_1f.jl:228-285; BGK, the only collision it can run);
 - update_boundary! US1F (src/Solver/update_boundary.jl:546-566).
 """
+import ctypes
 import math
 
 import numpy as np
@@ -71,6 +75,7 @@ class UnstructOracle:
         self.u, self.v, self.wt = (np.asarray(a, dtype=np.float64) for a in (u, v, wt))
         self.K, self.g, self.mu, self.om, self.Pr, self.coll = K, gamma, mu_ref, omega, Pr, coll
         self.nf = nf
+        self._c = None
         if nf == 1 and coll != "bgk":
             raise ValueError("the 2D1F2V triangle step! runs BGK only")
         self.type = np.asarray(cell_type)
@@ -119,11 +124,62 @@ class UnstructOracle:
 
     def set_state(self, w, prim, h, b):
         self.w, self.prim, self.h, self.b = (np.array(a, dtype=np.float64) for a in (w, prim, h, b))
+        if self._c is not None:
+            self._c_call("kbou_set_state", *(np.ascontiguousarray(a) for a in (self.w, self.prim, self.h, self.b)))
 
     def get_state(self):
+        if self._c is not None:
+            for a in (self.w, self.prim, self.h, self.b):
+                assert a.flags.c_contiguous
+            self._c_call("kbou_get_state", self.w, self.prim, self.h, self.b)
         return self.w.copy(), self.prim.copy(), self.h.copy(), self.b.copy()
 
+    # ------------------------------------------------ C backend (kb_oracle_us.c)
+
+    def use_c(self):
+        """Step through the multithreaded C restatement (kb_oracle_us.c) on
+        this oracle's own mesh tables; returns self."""
+        import oracle as O
+        L = ctypes.CDLL(O.build())
+        D, I = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int32)
+        L.kbou_create.restype = ctypes.c_void_p
+        L.kbou_create.argtypes = [ctypes.c_int, ctypes.c_int] + [I] * 4 + [D] * 5 + [ctypes.c_int] + [D] * 3 + \
+            [ctypes.c_double] * 5 + [ctypes.c_int] * 2
+        L.kbou_timestep.restype = ctypes.c_double
+        L.kbou_timestep.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 5
+        for name in ("kbou_set_state", "kbou_get_state"):
+            getattr(L, name).argtypes = [ctypes.c_void_p] + [D] * 4
+        L.kbou_step.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, D]
+        L.kbou_destroy.argtypes = [ctypes.c_void_p]
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        nf = len(self.faces)
+        self._keep = [
+            i32([[c1, c2] for c1, c2, n, ln in self.faces]), i32(self.cell_face), i32(self.nb),
+            i32(self.type), f64([n for c1, c2, n, ln in self.faces]), f64([ln for c1, c2, n, ln in self.faces]),
+            f64(self.dirc), f64(self.area), f64(self.dx.min(axis=1)), f64(self.u), f64(self.v), f64(self.wt)]
+        k = self._keep
+        ptr = lambda a: a.ctypes.data_as(I if a.dtype == np.int32 else D)
+        self._L = L
+        self._c = L.kbou_create(self.ncell, nf, *[ptr(a) for a in k[:9]], len(self.u),
+                                *[ptr(a) for a in k[9:]], self.K, self.g, self.mu, self.om, self.Pr,
+                                1 if self.coll == "shakhov" else 0, self.nf)
+        if hasattr(self, "w"):
+            self.set_state(self.w, self.prim, self.h, self.b)
+        return self
+
+    def _c_call(self, name, *arrays):
+        D = ctypes.POINTER(ctypes.c_double)
+        getattr(self._L, name)(self._c, *[a.ctypes.data_as(D) for a in arrays])
+
+    def __del__(self):
+        if getattr(self, "_c", None):
+            self._L.kbou_destroy(self._c)
+            self._c = None
+
     def timestep(self, cfl, t, tmax_time, umax, vmax):
+        if self._c is not None:
+            return self._L.kbou_timestep(self._c, cfl, t, tmax_time, umax, vmax)
         tmax = 0.0
         for c in range(self.ncell):
             sos = (0.5 * self.g / self.prim[c, 3]) ** 0.5
@@ -252,6 +308,10 @@ class UnstructOracle:
         return res
 
     def step(self, dt, n=1):
+        if self._c is not None:
+            r = np.zeros(4)
+            self._L.kbou_step(self._c, dt, n, r.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+            return r
         res = None
         for _ in range(n):
             self.evolve(dt)

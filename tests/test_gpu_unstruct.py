@@ -118,3 +118,20 @@ def test_unstructured_conservation(gpu_lib):
     scale = np.sum(np.abs(w0[inner]) * area[inner, None], axis=0)
     assert np.all(np.abs(change + leak) <= 1e-13 * scale), (change, leak)
     assert np.all(np.abs(leak) > 1e-10 * scale)  # flux does cross to the fixed ring
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 1e-5)])
+def test_unstructured_long_run_against_c_oracle(gpu_lib, prec, tol):
+    """A 48 x 48-quad mesh (4608 triangles, extrapolated boundaries, Shakhov)
+    over 200 steps against the multithreaded C oracle: rho, U, T within
+    1e-12 (FP64) and 1e-5 (FP32 split)."""
+    c = dict(boundary="extra", collision="shakhov", nx=48, ny=48, jitter=0.2)
+    KS, orc = _setup(c)
+    orc.use_c()
+    hd = US.init_fvm(KS, prec)
+    dt = hd.timestep()
+    assert dt == pytest.approx(orc.timestep(KS.set.cfl, 0.0, KS.set.maxTime, KS.vs.u1, KS.vs.v1), rel=1e-14)
+    hd.step(dt, 200)
+    orc.step(dt, 200)
+    e = rho_u_t_error(hd.download()["prim"], orc.get_state()[1])
+    assert max(e) < tol, e
