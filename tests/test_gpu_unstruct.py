@@ -36,6 +36,8 @@ CASES = [
                               space="2d1f2v")),
     ("1f-extra-bgk-inK0", dict(boundary="extra", collision="bgk", nx=10, ny=9, jitter=0.2,
                                space="2d1f2v", inK=0.0)),
+    # 18 x 18 velocities: past the staged FP32 form's 256, the direct-load form
+    ("fix-shakhov-v18", dict(boundary="fix", collision="shakhov", nx=8, ny=7, jitter=0.2, nu=18)),
 ]
 
 
