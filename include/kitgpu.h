@@ -232,7 +232,9 @@ int kb_get_timing(kb_handle_t* h, double* ms, int64_t* count);
  * per CTA of the update pass (1..4096), params[2] update-pass form (64: two
  * velocities per thread in packed FP32 pairs -- the 2D FP32 form -- or 64
  * threads per CTA elsewhere; 128: one velocity per thread, 128 threads),
- * params[3] faces per warp of the moment pass (2, 4).  0 keeps the default.
+ * params[3] faces per warp of the moment pass (2, 4) along x and y lines,
+ * or 8: both face directions in one launch over the update pass's row rings
+ * (2D FP32 BGK; other solves keep the line form).  0 keeps the default.
  * No reference counterpart. */
 #define KB_NTUNE 4
 int kb_set_tuning(kb_handle_t* h, const int32_t* params, int32_t n);

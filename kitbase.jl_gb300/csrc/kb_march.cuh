@@ -21,6 +21,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <type_traits>
 
 #include "kb_kernels.cuh"
@@ -1944,16 +1945,15 @@ static void mom_st_go(DevState& s, cudaStream_t st) {
   auto kern = k_mom_st<D, FLUX, TS, SHAK, DIR>;
   const CUtensorMap* tm =
       (const CUtensorMap*)s.tmaps + 8 + ((DIR * 2 + (TS == 4 ? 1 : 0)) * 2 + s.cur) * 2;
-  static bool raised[64] = {false};
+  static std::once_flag once[64];  // per device; thread-safe for concurrent host threads
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && !raised[dev]) {
+  std::call_once(once[dev & 63], [&] {
     if (SL::BYTES > 48 * 1024)
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SL::BYTES);
     cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
-    raised[dev] = true;
-  }
+  });
   kern<<<(unsigned)nblk, MOM_THREADS, SL::BYTES, st>>>(tm[0], tm[1], s);
 }
 
@@ -2012,17 +2012,16 @@ static void march3_go(DevState& s, cudaStream_t st) {
   void (*kern)(CUtensorMap, CUtensorMap, DevState, int);
   if constexpr (PAIR) kern = k_march4<FLUX, TX, NS, G>;
   else kern = k_march3<FLUX, TX, NS>;
-  static bool raised[64] = {false};
+  static std::once_flag once[64];  // per device; thread-safe for concurrent host threads
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && !raised[dev]) {
+  std::call_once(once[dev & 63], [&] {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
     // all of the unified L1 / shared storage as shared memory: the ring is the
     // kernel's only reuse, so residency counts for more than L1 cache
     cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
-    raised[dev] = true;
-  }
+  });
   dim3 grid((g.nvel + M3_BS - 1) / M3_BS, (g.nx + TX - 1) / TX, (g.ny + ry - 1) / ry);
   kern<<<grid, PAIR ? M4_THREADS * G : M3_BS, L::BYTES, st>>>(tm[0], tm[1], s, ry);
 }
