@@ -137,3 +137,32 @@ def test_unstructured_long_run_against_c_oracle(gpu_lib, prec, tol):
     orc.step(dt, 200)
     e = rho_u_t_error(hd.download()["prim"], orc.get_state()[1])
     assert max(e) < tol, e
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_unstructured_shape_independent_and_tuned(gpu_lib, prec):
+    """The cells-per-CTA shape changes only how cells are grouped: the state
+    after 5 steps is bit-identical for 4 and 32 cells per CTA; out-of-range
+    shapes are refused; the autotuner keeps one of its candidates."""
+    from kitgpu import _native as N
+    from kitgpu import tune
+    c = dict(boundary="extra", collision="shakhov", nx=11, ny=9, jitter=0.2)
+    KS, orc = _setup(c)
+    out = []
+    for cb in (4, 32):
+        hd = US.init_fvm(KS, prec)
+        hd.set_tuning(cb)
+        assert hd.tuning() == cb
+        dt = hd.timestep()
+        hd.step(dt, 5)
+        out.append(hd.download())
+        hd.close()
+    for k in ("w", "prim", "h", "b"):
+        assert np.array_equal(out[0][k], out[1][k]), k
+    hd = US.init_fvm(KS, prec)
+    for bad in (-1, 33):
+        with pytest.raises(N.KitGPUError):
+            hd.set_tuning(bad)
+    dt = hd.timestep()
+    best, times = tune.autotune_unstruct(hd, dt, steps=2, use_cache=False)
+    assert best in tune.US_CELLS_PER_CTA and hd.tuning() == best and len(times) >= 1

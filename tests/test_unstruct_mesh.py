@@ -171,3 +171,35 @@ def test_c_oracle_matches_numpy_oracle(bc, coll, space):
     assert np.max(np.abs(h1 - h0)) <= 1e-13 * np.max(np.abs(h0))
     assert np.max(np.abs(b1 - b0)) <= 1e-13 * max(np.max(np.abs(b0)), 1e-300)
     assert np.allclose(rs[1], rs[0], rtol=1e-9, atol=1e-300)
+
+
+def test_inconsistent_tables_refused():
+    """kb_us_create checks the tables against each other before any CUDA
+    call: a neighbour list that disagrees with face_cells, an out-of-range
+    face, a stepped cell without three neighbours."""
+    m = US.build_mesh(*US.rectangle_mesh(4, 3))
+    lib = US._lib()
+    c = N.KbConfig()
+    c.dim, c.nx, c.ny, c.nu, c.nv = 2, m.ncell, 1, 4, 4
+    c.flux, c.collision, c.interp_order, c.precision = 0, 0, 1, 0
+    c.K, c.gamma, c.mu_ref, c.omega, c.Pr, c.nf = 1.0, 5 / 3, 1e-3, 0.72, 1.0, 2
+    vel = [np.zeros(16), np.zeros(16), np.ones(16)]
+    P = ctypes.POINTER(ctypes.c_int32)
+
+    def create(keep):
+        h = ctypes.c_void_p()
+        return lib.kb_us_create(ctypes.byref(c), m.ncell, m.nface, *[a.ctypes.data_as(P) for a in keep[:4]],
+                                *[N.ptr(a) for a in keep[4:] + vel], ctypes.byref(h))
+
+    keep = US.mesh_arrays(m)
+    inner = int(np.nonzero(m.cell_type == 0)[0][0])
+    bad = [a.copy() for a in keep]
+    bad[2][inner, [0, 1]] = bad[2][inner, [1, 0]]  # neighbours swapped against the faces
+    assert create(bad) == -1 and b"disagree" in N.load().kb_last_error()
+    bad = [a.copy() for a in keep]
+    bad[1][inner, 0] = m.nface  # a face index past the end
+    assert create(bad) == -1 and b"out of range" in N.load().kb_last_error()
+    bad = [a.copy() for a in keep]
+    bnd = int(np.nonzero(m.cell_type == 1)[0][0])
+    bad[3][bnd] = 0  # a boundary cell marked as stepped
+    assert create(bad) == -2 and b"three neighbours" in N.load().kb_last_error()
