@@ -176,6 +176,16 @@ int kb_update(kb_handle_t* h, double dt, double* residual);
  * Replaces the body of the solve! loop (src/Solver/solver_main.jl:32-72). */
 int kb_step(kb_handle_t* h, double dt, int32_t nsteps, double* residual);
 
+/* nsteps steps, each with its own dt: before every step the CFL rate of the
+ * current state is reduced on the device (as kb_timestep: timestep,
+ * src/Solver/solver_main.jl:240-342) and dt = cfl / rate, clipped to
+ * max_time - t; stops early once t reaches max_time.  time_out receives the
+ * simulated time reached, residual (may be NULL) the last step's residual.
+ * The per-step dt option of the time loop; solve! itself keeps the dt of the
+ * initial state (src/Solver/solver_main.jl:12-76). */
+int kb_step_cfl(kb_handle_t* h, double cfl, double sim_time, double max_time, int32_t nsteps,
+                double* time_out, double* residual);
+
 /* Asynchronous form of kb_step for serving many solves at once: enqueue
  * nsteps steps on the handle's stream and return immediately; the residual of
  * the last step is copied to pinned host memory behind the steps.  kb_query

@@ -633,6 +633,27 @@ int kb_step(kb_handle_t* h, double dt, int32_t nsteps, double* residual) {
   return read_residual(h, residual);
 }
 
+int kb_step_cfl(kb_handle_t* h, double cfl, double sim_time, double max_time, int32_t nsteps,
+                double* time_out, double* residual) {
+  if (!h || !time_out) return fail(KB_ERR_ARG, "kb_step_cfl: null argument");
+  if (!(cfl > 0.0) || nsteps < 0) return fail(KB_ERR_ARG, "kb_step_cfl: cfl must be positive, nsteps >= 0");
+  double t = sim_time;
+  double r[4] = {0.0, 0.0, 0.0, 0.0};
+  // stop at max_time (within rounding of the accumulated time)
+  const double t_eps = 1e-14 * fabs(max_time);
+  for (int s = 0; s < nsteps && t < max_time - t_eps; ++s) {
+    double dt = 0.0;
+    KB_TRY(kb_timestep(h, cfl, t, max_time, &dt));  // device CFL reduction of the current state
+    if (!(dt > 0.0)) break;
+    KB_TRY(kb_step(h, dt, 1, r));
+    t += dt;
+  }
+  *time_out = t;
+  if (residual)
+    for (int k = 0; k < h->s.g.NW; ++k) residual[k] = r[k];
+  return KB_OK;
+}
+
 // Forget the recorded step graphs of kb_step_async.
 static void drop_graphs(kb_handle* h) {
   for (int k = 0; k < 2; ++k)

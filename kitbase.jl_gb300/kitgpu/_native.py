@@ -67,6 +67,7 @@ SIGNATURES = {
     "kb_evolve": [_H, ctypes.c_double],
     "kb_update": [_H, ctypes.c_double, _D],
     "kb_step": [_H, ctypes.c_double, ctypes.c_int32, _D],
+    "kb_step_cfl": [_H, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int32, _D, _D],
     "kb_download_faces": [_H, ctypes.c_double, _D, _D, _D],
     "kb_download_slopes": [_H, _D, _D, _D],
     "kb_upload_slopes": [_H, _D],

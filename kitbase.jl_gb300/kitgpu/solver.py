@@ -134,6 +134,14 @@ class Handle:
         self.call("kb_update", float(dt), N.ptr(r))
         return r[: self.nw]
 
+    def step_cfl(self, cfl, t, max_time, n=1):
+        """n steps, each with dt recomputed from the current state on the
+        device (kb_step_cfl); returns (time reached, last residual)."""
+        r = np.zeros(4)
+        to = ctypes.c_double()
+        self.call("kb_step_cfl", float(cfl), float(t), float(max_time), int(n), ctypes.byref(to), N.ptr(r))
+        return to.value, r[: self.nw]
+
     def step(self, dt, n=1):
         r = np.zeros(4)
         self.call("kb_step", float(dt), int(n), N.ptr(r))
@@ -402,12 +410,21 @@ def step(KS, ctr, dt, nsteps=1):
     return ctr.handle.step(dt, nsteps)
 
 
-def solve(KS, ctr, *faces, simTime=0.0, steady=False, chunk=64):
+def solve(KS, ctr, *faces, simTime=0.0, steady=False, chunk=64, adaptive=False):
     """solve! (src/Solver/solver_main.jl:12-150): fixed dt from the initial
     state, nt = floor(maxTime/dt) + 1 iterations, stop when t > maxTime or,
     if steady, when max(res) < 5e-7 (checked every `chunk` steps; chunk=1
-    reproduces the per-step test)."""
+    reproduces the per-step test).  adaptive=True is the per-step dt option:
+    before every step dt is recomputed from the current state on the device
+    (kb_step_cfl) and the run ends at maxTime."""
     t = float(simTime)
+    if adaptive:
+        res = np.zeros(KS.dim + 2)
+        while t < KS.set.maxTime * (1.0 - 1e-14):
+            t, res = ctr.handle.step_cfl(KS.set.cfl, t, KS.set.maxTime, chunk)
+            if steady and np.max(res) < 5.0e-7:
+                break
+        return t
     dt = timestep(KS, ctr, t)
     nt = int(math.floor(KS.set.maxTime / dt)) + 1
     it = 0

@@ -220,3 +220,29 @@ def test_fp32_ring_moment_pass_against_oracle(gpu_lib, name, cfg):
     orc.step(dt, 30)
     e = rho_u_t_error(ctr.handle.download()["prim"], orc.get_state()[1])
     assert max(e) < 1e-5, e
+
+
+@pytest.mark.parametrize("name,cfg", [("sod-kfvs-shakhov", sod(nx=60, flux="kfvs", coll="shakhov")),
+                                      ("quadrant-ugks-bgk", quadrant(nx=12, ny=11, nu=12, nv=10))],
+                         ids=lambda x: x if isinstance(x, str) else "")
+def test_per_step_dt_option(gpu_lib, name, cfg):
+    """kb_step_cfl (solve(..., adaptive=True)): dt recomputed from the current
+    state on the device before every step; the oracle doing the same loop
+    (timestep, then one step) matches to 1e-12 in rho, U, T and in the time
+    reached; the run stops at maxTime."""
+    KS, ctr, *faces, t = kitgpu.initialize(cfg, precision="fp64")
+    orc = oracle_for(KS)
+    n = 15
+    tg, rg = ctr.handle.step_cfl(KS.set.cfl, 0.0, KS.set.maxTime, n)
+    to = 0.0
+    for _ in range(n):
+        dt = orc.timestep(KS.set.cfl, to, KS.set.maxTime)
+        orc.step(dt, 1)
+        to += dt
+    assert tg == pytest.approx(to, rel=1e-13)
+    e = rho_u_t_error(ctr.handle.download()["prim"], orc.get_state()[1])
+    assert max(e) < 1e-12, e
+    # a short maxTime ends the loop there
+    KS2, ctr2, *faces2, t2 = kitgpu.initialize(dict(cfg, maxTime=3.5 * tg / n), precision="fp64")
+    t_end = kitgpu.solve(KS2, ctr2, adaptive=True, chunk=4)
+    assert t_end == pytest.approx(KS2.set.maxTime, rel=1e-12)
