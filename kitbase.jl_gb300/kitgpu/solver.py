@@ -16,7 +16,7 @@ from collections import namedtuple
 import numpy as np
 
 from . import _native as N
-from .setup import conserve_prim, solver_set
+from .setup import conserve_prim, read_dict, solver_set
 
 ControlVolume = namedtuple("ControlVolume", "w prim h b")
 
@@ -356,7 +356,9 @@ def initialize(config, precision=None, **ib_kw):
     write_checkpoint (a path ending in ".npz"): like the reference's
     initialize("*.jld2") (src/Solver/solver_init.jl:19-26) the solver set and
     cells come from the file and the time is the checkpoint's.  `precision`
-    ("fp64" or "fp32") defaults to "fp64", or to the checkpoint's own."""
+    ("fp64" or "fp32") defaults to "fp64", or to the checkpoint's own.  A
+    config with a `mesh` key (a gmsh file) gives the unstructured solve:
+    (KS, cells, t) from kitgpu.unstruct.initialize."""
     if isinstance(config, str) and config.endswith(".npz"):
         d = np.load(config, allow_pickle=False)
         meta = json.loads(str(d["set"]))
@@ -364,6 +366,10 @@ def initialize(config, precision=None, **ib_kw):
         out = init_fvm(KS, precision or meta.get("precision", "fp64"))
         t = read_checkpoint(d, out[0])
         return (KS,) + out + (t,)
+    if (isinstance(config, str) and "mesh" in read_dict(config)) or (isinstance(config, dict) and "mesh" in config):
+        # a gmsh mesh: the unstructured solve (UnstructPSpace, set_geometry)
+        from . import unstruct
+        return unstruct.initialize(config, precision or "fp64", **ib_kw)
     KS = solver_set(config, **ib_kw)
     return (KS,) + init_fvm(KS, precision or "fp64") + (0.0,)
 

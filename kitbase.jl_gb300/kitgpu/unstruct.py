@@ -41,6 +41,7 @@ does not have, under Shakhov.
 """
 import ctypes
 import math
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -256,17 +257,19 @@ class UnstructSolverSet:
 
 def unstruct_solver_set(mesh, nu=16, nv=16, umax=5.0, vmax=5.0, vmesh="rectangle", Kn=0.075,
                         Pr=1.0, inK=1.0, omega=0.72, collision="bgk", cfl=0.8, maxTime=1.0,
-                        prim_at=None, space="2d2f2v"):
+                        prim_at=None, space="2d2f2v", umin=None, vmin=None, case="unstructured"):
     """The reference's unstructured test setup (test/t1_2f.txt, or
     test/t1_1f.txt with space = "2d1f2v": KFVS, first order, 16 x 16
     velocities on [-5, 5]^2, Kn 0.075, Pr 1, inK 1) on `mesh`; prim_at(x, y)
-    gives the initial primitive state (default: rest, lambda 1)."""
+    gives the initial primitive state (default: rest, lambda 1); the velocity
+    box is [umin, umax] x [vmin, vmax] (umin, vmin default to -umax, -vmax)."""
     if space not in ("2d2f2v", "2d1f2v"):
         raise ValueError("unstructured spaces: 2d2f2v or 2d1f2v, not %r" % space)
-    s = Setup(matter="gas", case="unstructured", space=space, flux="kfvs",
+    s = Setup(matter="gas", case=case, space=space, flux="kfvs",
               collision=collision, interpOrder=1, limiter="vanleer", boundary=["fix"] * 4,
               cfl=cfl, maxTime=maxTime)
-    vs = VSpace2D.build(-umax, umax, nu, -vmax, vmax, nv, type=vmesh)
+    vs = VSpace2D.build(-umax if umin is None else umin, umax, nu, -vmax if vmin is None else vmin, vmax,
+                        nv, type=vmesh)
     gas = gas_property(space=space, inK=inK, knudsen=Kn, prandtl=Pr, omega=omega)
     if prim_at is None:
         def prim_at(x, y):
@@ -423,3 +426,58 @@ def init_fvm(KS, precision="fp64"):
     hd = UnstructHandle(KS, precision)
     hd.upload(*initial_cells(KS))
     return hd
+
+
+def solver_set_from_config(D, base_dir=".", prim_at=None):
+    """SolverSet of a `key = value` config whose `mesh` names a gmsh file
+    (set_geometry takes UnstructPSpace(mesh) when `mesh` is given,
+    src/Geometry/geometry.jl:15-45, src/Geometry/geo_unstruct.jl:34-39; the
+    mesh path is relative to the config's directory, as the reference's test
+    runs from its own).  Boundary cells follow `boundary`: "fix" holds them,
+    "extra" sets them to the mean of their neighbours; "maxwell" (type-2 wall
+    cells) is refused, because the reference's unstructured evolve! calls
+    flux_boundary_maxwell! with an argument list no method takes.  The
+    initial state is prim_at(x, y), by default the reference's test state:
+    the gas at rest at the config's Mach number, prim [1, Ma c, 0, 1]
+    (test/test_unstructure.jl)."""
+    bc = D.get("boundary", "fix")
+    bc = bc[0] if isinstance(bc, (list, tuple)) else bc
+    if bc == "maxwell":
+        raise ValueError("unstructured Maxwell wall cells are not offered: the reference's US2F evolve! "
+                         "calls flux_boundary_maxwell! with an argument list no method takes")
+    if bc not in ("fix", "extra"):
+        raise ValueError("unstructured boundaries: fix or extra, not %r" % bc)
+    if str(D.get("flux", "kfvs")) != "kfvs" or int(D.get("interpOrder", 1)) != 1:
+        raise ValueError("unstructured solves are first-order KFVS (flux = kfvs, interpOrder = 1)")
+    path = D["mesh"] if os.path.isabs(D["mesh"]) else os.path.join(base_dir, D["mesh"])
+    m = build_mesh(*read_gmsh(path), boundary=bc)
+    space = D.get("space", "2d2f2v")
+    gamma = gas_property(space=space, inK=float(D.get("inK", 1.0)), knudsen=float(D["knudsen"])).gamma
+    if prim_at is None:
+        c = (0.5 * gamma / 1.0) ** 0.5  # sound_speed(lambda = 1, gamma)
+        p0 = np.array([1.0, c * float(D.get("mach", 0.0)), 0.0, 1.0])
+
+        def prim_at(x, y):
+            return p0
+
+    return unstruct_solver_set(
+        m, nu=int(D["nu"]), nv=int(D["nv"]), umin=float(D["umin"]), umax=float(D["umax"]),
+        vmin=float(D["vmin"]), vmax=float(D["vmax"]), vmesh=D.get("vMeshType", "rectangle"),
+        Kn=float(D["knudsen"]), Pr=float(D.get("prandtl", 1.0)), inK=float(D.get("inK", 1.0)),
+        omega=float(D.get("omega", 0.72)), collision=D.get("collision", "bgk"), cfl=float(D["cfl"]),
+        maxTime=float(D["maxTime"]), prim_at=prim_at, space=space, case=D.get("case", "unstructured"))
+
+
+def initialize(config, precision="fp64", prim_at=None):
+    """initialize(config) of an unstructured solve (src/Solver/solver_init.jl:
+    10-48 with the UnstructPSpace of set_geometry): (KS, cells, t = 0), the
+    cells an UnstructHandle in their init_fvm state.  `config` is a config
+    file path or a dict (a dict's relative mesh path is taken from the
+    current directory)."""
+    from .setup import read_cfg
+    if isinstance(config, str):
+        D, base = read_cfg(config), os.path.dirname(os.path.abspath(config))
+    else:
+        D, base = dict(config), "."
+    KS = solver_set_from_config(D, base, prim_at)
+    return KS, init_fvm(KS, precision), 0.0

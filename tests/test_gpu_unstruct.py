@@ -166,3 +166,29 @@ def test_unstructured_shape_independent_and_tuned(gpu_lib, prec):
     dt = hd.timestep()
     best, times = tune.autotune_unstruct(hd, dt, steps=2, use_cache=False)
     assert best in tune.US_CELLS_PER_CTA and hd.tuning() == best and len(times) >= 1
+
+
+@pytest.mark.parametrize("space", ["2d2f2v", "2d1f2v"])
+def test_initialize_from_config(gpu_lib, tmp_path, space):
+    """kitgpu.initialize on a config in the reference's format with
+    `mesh = <gmsh file>` (as test/test_unstructure.jl reads t1_2f.txt /
+    t1_1f.txt, here with extrapolated boundary cells) gives the device cells
+    of the unstructured solve; 10 steps match the oracle to 1e-12."""
+    import kitgpu
+    from test_unstruct_mesh import T1_CFG
+    P, T = US.rectangle_mesh(9, 7, jitter=0.2)
+    US.write_gmsh(str(tmp_path / "m.msh"), P, T)
+    cfg = tmp_path / "u.txt"
+    cfg.write_text(T1_CFG.format(space=space, bc="extra", mesh="m.msh"))
+    KS, hd, t = kitgpu.initialize(str(cfg))
+    assert t == 0.0 and KS.nf == (2 if space == "2d2f2v" else 1)
+    vs, g = KS.vs, KS.gas
+    orc = OU.UnstructOracle(P, T, KS.ps.cell_type, vs.flat(vs.u), vs.flat(vs.v), vs.flat(vs.weights),
+                            g.K, g.gamma, g.mu_ref, g.omega, g.Pr, "bgk", nf=KS.nf)
+    orc.set_state(*US.initial_cells(KS))
+    dt = hd.timestep()
+    assert dt == pytest.approx(orc.timestep(KS.set.cfl, 0.0, KS.set.maxTime, vs.u1, vs.v1), rel=1e-14)
+    hd.step(dt, 10)
+    orc.step(dt, 10)
+    e = rho_u_t_error(hd.download()["prim"], orc.get_state()[1])
+    assert max(e) < 1e-12, e

@@ -203,3 +203,57 @@ def test_inconsistent_tables_refused():
     bnd = int(np.nonzero(m.cell_type == 1)[0][0])
     bad[3][bnd] = 0  # a boundary cell marked as stepped
     assert create(bad) == -2 and b"three neighbours" in N.load().kb_last_error()
+
+
+T1_CFG = """# unstructured setup in the reference's test-config format
+matter = gas
+case = cavity
+space = {space}
+flux = kfvs
+collision = bgk
+nSpecies = 1
+interpOrder = 1
+limiter = vanleer
+boundary = {bc}
+cfl = 0.8
+maxTime = 0.001
+hasForce = false
+mesh = {mesh}
+umin = -5.0
+umax = 5.0
+nu = 16
+vmin = -4.0
+vmax = 5.0
+nv = 12
+vMeshType = rectangle
+nug = 0
+nvg = 0
+knudsen = 0.075
+mach = 0.5
+prandtl = 1.0
+inK = 1.0
+omega = 0.72
+alphaRef = 1.0
+omegaRef = 0.5
+"""
+
+
+def test_solver_set_from_config(tmp_path):
+    """A config in the reference's format with `mesh = <gmsh file>` gives
+    the unstructured solver set (mesh relative to the config's directory,
+    velocity box and gas from the config, the gas at rest at the config's
+    Mach number); boundary = maxwell is refused with the reason."""
+    P, T = US.rectangle_mesh(6, 5, jitter=0.2)
+    US.write_gmsh(str(tmp_path / "m.msh"), P, T)
+    (tmp_path / "u.txt").write_text(T1_CFG.format(space="2d2f2v", bc="extra", mesh="m.msh"))
+    from kitgpu.setup import read_cfg
+    D = read_cfg(str(tmp_path / "u.txt"))
+    KS = US.solver_set_from_config(D, str(tmp_path))
+    assert KS.ps.ncell == len(T) and KS.vs.nu == 16 and KS.vs.nv == 12
+    assert KS.vs.v0 == -4.0 and KS.vs.v1 == 5.0 and KS.set.cfl == 0.8 and KS.nf == 2
+    w, p, h, b = US.initial_cells(KS)
+    assert np.allclose(p[:, 1], 0.5 * np.sqrt(0.5 * KS.gas.gamma)) and np.all(p[:, 3] == 1.0)
+    assert set(np.unique(KS.ps.cell_type)) <= {0, 1, 3}
+    (tmp_path / "w.txt").write_text(T1_CFG.format(space="2d2f2v", bc="maxwell", mesh="m.msh"))
+    with pytest.raises(ValueError, match="Maxwell"):
+        US.solver_set_from_config(read_cfg(str(tmp_path / "w.txt")), str(tmp_path))
