@@ -220,6 +220,15 @@ int kb_upload_slopes(kb_handle_t* h, const double* sw);
  * bounded device wait (coefficient staging of the update pass) gave up. */
 int kb_status(kb_handle_t* h);
 
+/* Test of the bounded device waits, no reference counterpart: one CTA waits
+ * through the same bounded mbarrier wait the staging kernels use, on a phase
+ * that nothing completes.  The wait gives up after limit_s (0 < limit_s <= 2)
+ * and the call returns KB_ERR_TIMEOUT with *status_out = 2 (the status bit
+ * the staging kernels set) and *waited_s = how long the wait took; the CUDA
+ * context stays usable.  Either pointer may be NULL.  Allocates 16 bytes of
+ * device memory for the result; runs on the default stream and synchronizes. */
+int kb_wait_probe(double limit_s, int32_t* status_out, double* waited_s);
+
 /* Device bytes held by the handle. */
 int kb_device_bytes(kb_handle_t* h, int64_t* bytes);
 

@@ -49,13 +49,18 @@ __device__ __forceinline__ bool mbar_try(unsigned long long* bar, unsigned parit
 __device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-// true once the phase with this parity completed; false after KB_WAIT_NS.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+// true once the phase with this parity completed; false after limit_ns.
+__device__ __forceinline__ bool mbar_wait_ns(unsigned long long* bar, unsigned parity,
+                                             unsigned long long limit_ns) {
   if (mbar_try(bar, parity)) return true;
   const unsigned long long t0 = gtimer();
   while (!mbar_try(bar, parity))
-    if (gtimer() - t0 > KB_WAIT_NS) return false;
+    if (gtimer() - t0 > limit_ns) return false;
   return true;
+}
+// the wait every staging kernel uses: gives up after KB_WAIT_NS
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  return mbar_wait_ns(bar, parity, KB_WAIT_NS);
 }
 // global -> shared bulk copy; dst, src 16-byte aligned, bytes a multiple of 16.
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,

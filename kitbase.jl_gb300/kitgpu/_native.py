@@ -13,6 +13,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libkitgpu.so")
 
 KB_OK = 0
+KB_ERR_ARG, KB_ERR_CONFIG, KB_ERR_CUDA, KB_ERR_NUMERIC = -1, -2, -3, -4
+KB_ERR_TIMEOUT, KB_ERR_NOMEM, KB_ERR_STATE = -5, -6, -7
 ERRORS = {
     -1: "KB_ERR_ARG", -2: "KB_ERR_CONFIG", -3: "KB_ERR_CUDA", -4: "KB_ERR_NUMERIC",
     -5: "KB_ERR_TIMEOUT", -6: "KB_ERR_NOMEM", -7: "KB_ERR_STATE",
@@ -83,6 +85,7 @@ SIGNATURES = {
                             ctypes.c_void_p],
     "kb_query": [_H, _D, ctypes.POINTER(ctypes.c_int32)],
     "kb_get_tuning": [_H, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32],
+    "kb_wait_probe": [ctypes.c_double, ctypes.POINTER(ctypes.c_int32), _D],
 }
 STAGES = ("reconstruct", "face_param", "moments", "wall", "cell_param", "update", "finish")
 
