@@ -256,7 +256,20 @@ int kb_create(const kb_config_t* cfg, const double* u, const double* v, const do
   h->s.flux = c.flux;
   h->s.coll = c.collision;
   h->s.cur = 0;
-  h->s.res_blocks = (c.nx * g.ny + 255) / 256;
+  {
+    // GB300 runs FP64 at a small fraction of its FP32 rate, and the cell
+    // parameters are FP64 work per cell: a grid with fewer than two full
+    // 256-thread blocks per multiprocessor spreads its cells one warp per
+    // block so that more FP64 pipes share them (the block count also fixes
+    // the order of the residual's partial sums)
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    h->s.sm_count = sms > 0 ? sms : 1;
+    const long cells = (long)c.nx * g.ny;
+    h->s.cell_bs = cells < 2L * h->s.sm_count * 256 ? 32 : 256;
+    h->s.res_blocks = (int)((cells + h->s.cell_bs - 1) / h->s.cell_bs);
+  }
   for (int k = 0; k < kb::TUNE_N; ++k) h->s.tune[k] = 0;
 
   int rc = KB_OK;
@@ -351,6 +364,21 @@ int kb_create(const kb_config_t* cfg, const double* u, const double* v, const do
   kb::face_kinds_host(g, kinds.data());
   if (cudaMemcpy(h->s.kind, kinds.data(), h->nface, cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(fail(KB_ERR_CUDA, "face kind upload failed"));
+  {
+    // the wall faces, one CTA each in k_wall
+    std::vector<int> walls;
+    for (int f = 0; f < h->nface; ++f)
+      if (kinds[f] == 2) walls.push_back(f);
+    h->s.nwall = (int)walls.size();
+    h->s.wall_list = nullptr;
+    if (!walls.empty()) {
+      if ((rc = dev_alloc(h, &p, sizeof(int) * walls.size())) != KB_OK) return bail(rc);
+      h->s.wall_list = (int*)p;
+      if (cudaMemcpy(h->s.wall_list, walls.data(), sizeof(int) * walls.size(), cudaMemcpyHostToDevice) !=
+          cudaSuccess)
+        return bail(fail(KB_ERR_CUDA, "wall face list upload failed"));
+    }
+  }
   // the set-up copies above are synchronous; wait for this handle's stream
   // only, so that creating a handle never waits for other solves' work
   if (cudaStreamSynchronize(h->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)

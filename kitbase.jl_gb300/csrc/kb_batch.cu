@@ -447,6 +447,10 @@ static int batch_set_shape(kb_batch* B, int seg, int threads, int persist) {
   const int smem = var->smem(B->d.sst_max, B->d.nu4_max);
   ok &= cudaFuncSetAttribute(var->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, var->smem_max) ==
         cudaSuccess;
+  // the carveout of every step kernel (kb::prefer_max_shared): a pool that
+  // shares the GPU with other solves' streams keeps their CTAs on common SMs
+  kb::prefer_max_shared(var->fn);
+  kb::prefer_max_shared((const void*)kb::k_batch_seg_res);
   int per = 0, dev = 0, sms = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -9,6 +9,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
+#include <set>
+#include <utility>
 #include <stdio.h>
 
 #include "kb_kernels.cuh"
@@ -269,15 +272,17 @@ __global__ void k_face_param(DevState s, double dt) {
 
 // flux_boundary_maxwell! 1D2F1V (src/Flux/flux_boundary.jl:39-61) and 2D2F2V
 // (:190-220) in the face-local frame; rot = +1 on the left / bottom wall and
-// -1 on the right / top wall (src/Solver/evolve_boundary.jl).  One warp per
-// wall face: pass 1 finds the wall density, pass 2 the moments of h_wall.
+// -1 on the right / top wall (src/Solver/evolve_boundary.jl).  One CTA of
+// WALL_T threads per wall face (DevState::wall_list): the velocities are
+// shared by all its warps, each warp sums its part, and thread 0 adds the
+// warps' sums in warp order (deterministic) and finishes the face.
+constexpr int WALL_T = 128;
 template <typename R, int D>
-__global__ void __launch_bounds__(256) k_wall(DevState s, double dt) {
+__global__ void __launch_bounds__(WALL_T) k_wall(DevState s, double dt) {
+  __shared__ double part[WALL_T / 32][8];
   const Geo& g = s.g;
-  int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (f >= s.nface_x + s.nface_y) return;
-  if (s.kind[f] != 2) return;
+  const int f = s.wall_list[blockIdx.x];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   FaceGeo r = face_geo(g, f);
   int pos = r.d == 0 ? r.fi : r.fj;
   int rot = pos == 0 ? 1 : -1;
@@ -305,7 +310,7 @@ __global__ void __launch_bounds__(256) k_wall(DevState s, double dt) {
   // cancels to FP64 round-off by construction (the density is chosen so that
   // no mass crosses the wall), also when h is stored in FP32.
   Acc<R> o0, o1, o2, o3, i0, i1, i2, i3;
-  for (int v = lane; v < g.nvel; v += 32) {
+  for (int v = threadIdx.x; v < g.nvel; v += WALL_T) {
     R un, ut;
     if (D == 1) { un = U[v]; ut = R(0); }
     else if (r.d == 0) { un = U[v]; ut = V[v]; }
@@ -329,38 +334,51 @@ __global__ void __launch_bounds__(256) k_wall(DevState s, double dt) {
       o3.add(t * c2 + W[v] * un * Bq[(long)c * vs + v]);
     }
   }
+  {
+    const double t0 = o0.total(), t1 = o1.total(), t2 = D == 2 ? o2.total() : 0.0, t3 = o3.total();
+    const double t4 = i0.total(), t5 = i1.total(), t6 = D == 2 ? i2.total() : 0.0, t7 = i3.total();
+    if (lane == 0) {
+      part[wid][0] = t0; part[wid][1] = t1; part[wid][2] = t2; part[wid][3] = t3;
+      part[wid][4] = t4; part[wid][5] = t5; part[wid][6] = t6; part[wid][7] = t7;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double T[8];
+  for (int k = 0; k < 8; ++k) {
+    T[k] = part[0][k];
+    for (int w = 1; w < WALL_T / 32; ++w) T[k] += part[w][k];
+  }
   const double norm = D == 1 ? sqrt(lw / PI) : (lw / PI);
-  const double SF = o0.total(), I0 = i0.total();
+  const double SF = T[0], I0 = T[4];
   const double rho = -SF / (I0 * norm);
   const double rn = rho * norm;  // wall density times the Maxwellian's normalisation
   const double cBw = g.Kb / (2.0 * lw);
   double len = D == 2 ? (r.d == 0 ? g.dy : g.dx) : 1.0;
   double sc = D == 2 ? len * dt : dt;
   const double S0 = SF + rn * I0;
-  const double S1 = o1.total() + rn * i1.total();
-  const double S2 = D == 2 ? o2.total() + rn * i2.total() : 0.0;
-  const double S3 = o3.total() + rn * (i3.total() + cBw * I0);
-  if (lane == 0) {
-    s.rhow[f] = rho;
-    FaceCoef32 wc;
-    float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    wc.G = wc.Cp = wc.Dp = wc.Cm = wc.Dm = z;
-    wc.E = maxwell_exp2(D == 1 ? rho * sqrt(lw / PI) : rho * (lw / PI), bw[1], bw[2], lw);
-    wc.T = make_float4(float(sc), 0.f, float(g.Kb / (2.0 * lw)), float(rot));
-    s.fc[f] = wc;
-    double fl[4] = {S0 * sc, S1 * sc, 0.0, 0.0};
-    if (D == 1) {
-      fl[2] = 0.5 * S3 * sc;
-    } else {
-      fl[2] = S2 * sc;
-      fl[3] = 0.5 * S3 * sc;
-    }
-    double* out = s.fw + (long)f * 4;
-    if (D == 2 && r.d == 1) {
-      out[0] = fl[0]; out[1] = -fl[2]; out[2] = fl[1]; out[3] = fl[3];
-    } else {
-      for (int k = 0; k < 4; ++k) out[k] = fl[k];
-    }
+  const double S1 = T[1] + rn * T[5];
+  const double S2 = D == 2 ? T[2] + rn * T[6] : 0.0;
+  const double S3 = T[3] + rn * (T[7] + cBw * I0);
+  s.rhow[f] = rho;
+  FaceCoef32 wc;
+  float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+  wc.G = wc.Cp = wc.Dp = wc.Cm = wc.Dm = z;
+  wc.E = maxwell_exp2(D == 1 ? rho * sqrt(lw / PI) : rho * (lw / PI), bw[1], bw[2], lw);
+  wc.T = make_float4(float(sc), 0.f, float(g.Kb / (2.0 * lw)), float(rot));
+  s.fc[f] = wc;
+  double fl[4] = {S0 * sc, S1 * sc, 0.0, 0.0};
+  if (D == 1) {
+    fl[2] = 0.5 * S3 * sc;
+  } else {
+    fl[2] = S2 * sc;
+    fl[3] = 0.5 * S3 * sc;
+  }
+  double* out = s.fw + (long)f * 4;
+  if (D == 2 && r.d == 1) {
+    out[0] = fl[0]; out[1] = -fl[2]; out[2] = fl[1]; out[3] = fl[3];
+  } else {
+    for (int k = 0; k < 4; ++k) out[k] = fl[k];
   }
 }
 
@@ -388,12 +406,12 @@ __device__ inline int update_group(const Geo& g, int i, int j) {
 // per physical cell; each block writes its residual partials in a fixed order.
 // FAST (the FP32 split form): tau, the density factors and the exponent
 // offsets of the coefficient blocks with FP32 transcendentals, conserve_prim
-// by reciprocals (see t_exp); w and prim stay FP64.
-template <int D, bool FAST>
-__global__ void __launch_bounds__(256) k_cell_param(DevState s, double dt) {
+// by reciprocals (see t_exp); w and prim stay FP64.  BS threads per block
+// (32 on small grids, 256 otherwise: DevState::cell_bs).
+template <int D, bool FAST, int BS>
+__global__ void __launch_bounds__(BS) k_cell_param(DevState s, double dt) {
   const Geo& g = s.g;
-  __shared__ double red[256][8];
-  __shared__ int isb[256];
+  __shared__ double red[BS][8];
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   double rr[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int grp = 0;
@@ -505,9 +523,8 @@ __global__ void __launch_bounds__(256) k_cell_param(DevState s, double dt) {
   for (int half = 0; half < 2; ++half) {
     bool take = grp == half + 1;
     for (int k = 0; k < 8; ++k) red[threadIdx.x][k] = take ? rr[k] : 0.0;
-    isb[threadIdx.x] = 0;
     __syncthreads();
-    for (int st = 128; st >= 1; st >>= 1) {
+    for (int st = BS / 2; st >= 1; st >>= 1) {
       if (threadIdx.x < st)
         for (int k = 0; k < 8; ++k) red[threadIdx.x][k] += red[threadIdx.x + st][k];
       __syncthreads();
@@ -818,52 +835,66 @@ __global__ void k_init_eq(DevState s, R* __restrict__ H, R* __restrict__ Bq) {
 
 static inline unsigned nblk(long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// Every kernel of a step asks for the largest shared-memory carveout, the one
+// the two HBM passes need for their rings.  An SM holds CTAs of kernels with
+// different carveouts only after it drains and reconfigures, so when many
+// solves share the GPU (a served stream: one CUDA stream per solve) a single
+// carveout for all step kernels lets their CTAs share SMs.  Set once per
+// kernel and device, on the first (uncaptured) launch.
+void prefer_max_shared(const void* fn) {
+  static std::mutex m;
+  static std::set<std::pair<const void*, int>> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(m);
+  if (done.insert(std::make_pair(fn, dev)).second)
+    cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+}
+
+// Threads per block of the one-thread-per-item FP64 kernels (w slopes, face
+// parameters): one warp per block while the items fill fewer than two
+// 128-thread blocks per multiprocessor, so a small grid spreads its FP64 work
+// over more multiprocessors' FP64 pipes instead of queueing on a few.
+static inline int item_bs(const DevState& s, long n) { return n < 2L * s.sm_count * 128 ? 32 : 128; }
+
 int launch_reconstruct(DevState& s, cudaStream_t st) {
   if (s.flux == FLUX_KFVS) return 0;  // KFVS reads no w slopes
   long n = (long)s.g.nx * s.g.ny * s.g.D;
   if (s.g.interp == 1) return 0;
-  if (s.prec != 0) k_wslope<true><<<nblk(n, 128), 128, 0, st>>>(s);
-  else k_wslope<false><<<nblk(n, 128), 128, 0, st>>>(s);
+  const int bs = item_bs(s, n);
+  void (*fn)(DevState) = s.prec != 0 ? k_wslope<true> : k_wslope<false>;
+  prefer_max_shared((const void*)fn);
+  fn<<<nblk(n, bs), bs, 0, st>>>(s);
   return 1;
+}
+
+template <int D>
+static void (*face_param_fn(int flux, bool fast))(DevState, double) {
+  switch (flux) {
+    case FLUX_KFVS: return fast ? k_face_param<D, FLUX_KFVS, true> : k_face_param<D, FLUX_KFVS, false>;
+    case FLUX_KCU: return fast ? k_face_param<D, FLUX_KCU, true> : k_face_param<D, FLUX_KCU, false>;
+    default: return fast ? k_face_param<D, FLUX_UGKS, true> : k_face_param<D, FLUX_UGKS, false>;
+  }
 }
 
 int launch_face_param(DevState& s, double dt, cudaStream_t st) {
   int nf = s.nface_x + s.nface_y;
-  const bool two = s.g.D == 2, fast = s.prec != 0;
-#define KB_FP(D, F)                                                              \
-  (fast ? k_face_param<D, F, true><<<nblk(nf, 128), 128, 0, st>>>(s, dt)        \
-        : k_face_param<D, F, false><<<nblk(nf, 128), 128, 0, st>>>(s, dt))
-  switch (s.flux) {
-    case FLUX_KFVS:
-      if (two) KB_FP(2, FLUX_KFVS);
-      else KB_FP(1, FLUX_KFVS);
-      break;
-    case FLUX_KCU:
-      if (two) KB_FP(2, FLUX_KCU);
-      else KB_FP(1, FLUX_KCU);
-      break;
-    default:
-      if (two) KB_FP(2, FLUX_UGKS);
-      else KB_FP(1, FLUX_UGKS);
-      break;
-  }
-#undef KB_FP
+  const bool fast = s.prec != 0;
+  const int bs = item_bs(s, nf);
+  void (*fn)(DevState, double) = s.g.D == 2 ? face_param_fn<2>(s.flux, fast) : face_param_fn<1>(s.flux, fast);
+  prefer_max_shared((const void*)fn);
+  fn<<<nblk(nf, bs), bs, 0, st>>>(s, dt);
   return 1;
 }
 
 int launch_wall(DevState& s, double dt, cudaStream_t st) {
-  bool wall = false;
-  for (int k = 0; k < 2 * s.g.D; ++k) wall |= s.g.bc[k] == BC_MAXWELL;
-  if (!wall) return 0;
-  int nf = s.nface_x + s.nface_y;
-  unsigned gb = nblk((long)nf * 32, 256);
-  if (s.g.D == 1) {
-    if (s.prec == 0) k_wall<double, 1><<<gb, 256, 0, st>>>(s, dt);
-    else k_wall<float, 1><<<gb, 256, 0, st>>>(s, dt);
-  } else {
-    if (s.prec == 0) k_wall<double, 2><<<gb, 256, 0, st>>>(s, dt);
-    else k_wall<float, 2><<<gb, 256, 0, st>>>(s, dt);
-  }
+  if (s.nwall == 0) return 0;
+  void (*fn)(DevState, double);
+  if (s.g.D == 1) fn = s.prec == 0 ? k_wall<double, 1> : k_wall<float, 1>;
+  else fn = s.prec == 0 ? k_wall<double, 2> : k_wall<float, 2>;
+  prefer_max_shared((const void*)fn);
+  fn<<<(unsigned)s.nwall, WALL_T, 0, st>>>(s, dt);
   return 1;
 }
 
@@ -874,15 +905,19 @@ int launch_evolve(DevState& s, double dt, cudaStream_t st) {
   return n;
 }
 
-int launch_cell_param(DevState& s, double dt, cudaStream_t st) {
+template <int BS>
+static void cell_param_bs(DevState& s, double dt, cudaStream_t st) {
   const bool fast = s.prec != 0;
-  if (s.g.D == 1) {
-    if (fast) k_cell_param<1, true><<<s.res_blocks, 256, 0, st>>>(s, dt);
-    else k_cell_param<1, false><<<s.res_blocks, 256, 0, st>>>(s, dt);
-  } else {
-    if (fast) k_cell_param<2, true><<<s.res_blocks, 256, 0, st>>>(s, dt);
-    else k_cell_param<2, false><<<s.res_blocks, 256, 0, st>>>(s, dt);
-  }
+  void (*fn)(DevState, double);
+  if (s.g.D == 1) fn = fast ? k_cell_param<1, true, BS> : k_cell_param<1, false, BS>;
+  else fn = fast ? k_cell_param<2, true, BS> : k_cell_param<2, false, BS>;
+  prefer_max_shared((const void*)fn);
+  fn<<<s.res_blocks, BS, 0, st>>>(s, dt);
+}
+
+int launch_cell_param(DevState& s, double dt, cudaStream_t st) {
+  if (s.cell_bs == 32) cell_param_bs<32>(s, dt, st);
+  else cell_param_bs<256>(s, dt, st);
   return 1;
 }
 
@@ -898,9 +933,11 @@ static int finish_t(DevState& s, cudaStream_t st) {
     DevState t = s;
     t.cur ^= 1;
     int nrow = D == 2 ? s.g.nyt : 1;
+    prefer_max_shared((const void*)k_ghost<R>);
     if (s.g.ngx > 0) { k_ghost<R><<<2 * s.g.ngx * nrow, 128, 0, st>>>(t, 0); ++n; }
     if (D == 2 && s.g.ngy > 0) { k_ghost<R><<<2 * s.g.ngy * s.g.nxt, 128, 0, st>>>(t, 1); ++n; }
   }
+  prefer_max_shared((const void*)k_residual);
   k_residual<<<1, 256, 0, st>>>(s);
   ++n;
   return n;

@@ -43,6 +43,8 @@ struct DevState {
   double* wall;     // [nface][4] wall prim, global frame (only wall faces read)
   double* rhow;     // [nface] Maxwell wall density
   signed char* kind;  // [nface] 0 none, 1 interior, 2 wall
+  int* wall_list;   // [nwall] indices of the wall faces (kind 2), in face order
+  int nwall;
   double* q;        // [ncell][2]
   CellParam* cp;    // [ncell]
   CellParamF* cpf;  // [ncell]
@@ -59,7 +61,14 @@ struct DevState {
   int nface_x, nface_y;
   int ncell;
   int res_blocks;   // number of blocks of k_cell_param
+  int cell_bs;      // threads per block of k_cell_param (32 or 256)
+  int sm_count;     // multiprocessors of the device: small grids spread their
+                    // FP64-heavy per-face / per-cell threads over more of them
 };
+
+// Ask for the largest shared-memory carveout for kernel fn on the current
+// device (once per kernel and device; see kb_kernels.cu).
+void prefer_max_shared(const void* fn);
 
 // Face classification for the current configuration (host computes, uploads).
 void face_kinds_host(const Geo& g, signed char* kind);

@@ -1968,6 +1968,9 @@ static int mom_go(DevState& s, cudaStream_t st) {
   }
   int n = 0;
   long wx = (long)((g.nx + TS - 1) / TS) * g.ny;
+  prefer_max_shared((const void*)k_mom<R, D, FLUX, TS, true, 0>);
+  prefer_max_shared((const void*)k_mom<R, D, FLUX, TS, false, 0>);
+  prefer_max_shared((const void*)k_mom<R, D, FLUX, TS, false, 1>);
   if (s.coll == COLL_SHAKHOV)
     k_mom<R, D, FLUX, TS, true, 0><<<nblk2(wx * 32, 128), 128, 0, st>>>(s);
   else
@@ -1996,6 +1999,7 @@ static void march_go(DevState& s, double dt, cudaStream_t st) {
   const int ry = s.tune[KB_TUNE_MARCH_RY] > 0 ? s.tune[KB_TUNE_MARCH_RY] : RY_MARCH;
   dim3 grid((g.nx + TX - 1) / TX, D == 2 ? (g.ny + ry - 1) / ry : 1, (g.nvel + BS - 1) / BS);
   const int smem = sizeof(R) == 4 && D == 2 ? MarchStage<TX>::BYTES : 0;
+  prefer_max_shared((const void*)k_march<R, D, FLUX, TX, BS>);
   k_march<R, D, FLUX, TX, BS><<<grid, BS, smem, st>>>(s, dt, ry);
 }
 

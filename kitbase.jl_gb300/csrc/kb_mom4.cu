@@ -413,6 +413,7 @@ int moments_ring(DevState& s, cudaStream_t st) {
     cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
   });
+  prefer_max_shared((const void*)k_mom_fin);
   const int nchunk = (g.nvel + M3_BS - 1) / M3_BS;
   dim3 grid(nchunk, (g.nx + TX - 1) / TX, (g.ny + ry - 1) / ry);
   kern<<<grid, M4_THREADS * G, L::BYTES, st>>>(tm[0], tm[1], s, ry);

@@ -92,6 +92,16 @@ def mixed_stream(rate, duration, seed=20261203, max_steps=200, tol=1e-6, frac_1d
     return out
 
 
+# Launch shapes of the served 2D solves.  Served grids are small (16^2 to
+# 128^2 cells): the shapes that suit one large solve give them few CTAs, each
+# a long serial march.  Two-column strips of 8 rows with one velocity per
+# thread in the update pass and two faces per warp in the moment pass were
+# the fastest on every served size measured (16^2 x 21^2 to 128^2 x 48^2 cells
+# x velocities: 1.3-2x the default shapes).  Fixed rather than autotuned per
+# request: a tuning search would advance the request's own solution.
+SERVE_SHAPE_2D = dict(march_tx=2, march_ry=8, march_bs=128, mom_ts=2)
+
+
 def estimate_bytes(cfg, precision):
     """Device bytes of a handle for `cfg` (distributions x2 buffers dominate)."""
     d = int(cfg["space"][0])
@@ -116,6 +126,7 @@ class Server:
     chunk: int = 20
     pool_1d: bool = True          # 1D requests share one fused launch (FP32 only)
     pool_cells: int = None        # cell capacity of the pool; None: from the HBM budget
+    shape_2d: dict = field(default_factory=lambda: dict(SERVE_SHAPE_2D))  # None: library defaults
     done: list = field(default_factory=list)
 
     def run(self, requests, time_scale=1.0, keep_results=False, on_retire=None):
@@ -184,6 +195,8 @@ class Server:
                 else:
                     h = Handle(kb_config(KS, self.precision), vs.flat(vs.u), vs.flat(vs.v),
                                vs.flat(vs.weights))
+                if KS.dim == 2 and self.precision == "fp32" and self.shape_2d:
+                    h.set_tuning(**self.shape_2d)
                 # the Sod and cavity presets start in equilibrium: only w and
                 # prim cross the bus, h and b are built on the device
                 w, p = initial_cells(KS)
