@@ -1,9 +1,12 @@
-"""Shared problem builders for the parity tests: one config dict -> the same
-initial state, walls and velocity tables for the oracle and for libkitgpu."""
+"""Shared problem builders for the parity tests: one config dict, from which
+libkitgpu (through the product's set-up) and the oracle (through its own
+restated set-up, oracle/oracle_setup.py) each build their initial state,
+walls and velocity tables."""
 import numpy as np
 
 import kitgpu
 import oracle as O
+import oracle_setup as OP
 
 
 def sod(nx=40, nu=33, flux="kfvs", coll="shakhov", bc="fix", ng=0, Kn=1e-4, maxTime=0.2,
@@ -44,21 +47,16 @@ def quadrant(nx=8, ny=8, nu=12, nv=12, flux="ugks", coll="bgk", bc="extra", ng=1
 
 
 def oracle_for(KS, threads=None):
-    """An oracle solver with the same state as a fresh init_fvm(KS)."""
-    cfg = kitgpu.kb_config(KS)
-    c = O.make_config(cfg.dim, cfg.nx, cfg.ny, cfg.ngx, cfg.ngy, cfg.nu, cfg.nv, cfg.flux,
-                      cfg.collision, [cfg.bc[k] for k in range(4)], cfg.interp_order,
-                      cfg.x0, cfg.x1, cfg.y0, cfg.y1, cfg.umax, cfg.vmax, cfg.K, cfg.gamma,
-                      cfg.mu_ref, cfg.omega, cfg.Pr, nf=cfg.nf)
-    vs = KS.vs
-    if KS.dim == 1:
-        orc = O.Oracle(c, vs.u, None, vs.weights, threads=threads)
-    else:
-        orc = O.Oracle(c, vs.flat(vs.u), vs.flat(vs.v), vs.flat(vs.weights), threads=threads)
-    w, p, h, b = kitgpu.initial_state(KS)
-    orc.set_state(w, p, h, b)
-    for side, prim in enumerate(kitgpu.wall_states(KS)):
-        if KS.set.boundary[side] == "maxwell":
+    """An oracle solver started from the configuration KS was built from, with
+    its own set-up (oracle/oracle_setup.py: velocity grid, gas constants, initial
+    cells and walls restated from the reference), not the product's: the GPU
+    starts from kitgpu's set-up, so a set-up error on either side shows up as
+    a parity failure."""
+    P = OP.problem(KS.config, KS.ib_kw)
+    orc = O.Oracle(P["cfg"], P["u"], P["v"], P["weights"], threads=threads)
+    orc.set_state(P["w"], P["prim"], P["h"], P["b"])
+    for side, prim in enumerate(P["walls"]):
+        if prim is not None and P["boundary"][side] == "maxwell":
             orc.set_wall(side, prim)
     return orc
 

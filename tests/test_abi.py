@@ -166,3 +166,59 @@ def test_tune_signature_and_options():
     from kitgpu import tune
     # the values kb_set_tuning accepts (8: the row-ring pass A)
     assert set(tune.MARCH_TX) <= {2, 4} and set(tune.MOM_TS) <= {2, 4, 8}
+
+
+@pytest.mark.parametrize("cfg", [
+    ("sod", dict()), ("sod-ghosts-rect", dict(ng=2, vmesh="rectangle", nu=31)),
+    ("sod-1f", dict(space="1d1f1v")), ("shock", dict()), ("shock-lam05", dict(lamL=0.5)),
+    ("cavity", dict()), ("cavity-19", dict(nx=19, ny=19)), ("cavity-lid", dict(lid=0.3)),
+    ("quadrant", dict()), ("quadrant-seed", dict(seed=7)), ("cavity-1f", dict(space="2d1f2v")),
+], ids=lambda c: c[0])
+def test_product_setup_matches_independent_oracle_setup(cfg):
+    """The product's set-up (kitgpu.setup: SolverSet, init_fvm, wall states)
+    and the oracle's own restatement (oracle_setup.problem) give the same
+    configuration, velocity tables, initial cells and walls from one config
+    dict, for every preset the parity tests run."""
+    import oracle_setup as OP
+    from cases import cavity, quadrant, shock, sod
+    name, kw = cfg
+    ib_kw = {}
+    if name.startswith("sod"):
+        D = sod(**{k: v for k, v in kw.items() if k != "space"})
+    elif name.startswith("shock"):
+        D = shock()
+        if "lamL" in kw:
+            ib_kw["lamL"] = kw["lamL"]
+    elif name.startswith("cavity"):
+        D = cavity(**{k: v for k, v in kw.items() if k != "space"})
+    else:
+        D = quadrant()
+        if "seed" in kw:
+            ib_kw["seed"] = kw["seed"]
+    if "space" in kw:
+        D["space"] = kw["space"]
+        if kw["space"] == "2d1f2v":
+            D["collision"] = "bgk"
+    KS = kitgpu.solver_set(D, **ib_kw)
+    P = OP.problem(KS.config, KS.ib_kw)
+    mine = kitgpu.kb_config(KS)
+    ref = P["cfg"]
+    for f in ("dim", "nx", "ny", "ngx", "ngy", "nu", "nv", "flux", "collision", "interp_order", "nf"):
+        assert getattr(mine, f) == getattr(ref, f), f
+    assert list(mine.bc) == list(ref.bc)
+    for f in ("x0", "x1", "umax", "K", "omega", "Pr"):
+        assert getattr(mine, f) == getattr(ref, f), f
+    for f in ("gamma", "mu_ref"):
+        assert getattr(mine, f) == pytest.approx(getattr(ref, f), rel=1e-15), f
+    vs = KS.vs
+    if KS.dim == 1:
+        assert np.array_equal(vs.u, P["u"]) and np.array_equal(vs.weights, P["weights"])
+    else:
+        assert np.array_equal(vs.flat(vs.u), P["u"]) and np.array_equal(vs.flat(vs.v), P["v"])
+        assert np.array_equal(vs.flat(vs.weights), P["weights"])
+    w, p, h, b = kitgpu.initial_state(KS)
+    for a, r in ((w, P["w"]), (p, P["prim"]), (h, P["h"]), (b, P["b"])):
+        assert a.shape == r.shape
+        assert np.allclose(a, r, rtol=1e-14, atol=1e-300)
+    for side, prim in enumerate(kitgpu.wall_states(KS)):
+        assert np.allclose(prim, P["walls"][side], rtol=1e-15, atol=0)

@@ -27,6 +27,7 @@ import pytest
 
 import kitgpu
 import oracle as O
+import oracle_setup as OP
 from cases import cavity, quadrant, rho_u_t_error, sod
 
 pytestmark = pytest.mark.gpu
@@ -66,20 +67,20 @@ def q_error(ga, oa, u, v, wt):
 
 def _oracle_sod(KS):
     """Oracle for the Sod config from the oracle's own setup restatement."""
-    c = kitgpu.kb_config(KS)
+    mu = OP.mu_ref_of(1e-4, 1.0, 0.5)
     u, wt = O.vspace1d(-5.0, 5.0, 101, "newton")
     cfg = O.make_config(1, 200, 1, 0, 0, 101, 1, "kfvs", "shakhov", "fix", 2, 0.0, 1.0, 0.0, 1.0,
-                        5.0, 0.0, 2.0, 5.0 / 3.0, c.mu_ref, 0.81, 2.0 / 3.0)
+                        5.0, 0.0, 2.0, 5.0 / 3.0, mu, 0.81, 2.0 / 3.0)
     orc = O.Oracle(cfg, u, None, wt)
     orc.set_state(*O.sod_state(200, 0, 0.0, 1.0, u, 5.0 / 3.0, 2.0))
     return orc, u, None, wt
 
 
 def _oracle_cavity(KS):
-    c = kitgpu.kb_config(KS)
+    mu = OP.mu_ref_of(0.075, 1.0, 0.5)
     u, v, wt = O.vspace2d(-5.0, 5.0, 28, -5.0, 5.0, 28, "newton")
     cfg = O.make_config(2, 64, 64, 0, 0, 28, 28, "kcu", "shakhov", "maxwell", 2, 0.0, 1.0, 0.0,
-                        1.0, 5.0, 5.0, 1.0, 5.0 / 3.0, c.mu_ref, 0.72, 2.0 / 3.0)
+                        1.0, 5.0, 5.0, 1.0, 5.0 / 3.0, mu, 0.72, 2.0 / 3.0)
     orc = O.Oracle(cfg, u, v, wt)
     orc.set_state(*O.cavity_state(64, 64, 0, 0, u, v, 5.0 / 3.0, 1.0))
     for side, prim in enumerate(O.cavity_walls(64, 64, 0.0, 1.0, 0.0, 1.0)):
@@ -166,13 +167,10 @@ def test_quadrant_128_fp32_split(gpu_lib, mom_ts):
     or over row rings) against the oracle."""
     KS, ctr, *faces, t = kitgpu.initialize(C3S, precision="fp32")
     ctr.handle.set_tuning(4, 64, 64, mom_ts)
-    u, v, wt = O.vspace2d(-6.0, 6.0, 64, -6.0, 6.0, 64, "newton")
-    assert np.array_equal(u, KS.vs.flat(KS.vs.u)) and np.array_equal(wt, KS.vs.flat(KS.vs.weights))
-    c = kitgpu.kb_config(KS)
-    cfg = O.make_config(2, 128, 128, 1, 1, 64, 64, "ugks", "bgk", "extra", 2, 0.0, 1.0, 0.0, 1.0,
-                        6.0, 6.0, 1.0, 5.0 / 3.0, c.mu_ref, c.omega, c.Pr)
-    orc = O.Oracle(cfg, u, v, wt)
-    orc.set_state(*kitgpu.initial_state(KS))
+    P = OP.problem(KS.config, KS.ib_kw)  # the oracle's own set-up of the same config
+    u, v, wt = P["u"], P["v"], P["weights"]
+    orc = O.Oracle(P["cfg"], u, v, wt)
+    orc.set_state(P["w"], P["prim"], P["h"], P["b"])
     dt = kitgpu.timestep(KS, ctr, 0.0)
     assert dt == pytest.approx(orc.timestep(0.5, 0.0, 1.0), rel=1e-14)
     kitgpu.step(KS, ctr, dt, C3S_STEPS)
