@@ -8,7 +8,8 @@ not depend on who else shares the launch.  Every other request (the 2D
 cavities) owns a libkitgpu handle with its own CUDA stream, so its steps run
 concurrently with the pool and with each other.  The loop admits queued
 requests whenever a slot and the HBM budget allow, advances the pool by a
-chunk, enqueues a chunk for every idle handle (kb_step_async), polls
+chunk on a worker thread (so the loop keeps feeding the 2D solves while the
+pool steps), enqueues a chunk for every idle handle (kb_step_async), polls
 completions (kb_query) and retires a request when its residual (reference
 definition, src/Solver/solver_update.jl:86-88) falls below the tolerance or
 it reaches its step limit; its final state is downloaded and its memory
@@ -20,6 +21,7 @@ velocities in [32, 256]) and 40 % 2D lid-driven cavities (cells log-uniform
 in [16^2, 128^2], velocity grids in [16^2, 48^2], Kn log-uniform in
 [1e-4, 1]).
 """
+import concurrent.futures
 import math
 import time
 from dataclasses import dataclass, field
@@ -139,6 +141,8 @@ class Server:
         queue, active, pooled = [], [], []
         used = 0
         pool = None
+        pool_job = None  # (future, steps, launches before) of the pool chunk in flight
+        worker = concurrent.futures.ThreadPoolExecutor(max_workers=1)
         self.pool_launches = 0
         t0 = time.perf_counter()
         cv_total = 0
@@ -153,7 +157,7 @@ class Server:
             if on_retire:
                 on_retire(r)
 
-        while i < len(pending) or queue or active or pooled:
+        while i < len(pending) or queue or active or pooled or pool_job is not None:
             now = (time.perf_counter() - t0) * time_scale
             while i < len(pending) and pending[i].arrival <= now:
                 queue.append(pending[i])
@@ -165,6 +169,8 @@ class Server:
                 use_pool = (self.pool_1d and self.precision == "fp32" and KBATCH.poolable(KS)
                             and (pool is None or KBATCH.pool_key(KS) == pool.key)
                             and KS.ps.nx + 2 * KS.ps.ng <= self.pool_cells)
+                if use_pool and pool_job is not None:
+                    break  # the pool's chunk is in flight: join it when it returns
                 if use_pool and pool is None:
                     need = pool_bytes(self.pool_cells)
                     if used + need > self.hbm_budget and (active or pooled):
@@ -218,11 +224,18 @@ class Server:
                     n = min(self.chunk, r.max_steps - r.steps)
                     r.handle.step_async(r.dt, n)
                     r.inflight = n
-            # one chunk of the pool: every resident 1D request in each launch
-            if pooled:
-                n = self.chunk
+            # one chunk of the pool (every resident 1D request in each launch)
+            # runs on a worker thread, so that this loop keeps feeding and
+            # polling the 2D solves meanwhile; joins and leaves of the pool
+            # happen only between its chunks
+            if pooled and pool_job is None:
                 l0 = pool.launches()
-                res = pool.step(n, min(r.tol for r in pooled))
+                pool_job = (worker.submit(pool.step, self.chunk, min(r.tol for r in pooled)),
+                            self.chunk, l0)
+            if pool_job is not None and pool_job[0].done():
+                fut, n, l0 = pool_job
+                pool_job = None
+                res = fut.result()
                 self.pool_launches += pool.launches() - l0
                 still = []
                 for r in pooled:
@@ -262,6 +275,7 @@ class Server:
                 if wait > 0:
                     time.sleep(min(wait, 0.01))
         wall = time.perf_counter() - t0
+        worker.shutdown(wait=True)
         if pool is not None:
             pool.close()
         lat = np.array([r.latency for r in self.done if r.latency is not None]) / time_scale
