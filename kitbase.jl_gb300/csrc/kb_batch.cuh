@@ -314,15 +314,21 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
   {
     const int j = tid / SEG_FT, q = tid - j * SEG_FT;
     const int f = fa + j;
-    BSum<float> s0, s1, s2;
-    s0.init();
-    s1.init();
-    s2.init();
+    // Each moment term enters as an exact pair: the FP32 products w fh,
+    // w fh u, w fh u^2, w fb with their rounding errors (FMA), added with
+    // error-free sums (TwoSum).  In a supersonic flow the energy flux is
+    // large and the flux difference between a cell's two faces small, so
+    // FP32 rounding of the terms or of running partial sums would enter w as
+    // a bias of relative size ~1e-7 of the flux every step -- amplified in
+    // T = 1 / (2 lambda) by the kinetic-to-thermal energy ratio (~35 at
+    // Mach 8), it grew to 1e-5 of T within a few hundred steps.
+    DF m0, m1, m2;
+    m0.hi = m0.lo = m1.hi = m1.lo = m2.hi = m2.lo = 0.f;
+    float l0 = 0.f, l1 = 0.f, l2 = 0.f;  // sums of the products' rounding errors
     if (j <= SEG && f <= fb) {
       const int iL = f - 1, iR = f;
       const int rL = brule(iL, nx, ng), rR = brule(iR, nx, ng);
-      int it = 0;
-      for (int v = q; v < nu; v += SEG_FT, ++it) {
+      for (int v = q; v < nu; v += SEG_FT) {
         const float u = sU[v];
         const bool pos = u >= 0.f;
         const int c = pos ? iL : iR;
@@ -339,30 +345,33 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
         const float hf = h0 + side * sh, bf = b0 + side * sb;
         const float fh = T3 * u * hf - T4 * (u * u) * sh;
         const float fbb = T3 * u * bf - T4 * (u * u) * sb;
-        const float wf = sW[v] * fh;
-        s0.add(wf);
-        s1.add(wf * u);
-        s2.add(wf * u * u + sW[v] * fbb);
-        if ((it & 7) == 7) {
-          s0.flush();
-          s1.flush();
-          s2.flush();
-        }
+        // rounded products that the compiler may not fuse into a later add
+        // (a fused product would no longer match its error term)
+        const float wv = sW[v];
+        const float t0 = __fmul_rn(wv, fh), e0 = fmaf(wv, fh, -t0);  // w fh = t0 + e0 exactly
+        const float t1 = __fmul_rn(t0, u), e1 = fmaf(t0, u, -t1);
+        const float c1 = fmaf(e0, u, e1);                            // w fh u = t1 + c1
+        const float t2 = __fmul_rn(t1, u), e2 = fmaf(t1, u, -t2);
+        const float tb = __fmul_rn(wv, fbb), eb = fmaf(wv, fbb, -tb);
+        df_add(m0, t0);
+        df_add(m1, t1);
+        df_add(m2, t2);
+        df_add(m2, tb);
+        l0 += e0;
+        l1 += c1;
+        l2 += fmaf(c1, u, e2) + eb;                       // w (fh u^2 + fb) = t2 + tb + ...
       }
     }
-    // each thread's compensated partials, merged per face below in thread
-    // order: both segments that share a face map it to the same threads q,
-    // so they compute bit-identical fw (conservation holds exactly)
-    s0.flush();
-    s1.flush();
-    s2.flush();
+    // each thread's pairs, merged per face below in thread order: both
+    // segments that share a face map it to the same threads q, so they
+    // compute bit-identical fw (conservation holds exactly)
     float* o = sred + tid * 6;
-    o[0] = s0.d.hi;
-    o[1] = s0.d.lo;
-    o[2] = s1.d.hi;
-    o[3] = s1.d.lo;
-    o[4] = s2.d.hi;
-    o[5] = s2.d.lo;
+    o[0] = m0.hi;
+    o[1] = m0.lo + l0;
+    o[2] = m1.hi;
+    o[3] = m1.lo + l1;
+    o[4] = m2.hi;
+    o[5] = m2.lo + l2;
   }
   // the old prim of the stepped cells, read before warp 0 overwrites it
   // (warps 1 and 2 need the old U while warp 0 updates the cells)

@@ -155,11 +155,12 @@ def test_batch_autotune_picks_a_shape(gpu_lib):
 def test_batch_fp32_high_mach_accuracy(gpu_lib, coll):
     """Mach 6-8 shocks in the FP32 split form, started from the device-built
     equilibrium (kb_batch_init_equilibrium), against the FP64 batch after the
-    same 400 steps.  In the supersonic upstream flow the energy is ~35x the
-    thermal energy, so FP32 rounding of the stored distributions shows up
-    amplified in T = 1 / (2 lambda) next to the fixed upstream boundary: rho
-    and U stay within 1e-5, T within 1e-4 (the FP32 split form's bound in
-    this regime; the low-Mach configurations stay far inside 1e-5)."""
+    same 400 steps: rho, U and T within 1e-5.  In the supersonic upstream
+    flow the energy is ~35x the thermal energy, so any FP32 rounding that
+    reaches w shows up amplified in T = 1 / (2 lambda); the face moments are
+    therefore summed from exact product pairs with error-free additions (FP32
+    rounding of the moment terms had left T 1e-5 to 5e-5 off after 400
+    steps)."""
     cfgs = [KB.shock_config(Ma, nx, nu, coll=coll) for Ma, nx, nu in
             [(8.0, 200, 190), (7.5, 120, 104), (6.2, 300, 96)]]
     sets = KB.solver_sets(cfgs)
@@ -173,4 +174,4 @@ def test_batch_fp32_high_mach_accuracy(gpu_lib, coll):
         bt.close()
     for k in range(len(sets)):
         e_rho, e_u, e_t = rho_u_t_error(outs["fp32"][k]["prim"], outs["fp64"][k]["prim"])
-        assert e_rho < 1e-5 and e_u < 1e-5 and e_t < 1e-4, (k, e_rho, e_u, e_t)
+        assert e_rho < 1e-5 and e_u < 1e-5 and e_t < 1e-5, (k, e_rho, e_u, e_t)
