@@ -305,6 +305,18 @@ __global__ void k_batch_init_eq32(BatchDev B, int b0, float* H0, float* B0, floa
   seg_init_cell(B, b, blockIdx.x, H0, B0, H1, B1);
 }
 
+// FP32 Maxwellian coefficients of every cell from its prim (after a host
+// upload of prim): blockIdx.y = instance, one thread per cell.
+__global__ void k_batch_mcache(BatchDev B) {
+  const int b = blockIdx.y;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= B.nx[b] + 2 * B.ng[b]) return;
+  const long cell = B.cell_off[b] + c;
+  SegMax m;
+  m.set(B.prim + cell * 4, B.K);
+  seg_store_coef(B, cell, m);
+}
+
 // FP64 form: h = maxwellian(u, prim), b = h K / (2 lambda) in FP64
 // (src/Theory/theory_equilibrium.jl:8-13) into both buffers.
 __global__ void k_batch_init_eq64(BatchDev B, double* H0, double* B0, double* H1, double* B1) {
@@ -554,7 +566,7 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   double* d_respart;
   long *d_co, *d_eo, *d_fo;
   double *d_dx, *d_dt, *d_mu, *d_u, *d_w, *d_wv, *d_prim, *d_fw, *d_q, *d_cp, *d_res;
-  float *d_uf, *d_wf, *d_ul;
+  float *d_uf, *d_wf, *d_ul, *d_mc;
   BALLOC(d_order, int, n);
   BALLOC(d_nx, int, n);
   BALLOC(d_ng, int, n);
@@ -585,6 +597,7 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   BALLOC(d_fw, double, faces * 4);
   BALLOC(d_q, double, cells);
   BALLOC(d_cp, double, cells * 16);
+  BALLOC(d_mc, float, cells * 8);
   BALLOC(d_res, double, (size_t)n * 4);
   BALLOC(B->d_umax, double, n);
   size_t esz = B->prec == KB_PREC_FP64 ? 8 : 4;
@@ -667,6 +680,7 @@ extern "C" int kb_batch_create(const kb_config_t* base, int32_t n, const int32_t
   d.face_off = d_fo;
   d.q = d_q;
   d.cp = d_cp;
+  d.mc = d_mc;
   d.residual = d_res;
   d.active = d_active;
   d.counter = d_counter;
@@ -725,6 +739,13 @@ extern "C" int kb_batch_upload(kb_batch_t* B, const double* w, const double* pri
         kb::k_batch_convert<float><<<g, 256, 0, B->stream>>>((float*)dst, B->d_stage, n);
       B->launches++;
     }
+    cudaStreamSynchronize(B->stream);
+  }
+  if (B->prec == KB_PREC_FP32) {  // the FP32 step reads each cell's Maxwellian coefficients
+    int maxc = 1;
+    for (int b = 0; b < B->n; ++b) maxc = std::max(maxc, B->nx[b] + 2 * B->ng[b]);
+    kb::k_batch_mcache<<<dim3((unsigned)((maxc + 127) / 128), (unsigned)B->n), 128, 0, B->stream>>>(B->d);
+    B->launches++;
     cudaStreamSynchronize(B->stream);
   }
   std::vector<int> ones(B->n, 1);

@@ -39,6 +39,8 @@ struct BatchDev {
   const long* face_off;
   double* q;             // [cell] old heat flux
   double* cp;            // [cell][16] cell coefficients (see k_batch_step)
+  float* mc;             // [cell][8] FP32 Maxwellian coefficients of the cell's current prim
+                         // (SegMax: rn, U hi, lambda, K / (2 lambda), U lo), kept with prim
   double* residual;      // [n][4]
   int* active;           // [n] 1 while not converged
   int* counter;          // work counter
@@ -151,12 +153,20 @@ struct SegMax {
   }
 };
 
+// The cell's FP32 Maxwellian coefficients into B.mc (kept with its prim).
+__device__ __forceinline__ void seg_store_coef(const BatchDev& B, long cell, const SegMax& m) {
+  float4* mcc = (float4*)(B.mc + cell * 8);
+  mcc[0] = make_float4(m.rn, m.Uh, m.lam, m.cB);
+  mcc[1] = make_float4(m.Ul, 0.f, 0.f, 0.f);
+}
+
 // Equilibrium h, b of cell c (0-based incl. ghosts) of instance b into both
 // FP32 buffers (init_fvm, src/Solver/solver_init.jl:119-141); row padding zero.
 __device__ __forceinline__ void seg_init_cell(const BatchDev& B, int b, int c, float* H0, float* B0,
                                               float* H1, float* B1) {
   SegMax m;
   m.set(B.prim + (B.cell_off[b] + c) * 4, B.K);
+  if (threadIdx.x == 0) seg_store_coef(B, B.cell_off[b] + c, m);
   const int nu = B.nu[b], ns = B.nus[b];
   const long e = B.elem_off[b] + (long)c * ns;
   const float* uf = B.uf + B.vel_off[b];
@@ -445,21 +455,29 @@ __global__ void __launch_bounds__(SEG_T) k_batch_seg(BatchDev B, const float* __
       const float tau = float(B.mu[b]) * 2.f * powf(lf, float(1.0 - B.omega)) / rf;
       const float dtt = float(dt) / tau;
       const double Kd = B.K;
-      const float oUh = float(Uo);
       float4* kc = scc + lane * SEG_CC;
+      // the old Maxwellian's coefficients are the ones this cell's update
+      // formed from the same prim one step earlier (or the set-up formed from
+      // the initial prim): read instead of recomputed, which saves an FP64
+      // square root and division per cell, bit for bit the same values
+      float4* mcc = (float4*)(B.mc + c * 8);
+      const float4 mo = mcc[0];
+      const float mUl = mcc[1].x;
       // new Maxwellian: density factor, U (hi), lambda, K / (2 lambda)
       SegMax mn;
       mn.set(pn, Kd);
       kc[0] = make_float4(mn.rn, mn.Uh, mn.lam, mn.cB);
       // dt / tau, 1 / (1 + dt / tau), old Maxwellian (Shakhov) density factor and U (hi)
-      kc[1] = make_float4(dtt, 1.f / (1.f + dtt), float(rho_o * sqrt(lo * (1.0 / PI))), oUh);
+      kc[1] = make_float4(dtt, 1.f / (1.f + dtt), mo.x, mo.y);
       // old lambda, K / (2 lambda); .z (the Shakhov heat-flux factor) comes
       // from warps 1-2; .w the low part of U
       float* k2 = (float*)(kc + 2);
-      k2[0] = float(lo);
-      k2[1] = float(Kd / (2.0 * lo));
+      k2[0] = mo.z;
+      k2[1] = mo.w;
       k2[3] = mn.Ul;
-      kc[3] = make_float4(float(Uo - (double)oUh), 0.f, 0.f, 0.f);
+      kc[3] = make_float4(mUl, 0.f, 0.f, 0.f);
+      mcc[0] = make_float4(mn.rn, mn.Uh, mn.lam, mn.cB);
+      mcc[1] = make_float4(mn.Ul, 0.f, 0.f, 0.f);
     }
     // residual partial sums of the segment, in a fixed shuffle order (FP32:
     // GB300's FP64 pipe would make this tree the longest chain of the phase)
