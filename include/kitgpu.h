@@ -220,6 +220,36 @@ int kb_upload_slopes(kb_handle_t* h, const double* sw);
  * bounded device wait (coefficient staging of the update pass) gave up. */
 int kb_status(kb_handle_t* h);
 
+/* Groups of 2D solves advanced together (continuous batching of served 2D
+ * requests; no reference counterpart -- the reference runs each solve! on
+ * its own, src/Solver/solver_main.jl:12-150).  A group advances all of its
+ * member handles with ONE launch of each step kernel per step; a member's
+ * result is bit-identical to stepping it alone with the launch shapes the
+ * group uses (kb_set_tuning 2, 8, 128, 2: 2-column strips of 8 rows, one
+ * velocity per thread, pass A with 2 faces per warp).  Members: 2D FP32-split
+ * KCU solves, BGK or Shakhov (one model per group), without ghost-filled
+ * boundaries, small enough for 32-thread cell blocks (fewer than two
+ * 256-thread blocks per multiprocessor).  Members join and leave between
+ * chunks (after kb_group_query reported the chunk done); while in a group a
+ * handle must not be stepped on its own.  A group has its own stream.
+ *   kb_group_create    capacity = most members at a time
+ *   kb_group_add       member with its time step dt (KB_ERR_CONFIG when the
+ *                      solve is not covered)
+ *   kb_group_step_async  enqueue nsteps steps of every member
+ *   kb_group_query     *ready = 1 once the chunk finished; residual [n][4]
+ *                      and status [n] (KB_OK / KB_ERR_NUMERIC /
+ *                      KB_ERR_TIMEOUT) in member order (order of joining,
+ *                      members that left removed); either may be NULL
+ *   kb_group_info      members and kernel launches so far */
+typedef struct kb_group kb_group_t;
+int kb_group_create(int32_t capacity, kb_group_t** out);
+int kb_group_destroy(kb_group_t* g);
+int kb_group_add(kb_group_t* g, kb_handle_t* h, double dt);
+int kb_group_remove(kb_group_t* g, kb_handle_t* h);
+int kb_group_step_async(kb_group_t* g, int32_t nsteps);
+int kb_group_query(kb_group_t* g, double* residual, int32_t* status, int32_t* ready);
+int kb_group_info(kb_group_t* g, int32_t* members, int64_t* launches);
+
 /* Test of the bounded device waits, no reference counterpart: one CTA waits
  * through the same bounded mbarrier wait the staging kernels use, on a phase
  * that nothing completes.  The wait gives up after limit_s (0 < limit_s <= 2)

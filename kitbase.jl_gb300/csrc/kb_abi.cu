@@ -15,46 +15,12 @@
 #include <vector>
 
 #include "../../include/kitgpu.h"
+#include "kb_handle.h"
 #include "kb_kernels.cuh"
 
 using kb::DevState;
 using kb::Geo;
 
-struct kb_handle {
-  kb_config_t cfg;
-  DevState s;
-  cudaStream_t stream = nullptr;
-  int device = 0;
-  int nvel = 0, vstride = 0;
-  long ncell = 0;
-  int nface = 0;
-  int64_t bytes = 0;
-  int64_t launches = 0;
-  std::vector<void*> allocs;
-  double* d_stage = nullptr;  // host-layout staging buffer for up/downloads
-  long stage_elems = 0;
-  double* d_scalar = nullptr; // [8] scratch scalars
-  bool evolved = false;
-  // asynchronous stepping (kb_step_async / kb_query)
-  double* h_res = nullptr;    // pinned host copy of residual[4] + status
-  cudaEvent_t ev_done = nullptr;
-  bool pending = false;
-  // chunks of kb_step_async replayed as CUDA graphs: one executable graph per
-  // starting buffer index, valid for one (dt, nsteps) and the current tuning
-  cudaGraphExec_t agraph[2] = {nullptr, nullptr};
-  double agraph_dt = 0.0;
-  int agraph_n = 0;
-  int64_t agraph_launches = 0;
-  // per-stage kernel timing (kb_set_timing): CUDA events on the handle stream
-  bool timing = false;
-  std::vector<cudaEvent_t> events;
-  double stage_ms[KB_NSTAGE] = {0};
-  int64_t stage_n[KB_NSTAGE] = {0};
-  // TMA descriptors of the FP32 form: [0, 8) the 2D update, [strip width 2, 4]
-  // [buffer][h, b]; [8, 24) the moment pass, [direction][faces per warp 2, 4]
-  // [buffer][h, b]
-  CUtensorMap tmaps[24];
-};
 
 
 static thread_local std::string g_err;
@@ -316,6 +282,7 @@ int kb_create(const kb_config_t* cfg, const double* u, const double* v, const do
   ALLOC(h->s.cc, kb::CellCoef32, h->ncell);
   ALLOC(h->s.blockres, double, (size_t)h->s.res_blocks * 16);
   h->s.mpart = nullptr;
+  h->s.grp = nullptr;
   if (c.precision == KB_PREC_FP32 && g.D == 2) {
     const size_t nbox = (size_t)(g.nvel + kb::KB_TMA_VBOX - 1) / kb::KB_TMA_VBOX;
     ALLOC(h->s.mpart, float2, 2 * nbox * h->nface * 4);  // two warps per face and box

@@ -44,10 +44,13 @@ void face_kinds_host(const Geo& g, signed char* kind) {
 // one thread per (physical cell, direction).
 // FAST (the FP32 split form): one reciprocal of the cell size per thread in
 // place of two FP64 divisions per component.
-template <bool FAST>
-__global__ void k_wslope(DevState s) {
+template <bool FAST, bool GRP = false>
+__global__ void k_wslope(DevState sp) {
+  int lb;
+  const int gr = group_member<GRP, GK_WSLOPE>(sp, lb);
+  const DevState& s = group_state<GRP>(sp, gr);
   const Geo& g = s.g;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = lb * blockDim.x + threadIdx.x;
   int n = g.nx * g.ny;
   if (t >= n * g.D) return;
   int d = t / n, c0 = t % n;
@@ -138,10 +141,14 @@ __device__ __forceinline__ FaceCoef32 face_coef32(const Geo& g, const FaceParam&
 // flux_ugks.jl:47-56), then the KCU / UGKS time integrals, UGKS slopes and
 // the analytic part of fw.  One thread per face.
 // FAST: the FP32 split form (transcendentals in FP32, see t_exp).
-template <int D, int FLUX, bool FAST>
-__global__ void k_face_param(DevState s, double dt) {
+template <int D, int FLUX, bool FAST, bool GRP = false>
+__global__ void k_face_param(DevState sp, double dt_arg) {
+  int lb;
+  const int gr = group_member<GRP, GK_FACE>(sp, lb);
+  const DevState& s = group_state<GRP>(sp, gr);
+  const double dt = GRP ? sp.grp->dt[gr] : dt_arg;
   const Geo& g = s.g;
-  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  int f = lb * blockDim.x + threadIdx.x;
   if (f >= s.nface_x + s.nface_y) return;
   if (s.kind[f] != 1) return;
   FaceGeo r = face_geo(g, f);
@@ -277,11 +284,15 @@ __global__ void k_face_param(DevState s, double dt) {
 // shared by all its warps, each warp sums its part, and thread 0 adds the
 // warps' sums in warp order (deterministic) and finishes the face.
 constexpr int WALL_T = 128;
-template <typename R, int D>
-__global__ void __launch_bounds__(WALL_T) k_wall(DevState s, double dt) {
+template <typename R, int D, bool GRP = false>
+__global__ void __launch_bounds__(WALL_T) k_wall(DevState sp, double dt_arg) {
   __shared__ double part[WALL_T / 32][8];
+  int lb;
+  const int gr = group_member<GRP, GK_WALL>(sp, lb);
+  const DevState& s = group_state<GRP>(sp, gr);
+  const double dt = GRP ? sp.grp->dt[gr] : dt_arg;
   const Geo& g = s.g;
-  const int f = s.wall_list[blockIdx.x];
+  const int f = s.wall_list[lb];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   FaceGeo r = face_geo(g, f);
   int pos = r.d == 0 ? r.fi : r.fj;
@@ -408,11 +419,15 @@ __device__ inline int update_group(const Geo& g, int i, int j) {
 // offsets of the coefficient blocks with FP32 transcendentals, conserve_prim
 // by reciprocals (see t_exp); w and prim stay FP64.  BS threads per block
 // (32 on small grids, 256 otherwise: DevState::cell_bs).
-template <int D, bool FAST, int BS>
-__global__ void __launch_bounds__(BS) k_cell_param(DevState s, double dt) {
+template <int D, bool FAST, int BS, bool GRP = false>
+__global__ void __launch_bounds__(BS) k_cell_param(DevState sp, double dt_arg) {
+  int lb;
+  const int gr = group_member<GRP, GK_CELL>(sp, lb);
+  const DevState& s = group_state<GRP>(sp, gr);
+  const double dt = GRP ? sp.grp->dt[gr] : dt_arg;
   const Geo& g = s.g;
   __shared__ double red[BS][8];
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = lb * BS + threadIdx.x;
   double rr[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int grp = 0;
   if (t < g.nx * g.ny) {
@@ -530,14 +545,18 @@ __global__ void __launch_bounds__(BS) k_cell_param(DevState s, double dt) {
       __syncthreads();
     }
     if (threadIdx.x == 0)
-      for (int k = 0; k < 8; ++k) s.blockres[(long)blockIdx.x * 16 + half * 8 + k] = red[0][k];
+      for (int k = 0; k < 8; ++k) s.blockres[(long)lb * 16 + half * 8 + k] = red[0][k];
     __syncthreads();
   }
 }
 
 // residual = sqrt(sumRes N) / (sumAvg + 1e-7) + sqrt(boundary sumRes 2) / (...)
 // (src/Solver/solver_update.jl:86-88, :239-241; update_boundary.jl:41-44, :284-288).
-__global__ void k_residual(DevState s) {
+template <bool GRP = false>
+__global__ void k_residual(DevState sp) {
+  int lb;
+  const int gr = group_member<GRP, GK_RES>(sp, lb);
+  const DevState& s = group_state<GRP>(sp, gr);
   __shared__ double red[256][16];
   double acc[16];
   for (int k = 0; k < 16; ++k) acc[k] = 0.0;
@@ -937,10 +956,50 @@ static int finish_t(DevState& s, cudaStream_t st) {
     if (s.g.ngx > 0) { k_ghost<R><<<2 * s.g.ngx * nrow, 128, 0, st>>>(t, 0); ++n; }
     if (D == 2 && s.g.ngy > 0) { k_ghost<R><<<2 * s.g.ngy * s.g.nxt, 128, 0, st>>>(t, 1); ++n; }
   }
-  prefer_max_shared((const void*)k_residual);
-  k_residual<<<1, 256, 0, st>>>(s);
+  prefer_max_shared((const void*)k_residual<false>);
+  k_residual<false><<<1, 256, 0, st>>>(s);
   ++n;
   return n;
+}
+
+// ---- grouped launches (kb_group.cu): the per-face / per-cell kernels of one
+// step of the 2D FP32 form over all members of a group; ls.grp points at
+// the step's member table, the block counts are the members' summed.
+void group_small(int kind, const DevState& ls, int flux, int blocks, cudaStream_t st) {
+  if (blocks <= 0) return;
+  const void* fn = nullptr;
+  switch (kind) {
+    case GK_WSLOPE:
+      fn = (const void*)k_wslope<true, true>;
+      prefer_max_shared(fn);
+      k_wslope<true, true><<<blocks, 32, 0, st>>>(ls);
+      break;
+    case GK_FACE: {
+      void (*f)(DevState, double) = flux == FLUX_KFVS ? k_face_param<2, FLUX_KFVS, true, true>
+                                    : flux == FLUX_KCU ? k_face_param<2, FLUX_KCU, true, true>
+                                                       : k_face_param<2, FLUX_UGKS, true, true>;
+      prefer_max_shared((const void*)f);
+      f<<<blocks, 32, 0, st>>>(ls, 0.0);
+      break;
+    }
+    case GK_WALL:
+      fn = (const void*)k_wall<float, 2, true>;
+      prefer_max_shared(fn);
+      k_wall<float, 2, true><<<blocks, WALL_T, 0, st>>>(ls, 0.0);
+      break;
+    case GK_CELL:
+      fn = (const void*)k_cell_param<2, true, 32, true>;
+      prefer_max_shared(fn);
+      k_cell_param<2, true, 32, true><<<blocks, 32, 0, st>>>(ls, 0.0);
+      break;
+    case GK_RES:
+      fn = (const void*)k_residual<true>;
+      prefer_max_shared(fn);
+      k_residual<true><<<blocks, 256, 0, st>>>(ls);
+      break;
+    default:
+      break;
+  }
 }
 
 int launch_finish(DevState& s, cudaStream_t st) {

@@ -2,6 +2,8 @@
 // DVM kernels (kb_kernels.cu).
 #pragma once
 
+#include <cuda.h>
+
 #include <string>
 
 #include "kb_device.cuh"
@@ -18,6 +20,8 @@ void set_error(const std::string& msg);
 // Tunable launch shapes (kb_set_tuning); 0 selects the built-in default.
 enum { KB_TUNE_MARCH_TX = 0, KB_TUNE_MARCH_RY = 1, KB_TUNE_MARCH_BS = 2, KB_TUNE_MOM_TS = 3,
        TUNE_N = 4 };
+
+struct GroupTab;
 
 // Device buffers of one solve (owned by kb_handle, see kb_abi.cu).
 struct DevState {
@@ -62,6 +66,7 @@ struct DevState {
   int ncell;
   int res_blocks;   // number of blocks of k_cell_param
   int cell_bs;      // threads per block of k_cell_param (32 or 256)
+  const GroupTab* grp;  // device table of a grouped launch (kb_group_*), else null
   int sm_count;     // multiprocessors of the device: small grids spread their
                     // FP64-heavy per-face / per-cell threads over more of them
 };
@@ -69,6 +74,50 @@ struct DevState {
 // Ask for the largest shared-memory carveout for kernel fn on the current
 // device (once per kernel and device; see kb_kernels.cu).
 void prefer_max_shared(const void* fn);
+
+// One launch of a step kernel over the members of a group of 2D solves
+// (kb_group_*): member r owns blocks [start[k][r], start[k][r + 1]) of the
+// launch of kernel kind k, and runs there exactly the blocks it runs in its
+// own launch, so its results are bit-identical alone and in the group.
+enum { GK_WSLOPE = 0, GK_FACE, GK_MOMX, GK_MOMY, GK_WALL, GK_CELL, GK_MARCH, GK_RES, GK_N };
+struct GroupTab {
+  int n;                    // members
+  const DevState* states;   // [n] member states, buffer index of this step
+  const double* dt;         // [n] member time steps
+  const CUtensorMap* maps;  // [n][6] TMA maps of this step: pass A x (h, b), y (h, b), pass B (h, b)
+  const int* start;         // [GK_N][n + 1] first block of each member per kernel kind
+};
+
+// The member a block of a grouped launch belongs to, and the block's index in
+// that member's own launch (a plain launch: member 0, the block itself).
+template <bool GRP, int KIND>
+__device__ __forceinline__ int group_member(const DevState& sp, int& lb) {
+  if constexpr (!GRP) {
+    lb = blockIdx.x;
+    return 0;
+  } else {
+    const GroupTab& t = *sp.grp;
+    const int* st = t.start + KIND * (t.n + 1);
+    const int b = blockIdx.x;
+    int lo = 0, hi = t.n - 1;  // the last member whose first block is <= b
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (st[mid] <= b) lo = mid;
+      else hi = mid - 1;
+    }
+    lb = b - st[lo];
+    return lo;
+  }
+}
+template <bool GRP>
+__device__ __forceinline__ const DevState& group_state(const DevState& sp, int r) {
+  if constexpr (GRP) return sp.grp->states[r];
+  else return sp;
+}
+
+// Grouped launch of a per-face / per-cell step kernel (kind GK_WSLOPE,
+// GK_FACE, GK_WALL, GK_CELL or GK_RES) over `blocks` blocks (kb_kernels.cu).
+void group_small(int kind, const DevState& ls, int flux, int blocks, cudaStream_t st);
 
 // Face classification for the current configuration (host computes, uploads).
 void face_kinds_host(const Geo& g, signed char* kind);

@@ -313,11 +313,21 @@ struct MomStage {
 };
 constexpr int MOM_THREADS = 160;  // 4 consumer warps + 1 producer warp
 
-template <int D, int FLUX, int TS, bool SHAK, int DIR>
+template <int D, int FLUX, int TS, bool SHAK, int DIR, bool GRP = false>
 __global__ void __launch_bounds__(MOM_THREADS) k_mom_st(const __grid_constant__ CUtensorMap tmh,
                                                         const __grid_constant__ CUtensorMap tmb,
-                                                        DevState s) {
+                                                        DevState sp) {
   using R = float;
+  int lb;
+  const int gr = group_member<GRP, DIR == 0 ? GK_MOMX : GK_MOMY>(sp, lb);
+  const DevState& s = group_state<GRP>(sp, gr);
+  // a grouped launch reads each member's tensor maps from global memory
+  const CUtensorMap* mh = GRP ? sp.grp->maps + gr * 6 + DIR * 2 : &tmh;
+  const CUtensorMap* mb = GRP ? sp.grp->maps + gr * 6 + DIR * 2 + 1 : &tmb;
+  if (GRP && threadIdx.x == 4 * 32) {  // the producer warp's issuing lane
+    tmap_acquire(mh);
+    tmap_acquire(mb);
+  }
   using SL = MomStage<TS>;
   extern __shared__ __align__(1024) unsigned char smemA[];
   float* stg = (float*)smemA;
@@ -330,7 +340,7 @@ __global__ void __launch_bounds__(MOM_THREADS) k_mom_st(const __grid_constant__ 
   const int n = DIR == 0 ? g.nx : g.ny;  // cells along the line
   const int ng = DIR == 0 ? g.ngx : g.ngy;
   const int nseg = (n + SL::NF - 1) / SL::NF;
-  const int line = blockIdx.x / nseg, sgi = blockIdx.x - line * nseg;
+  const int line = lb / nseg, sgi = lb - line * nseg;
   const int p0 = sgi * SL::NF;      // first face of the CTA segment
   const int p0w = p0 + wid * TS;    // first face of this warp
   const int ncell = wid == PRODUCER ? 0 : max(0, min(TS, n - p0w));
@@ -366,8 +376,8 @@ __global__ void __launch_bounds__(MOM_THREADS) k_mom_st(const __grid_constant__ 
     const unsigned cb = (unsigned)min(MOM_VC, vs - v0) * 4u;  // a multiple of 16
     if (lane == 0) {
       mbar_expect(bar, 2u * SL::BOX * 4u + 3u * cb);
-      tma_load_3d(S, &tmh, v0, cx, cy, bar);
-      tma_load_3d(S + SL::BOX, &tmb, v0, cx, cy, bar);
+      tma_load_3d(S, mh, v0, cx, cy, bar);
+      tma_load_3d(S + SL::BOX, mb, v0, cx, cy, bar);
       for (int t = 0; t < 3; ++t) bulk_g2s(S + 2 * SL::BOX + t * MOM_VC, vtab<R>(s, t) + v0, cb, bar);
     }
     __syncwarp();
@@ -1280,11 +1290,28 @@ struct M3Layout {
 // (per-slot "empty" mbarriers), so only thread 0 ever waits on other warps
 // and the window costs no registers.  Each
 // x face and y face is evaluated once per velocity and feeds both neighbours.
-template <int FLUX, int TX, int NS>
+template <int FLUX, int TX, int NS, bool GRP = false>
 __global__ void __launch_bounds__(M3_BS) k_march3(const __grid_constant__ CUtensorMap tmh,
                                                   const __grid_constant__ CUtensorMap tmb,
-                                                  DevState s, int RY) {
+                                                  DevState sp, int RY) {
   static_assert(NS >= 6, "the ring holds the 4-row window plus at least one row ahead");
+  int lb;
+  const int gr = group_member<GRP, GK_MARCH>(sp, lb);
+  const DevState& s = group_state<GRP>(sp, gr);
+  const CUtensorMap* mh = GRP ? sp.grp->maps + gr * 6 + 4 : &tmh;
+  const CUtensorMap* mb = GRP ? sp.grp->maps + gr * 6 + 5 : &tmb;
+  if (GRP && threadIdx.x == 0) {  // the issuing thread
+    tmap_acquire(mh);
+    tmap_acquire(mb);
+  }
+  // block coordinates (velocity box, strip, row block) in the member's own grid
+  int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
+  if (GRP) {
+    const int gx = (s.g.nvel + M3_BS - 1) / M3_BS, gy = (s.g.nx + TX - 1) / TX;
+    bx = lb % gx;
+    by = (lb / gx) % gy;
+    bz = lb / (gx * gy);
+  }
   using L = M3Layout<TX, NS>;
   constexpr int D = 2;
   extern __shared__ __align__(1024) unsigned char smem3[];
@@ -1294,13 +1321,13 @@ __global__ void __launch_bounds__(M3_BS) k_march3(const __grid_constant__ CUtens
   volatile int* vbad = bad;
   const Geo& g = s.g;
   const int tid = threadIdx.x, lane = tid & 31;
-  const int v0 = blockIdx.x * M3_BS;
+  const int v0 = bx * M3_BS;
   const int vraw = v0 + tid;
   const bool vok = vraw < g.nvel;
   const int v = vok ? vraw : g.nvel - 1;
-  const int i0 = blockIdx.y * TX;
+  const int i0 = by * TX;
   const int ncol = min(TX, g.nx - i0);
-  const int j0 = blockIdx.z * RY;
+  const int j0 = bz * RY;
   const int j1 = min(g.ny, j0 + RY);
   const int q0 = j0 - 2;    // first staged row
   const int qend = j1 + 1;  // last staged row
@@ -1321,8 +1348,8 @@ __global__ void __launch_bounds__(M3_BS) k_march3(const __grid_constant__ CUtens
     const unsigned xb = (ncol + 1) * sizeof(FaceCoef32), yb = ncol * sizeof(FaceCoef32),
                    cb = ncol * sizeof(CellCoef32);
     mbar_expect(bar, 2 * L::BOX + (hy ? yb : 0u) + (hx ? xb + cb : 0u));
-    tma_load_3d(S, &tmh, v0, i0 - 2 + g.ngx, q + g.ngy, bar);
-    tma_load_3d(S + L::BOX, &tmb, v0, i0 - 2 + g.ngx, q + g.ngy, bar);
+    tma_load_3d(S, mh, v0, i0 - 2 + g.ngx, q + g.ngy, bar);
+    tma_load_3d(S + L::BOX, mb, v0, i0 - 2 + g.ngx, q + g.ngy, bar);
     if (hx) {
       bulk_g2s(C + L::XF, s.fc + (long)q * (g.nx + 1) + i0, xb, bar);
       bulk_g2s(C + L::CC, s.cc + cell_index(g, i0, q), cb, bar);

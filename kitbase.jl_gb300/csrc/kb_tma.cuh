@@ -72,6 +72,15 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
       : "memory");
 }
 
+// A tensor map in global memory that was written before the launch (the
+// table of a grouped launch): acquire it for the tensor-map proxy before the
+// first copy that uses it.
+__device__ __forceinline__ void tmap_acquire(const CUtensorMap* m) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                   reinterpret_cast<unsigned long long>(m))
+               : "memory");
+}
+
 // 3D tiled tensor load (TMA) of one box into shared memory, completed on an
 // mbarrier.  Coordinates outside the tensor read as zero.
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1,

@@ -86,6 +86,13 @@ SIGNATURES = {
     "kb_query": [_H, _D, ctypes.POINTER(ctypes.c_int32)],
     "kb_get_tuning": [_H, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32],
     "kb_wait_probe": [ctypes.c_double, ctypes.POINTER(ctypes.c_int32), _D],
+    "kb_group_create": [ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)],
+    "kb_group_destroy": [ctypes.c_void_p],
+    "kb_group_add": [ctypes.c_void_p, _H, ctypes.c_double],
+    "kb_group_remove": [ctypes.c_void_p, _H],
+    "kb_group_step_async": [ctypes.c_void_p, ctypes.c_int32],
+    "kb_group_query": [ctypes.c_void_p, _D, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)],
+    "kb_group_info": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64)],
 }
 STAGES = ("reconstruct", "face_param", "moments", "wall", "cell_param", "update", "finish")
 
