@@ -149,11 +149,17 @@ static int group_build(kb_group* G) {
     for (int k = 0; k < kb::GK_N; ++k) start[(size_t)k * (n + 1) + r + 1] = start[(size_t)k * (n + 1) + r] + nb[k];
     const CUtensorMap* tm = h->tmaps;
     for (int p = 0; p < 2; ++p) {
+      // the member's state with the buffer that is current at this parity
+      // in slot 0 (the grouped kernels take cur as the constant 0)
+      const int c = h->s.cur ^ p;
       DevState s = h->s;
-      s.cur = h->s.cur ^ p;
+      s.h[0] = h->s.h[c];
+      s.h[1] = h->s.h[c ^ 1];
+      s.b[0] = h->s.b[c];
+      s.b[1] = h->s.b[c ^ 1];
+      s.cur = 0;
       s.grp = nullptr;
       st[(size_t)p * G->cap + r] = s;
-      const int c = s.cur;
       CUtensorMap* m = &maps[((size_t)p * G->cap + r) * 6];
       m[0] = tm[8 + ((0 * 2 + 0) * 2 + c) * 2];  // pass A x faces, 2 faces per warp: h
       m[1] = tm[8 + ((0 * 2 + 0) * 2 + c) * 2 + 1];

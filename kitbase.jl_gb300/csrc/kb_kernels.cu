@@ -48,7 +48,7 @@ template <bool FAST, bool GRP = false>
 __global__ void k_wslope(DevState sp) {
   int lb;
   const int gr = group_member<GRP, GK_WSLOPE>(sp, lb);
-  const DevState& s = group_state<GRP>(sp, gr);
+  KB_GROUP_STATE(GRP, sp, gr);
   const Geo& g = s.g;
   int t = lb * blockDim.x + threadIdx.x;
   int n = g.nx * g.ny;
@@ -145,7 +145,7 @@ template <int D, int FLUX, bool FAST, bool GRP = false>
 __global__ void k_face_param(DevState sp, double dt_arg) {
   int lb;
   const int gr = group_member<GRP, GK_FACE>(sp, lb);
-  const DevState& s = group_state<GRP>(sp, gr);
+  KB_GROUP_STATE(GRP, sp, gr);
   const double dt = GRP ? sp.grp->dt[gr] : dt_arg;
   const Geo& g = s.g;
   int f = lb * blockDim.x + threadIdx.x;
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(WALL_T) k_wall(DevState sp, double dt_arg) {
   __shared__ double part[WALL_T / 32][8];
   int lb;
   const int gr = group_member<GRP, GK_WALL>(sp, lb);
-  const DevState& s = group_state<GRP>(sp, gr);
+  KB_GROUP_STATE(GRP, sp, gr);
   const double dt = GRP ? sp.grp->dt[gr] : dt_arg;
   const Geo& g = s.g;
   const int f = s.wall_list[lb];
@@ -423,7 +423,7 @@ template <int D, bool FAST, int BS, bool GRP = false>
 __global__ void __launch_bounds__(BS) k_cell_param(DevState sp, double dt_arg) {
   int lb;
   const int gr = group_member<GRP, GK_CELL>(sp, lb);
-  const DevState& s = group_state<GRP>(sp, gr);
+  KB_GROUP_STATE(GRP, sp, gr);
   const double dt = GRP ? sp.grp->dt[gr] : dt_arg;
   const Geo& g = s.g;
   __shared__ double red[BS][8];
@@ -556,7 +556,7 @@ template <bool GRP = false>
 __global__ void k_residual(DevState sp) {
   int lb;
   const int gr = group_member<GRP, GK_RES>(sp, lb);
-  const DevState& s = group_state<GRP>(sp, gr);
+  KB_GROUP_STATE(GRP, sp, gr);
   __shared__ double red[256][16];
   double acc[16];
   for (int k = 0; k < 16; ++k) acc[k] = 0.0;

@@ -109,11 +109,18 @@ __device__ __forceinline__ int group_member(const DevState& sp, int& lb) {
     return lo;
   }
 }
-template <bool GRP>
-__device__ __forceinline__ const DevState& group_state(const DevState& sp, int r) {
-  if constexpr (GRP) return sp.grp->states[r];
-  else return sp;
-}
+// The state a kernel body reads as `s`: the launch's own parameter, or in a
+// grouped launch a private copy of the member's state.  The group's tables
+// hold each member's state with its current buffer in slot 0 (cur = 0), and
+// the copy sets cur to the constant 0, so that `s.h[s.cur ^ 1]` and the like
+// index with constants and the copy's fields stay in registers.
+#define KB_GROUP_STATE(GRP, sp, gr)           \
+  DevState s_member_;                         \
+  if constexpr (GRP) {                        \
+    s_member_ = (sp).grp->states[gr];         \
+    s_member_.cur = 0;                        \
+  }                                           \
+  const DevState& s = (GRP) ? s_member_ : (sp)
 
 // Grouped launch of a per-face / per-cell step kernel (kind GK_WSLOPE,
 // GK_FACE, GK_WALL, GK_CELL or GK_RES) over `blocks` blocks (kb_kernels.cu).

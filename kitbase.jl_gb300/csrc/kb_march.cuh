@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(MOM_THREADS) k_mom_st(const __grid_constant__ 
   using R = float;
   int lb;
   const int gr = group_member<GRP, DIR == 0 ? GK_MOMX : GK_MOMY>(sp, lb);
-  const DevState& s = group_state<GRP>(sp, gr);
+  KB_GROUP_STATE(GRP, sp, gr);
   // a grouped launch reads each member's tensor maps from global memory
   const CUtensorMap* mh = GRP ? sp.grp->maps + gr * 6 + DIR * 2 : &tmh;
   const CUtensorMap* mb = GRP ? sp.grp->maps + gr * 6 + DIR * 2 + 1 : &tmb;
@@ -1297,7 +1297,7 @@ __global__ void __launch_bounds__(M3_BS) k_march3(const __grid_constant__ CUtens
   static_assert(NS >= 6, "the ring holds the 4-row window plus at least one row ahead");
   int lb;
   const int gr = group_member<GRP, GK_MARCH>(sp, lb);
-  const DevState& s = group_state<GRP>(sp, gr);
+  KB_GROUP_STATE(GRP, sp, gr);
   const CUtensorMap* mh = GRP ? sp.grp->maps + gr * 6 + 4 : &tmh;
   const CUtensorMap* mb = GRP ? sp.grp->maps + gr * 6 + 5 : &tmb;
   if (GRP && threadIdx.x == 0) {  // the issuing thread

@@ -1,7 +1,8 @@
-"""Served stream: continuous batching with HBM-budget admission; each
-request's result is the same alone and in the mix (FP32-split; bit-identical
-since every request owns its solver), all requests retire, latencies are
-reported."""
+"""Served stream: continuous batching with HBM-budget admission.  In the mix
+the 1D requests share the pool's fused launches and the 2D requests the
+group's launches (one launch per step kernel for all resident 2D solves);
+each request's result is bit-identical alone and in the mix, all requests
+retire, latencies are reported."""
 import numpy as np
 import pytest
 
@@ -50,6 +51,19 @@ def test_pooled_1d_requests_share_launches(gpu_lib):
     m = srv.run(reqs)
     assert m["requests"] == len(reqs)
     assert 0 < m["pool_launches"] < n1d * 40 * 2
+
+
+def test_2d_requests_share_group_launches(gpu_lib):
+    """The 2D requests of a stream are advanced together by the group's
+    launches: far fewer group launches than 2D request-steps times the
+    kernels of a step."""
+    reqs = S.mixed_stream(rate=400.0, duration=0.05, seed=11, max_steps=40, tol=1e-12, scale=0.08)
+    n2d = sum(1 for r in reqs if r.config["space"] == "2d2f2v")
+    assert n2d >= 2
+    srv = S.Server(precision="fp32", max_slots=8, chunk=8, hbm_budget=1 << 30)
+    m = srv.run(reqs)
+    assert m["requests"] == len(reqs)
+    assert 0 < m["group_launches"] < n2d * 40 * 8
 
 
 def test_pool_join_leave_and_accuracy(gpu_lib):
