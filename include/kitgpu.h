@@ -231,7 +231,9 @@ int kb_status(kb_handle_t* h);
  * boundaries, small enough for 32-thread cell blocks (fewer than two
  * 256-thread blocks per multiprocessor).  Members join and leave between
  * chunks (after kb_group_query reported the chunk done); while in a group a
- * handle must not be stepped on its own.  A group has its own stream.
+ * handle must not be stepped on its own, and it must leave the group before
+ * kb_destroy.  A group has its own stream and, like a handle, is not
+ * thread-safe.
  *   kb_group_create    capacity = most members at a time
  *   kb_group_add       member with its time step dt (KB_ERR_CONFIG when the
  *                      solve is not covered)
