@@ -191,7 +191,7 @@ class Server:
                     break  # the pool's chunk is in flight: join it when it returns
                 if use_pool and pool is None:
                     need = pool_bytes(self.pool_cells)
-                    if used + need > self.hbm_budget and (active or pooled):
+                    if used + need > self.hbm_budget and (active or pooled or grouped or joining):
                         break
                     pool = KBATCH.Pool(KS, max_instances=self.max_slots, max_cells=self.pool_cells)
                     used += need
@@ -210,7 +210,7 @@ class Server:
                     pooled.append(r)
                     continue
                 need = estimate_bytes(r.config, self.precision)
-                if used + need > self.hbm_budget and (active or pooled):
+                if used + need > self.hbm_budget and (active or pooled or grouped or joining):
                     break
                 queue.pop(0)
                 vs = KS.vs
