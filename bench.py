@@ -261,19 +261,28 @@ ERROR_CASES = (
 
 def error_table(args):
     """L-inf of the FP32-split form against the plain FP64 GPU path after the
-    same steps: rho, U, T (prim_errors) and q relative to max |q|."""
+    same steps: rho, U, T (prim_errors) and q relative to max |q|; and the
+    throughput of both forms on these runs (C1 Sod and C2 cavity in full,
+    the C3 physics at 128^2): the steps are timed on the host around the
+    synchronous kb_step (eager launches, no graph)."""
     import kitgpu
     rows = []
     for name, cfg, nsteps in ERROR_CASES:
         if cfg == "quadrant128":
             cfg = quadrant_cfg(**dict(WORKLOAD, nx=128, ny=128))
         KS = kitgpu.solver_set(cfg)
-        outs = {}
+        outs, rate, msps = {}, {}, {}
         for prec in ("fp32", "fp64"):
             ctr = kitgpu.init_fvm(KS, prec)[0]
             dt = kitgpu.timestep(KS, ctr, 0.0)
             n = nsteps or int(np.floor(KS.set.maxTime / dt)) + 1
+            t0 = time.perf_counter()
             kitgpu.step(KS, ctr, dt, n)
+            el = time.perf_counter() - t0
+            c = ctr.handle.cfg
+            cv = c.nx * (c.ny if KS.dim == 2 else 1) * ctr.handle.nvel
+            rate[prec] = cv * n / el
+            msps[prec] = 1e3 * el / n
             outs[prec] = ctr.handle.download()
             ctr.handle.close()
         vs = KS.vs
@@ -285,6 +294,8 @@ def error_table(args):
         wa, wb = outs["fp32"]["w"], outs["fp64"]["w"]
         rows.append({"case": name, "steps": n, "rho": e[0], "U": e[1], "T": e[2],
                      "q_rel_to_max": eq,
+                     "cv_per_s": rate, "ms_per_step": msps,
+                     "speedup_fp32_vs_fp64": rate["fp32"] / rate["fp64"],
                      "mass_fp32_vs_fp64": float(abs(wa[:, 0].sum() - wb[:, 0].sum())
                                                 / wb[:, 0].sum())})
     return {"reference": "plain FP64 GPU path (held to the FP64 oracle within 1e-12 by the "
