@@ -359,8 +359,10 @@ int kb_destroy(kb_handle_t* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   if (h->ev_done) cudaEventDestroy(h->ev_done);
-  for (int k = 0; k < 2; ++k)
+  for (int k = 0; k < 2; ++k) {
     if (h->agraph[k]) cudaGraphExecDestroy(h->agraph[k]);
+    if (h->sgraph[k]) cudaGraphExecDestroy(h->sgraph[k]);
+  }
   if (h->h_res) cudaFreeHost(h->h_res);
   for (void* p : h->allocs) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -593,6 +595,34 @@ static int timed_step(kb_handle* h, double dt, cudaEvent_t* ev) {
   return n;
 }
 
+static int enqueue_steps(kb_handle* h, double dt, int nsteps);
+static void drop_step_graphs(kb_handle* h);
+
+// Two steps from the current buffer recorded as a CUDA graph for kb_step,
+// cached per starting buffer and dt; null when recording failed (the caller
+// then steps eagerly).
+static cudaGraphExec_t step_pair_graph(kb_handle* h, double dt) {
+  const int c = h->s.cur;
+  if (h->sgraph_dt != dt) {
+    drop_step_graphs(h);
+    h->sgraph_dt = dt;
+  }
+  if (h->sgraph[c]) return h->sgraph[c];
+  cudaGraph_t gr = nullptr;
+  bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  const int n = ok ? enqueue_steps(h, dt, 2) : 0;
+  ok = cudaStreamEndCapture(h->stream, &gr) == cudaSuccess && ok;
+  h->s.cur = c;  // two recorded steps leave the buffer index where it was
+  if (ok && cudaGraphInstantiate(&h->sgraph[c], gr, 0) == cudaSuccess) {
+    h->sgraph_launches = n;
+  } else {
+    h->sgraph[c] = nullptr;
+  }
+  if (gr) cudaGraphDestroy(gr);
+  cudaGetLastError();  // a failed recording only means eager steps
+  return h->sgraph[c];
+}
+
 int kb_step(kb_handle_t* h, double dt, int32_t nsteps, double* residual) {
   if (!h) return fail(KB_ERR_ARG, "kb_step: null handle");
   if (!(dt > 0.0)) return fail(KB_ERR_ARG, "kb_step: dt must be positive");
@@ -617,12 +647,27 @@ int kb_step(kb_handle_t* h, double dt, int32_t nsteps, double* residual) {
       }
     }
   } else {
-    for (int s = 0; s < nsteps; ++s) {
+    // A long run replays two steps recorded as a CUDA graph: one graph
+    // launch per two steps instead of ~16 kernel launches, so small solves
+    // are bound by their kernels rather than by launch latency.  The first
+    // two steps run eagerly (modules load and function attributes are set
+    // outside any capture); results are those of the eager steps, bit for bit.
+    int s = 0;
+    auto eager = [&]() -> int {
       int n = kb::launch_reconstruct(h->s, h->stream);
       n += kb::launch_evolve(h->s, dt, h->stream);
       n += kb::launch_update(h->s, dt, h->stream);
-      KB_TRY(check_launch(h, n));
+      return check_launch(h, n);
+    };
+    for (; s < nsteps && s < 2; ++s) KB_TRY(eager());
+    if (nsteps - s >= 4) {
+      cudaGraphExec_t gx = step_pair_graph(h, dt);
+      for (; gx && s + 2 <= nsteps; s += 2) {
+        KB_CUDA(cudaGraphLaunch(gx, h->stream));
+        h->launches += h->sgraph_launches;
+      }
     }
+    for (; s < nsteps; ++s) KB_TRY(eager());
   }
   h->evolved = false;
   return read_residual(h, residual);
@@ -655,6 +700,14 @@ static void drop_graphs(kb_handle* h) {
     if (h->agraph[k]) {
       cudaGraphExecDestroy(h->agraph[k]);
       h->agraph[k] = nullptr;
+    }
+}
+
+static void drop_step_graphs(kb_handle* h) {
+  for (int k = 0; k < 2; ++k)
+    if (h->sgraph[k]) {
+      cudaGraphExecDestroy(h->sgraph[k]);
+      h->sgraph[k] = nullptr;
     }
 }
 
@@ -780,6 +833,7 @@ int kb_set_tuning(kb_handle_t* h, const int32_t* params, int32_t n) {
   }
   for (int k = 0; k < n; ++k) h->s.tune[k] = params[k];
   drop_graphs(h);  // recorded launch shapes are stale
+  drop_step_graphs(h);
   return KB_OK;
 }
 

@@ -33,6 +33,10 @@ struct kb_handle {
   // chunks of kb_step_async replayed as CUDA graphs: one executable graph per
   // starting buffer index, valid for one (dt, nsteps) and the current tuning
   cudaGraphExec_t agraph[2] = {nullptr, nullptr};
+  // kb_step's long runs: two steps recorded per starting buffer for one dt
+  cudaGraphExec_t sgraph[2] = {nullptr, nullptr};
+  double sgraph_dt = 0.0;
+  int64_t sgraph_launches = 0;
   double agraph_dt = 0.0;
   int agraph_n = 0;
   int64_t agraph_launches = 0;
