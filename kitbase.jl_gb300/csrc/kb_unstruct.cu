@@ -198,28 +198,32 @@ struct UsGeo {
   R n1, n2, len, sgn;
 };
 
-__device__ __forceinline__ void us_load_rec(const UsDev& d, int s, int4& rec, UsGeo<float> (&g)[3]) {
-  rec = __ldg(d.step_rec + s);
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    const float4 q = __ldg(d.step_geo32 + 3L * s + j);
-    g[j].n1 = q.x;
-    g[j].n2 = q.y;
-    g[j].len = q.z;
-    g[j].sgn = q.w;
-  }
+// Stage the records of a CTA's nloc cells (cell, neighbours, per-face
+// geometry) into shared memory: one coalesced read per CTA, so the warps'
+// cell loops hold no prefetched record in registers.
+__device__ __forceinline__ void us_stage_rec(const UsDev& d, int c0, int nloc, int4* RS, float4* GS) {
+  for (int t = threadIdx.x; t < nloc; t += US_T) RS[t] = __ldg(d.step_rec + c0 + t);
+  for (int t = threadIdx.x; t < 3 * nloc; t += US_T) GS[t] = __ldg(d.step_geo32 + 3L * c0 + t);
 }
-__device__ __forceinline__ void us_load_rec(const UsDev& d, int s, int4& rec, UsGeo<double> (&g)[3]) {
-  rec = __ldg(d.step_rec + s);
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    const UsG64 q = d.step_geo64[3L * s + j];
-    g[j].n1 = q.n1;
-    g[j].n2 = q.n2;
-    g[j].len = q.len;
-    g[j].sgn = q.sgn;
-  }
+__device__ __forceinline__ void us_stage_rec(const UsDev& d, int c0, int nloc, int4* RS, UsG64* GS) {
+  for (int t = threadIdx.x; t < nloc; t += US_T) RS[t] = __ldg(d.step_rec + c0 + t);
+  for (int t = threadIdx.x; t < 3 * nloc; t += US_T) GS[t] = d.step_geo64[3L * c0 + t];
 }
+__device__ __forceinline__ void us_geo(const float4& q, UsGeo<float>& g) {
+  g.n1 = q.x;
+  g.n2 = q.y;
+  g.len = q.z;
+  g.sgn = q.w;
+}
+__device__ __forceinline__ void us_geo(const UsG64& q, UsGeo<double>& g) {
+  g.n1 = q.n1;
+  g.n2 = q.n2;
+  g.len = q.len;
+  g.sgn = q.sgn;
+}
+template <typename R> struct UsGeoRow;
+template <> struct UsGeoRow<float> { using T = float4; };
+template <> struct UsGeoRow<double> { using T = UsG64; };
 
 // One CTA of US_T threads steps cb consecutive cells of the step list:
 // (1) each warp takes cells wid, wid + 4, ..., forms Dh, Db (kept in shared
@@ -232,7 +236,7 @@ __device__ __forceinline__ void us_load_rec(const UsDev& d, int s, int4& rec, Us
 // fraction of the FP32 rate, so per-cell FP64 work is kept to the lane-per-
 // cell phase).
 template <typename R, bool SHAK>
-__global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? 5 : 3)
+__global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? (SHAK ? 6 : 7) : 3)
     k_us_step(UsDev d, double dt, int cb, const R* __restrict__ hin,
                                                   const R* __restrict__ bin, R* __restrict__ hout,
                                                   R* __restrict__ bout) {
@@ -242,6 +246,9 @@ __global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? 5 : 3)
   double* S = (double*)us_smem;                  // [cb][US_NM]
   R* P = (R*)(S + cb * US_NM);                   // [cb][US_NP] (room for doubles)
   R* D = (R*)(S + cb * (US_NM + US_NP));         // [cb][2][vstride]: Dh, Db
+  using GR = typename UsGeoRow<R>::T;
+  GR* GS = (GR*)(D + (long)cb * 2 * d.vstride);  // [cb][3] face geometry
+  int4* RS = (int4*)(GS + 3 * cb);               // [cb] cell and neighbours
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int c0 = blockIdx.x * cb;
   const int nloc = min(cb, d.nstep - c0);
@@ -253,29 +260,30 @@ __global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? 5 : 3)
   constexpr bool shak = SHAK;
   const R rdt = R(dt);
 
-  // (1) face fluxes and velocity sums.  Each stepped cell's record (the
-  // cell, its three neighbours, and per face n1, n2, len and sg |n|^2) is
-  // one contiguous read, fetched a cell ahead.
-  int4 rec = make_int4(0, 0, 0, 0);
-  UsGeo<R> geo[3];
-  if (wid < nloc) us_load_rec(d, c0 + wid, rec, geo);
+  // (1) face fluxes and velocity sums.  The records of the CTA's cells (the
+  // cell, its three neighbours, and per face n1, n2, len and sg |n|^2) are
+  // staged in shared memory first.
+  us_stage_rec(d, c0, nloc, RS, GS);
+  __syncthreads();
   for (int i = wid; i < nloc; i += US_W) {
+    const int4 rec = RS[i];
     const int c = rec.x;
     UsFace<R> F[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      F[j].n1 = geo[j].n1;
-      F[j].n2 = geo[j].n2;
-      F[j].a = FAST ? rmul(rdt, geo[j].len) : R(dt);
-      F[j].l = FAST ? R(1) : geo[j].len;
-      F[j].sgn = geo[j].sgn;
-      F[j].left = geo[j].sgn > R(0);
+      UsGeo<R> geo;
+      us_geo(GS[3 * i + j], geo);
+      F[j].n1 = geo.n1;
+      F[j].n2 = geo.n2;
+      F[j].a = FAST ? rmul(rdt, geo.len) : R(dt);
+      F[j].l = FAST ? R(1) : geo.len;
+      F[j].sgn = geo.sgn;
+      F[j].left = geo.sgn > R(0);
       F[j].sg = F[j].left ? R(1) : R(-1);
     }
     F[0].nb = rec.y;
     F[1].nb = rec.z;
     F[2].nb = rec.w;
-    if (i + US_W < nloc) us_load_rec(d, c0 + i + US_W, rec, geo);
     const R2* Hc = (const R2*)(hin + (long)c * vs);
     const R2* Bc = (const R2*)(bin + (long)c * vs);
     const R2* H0 = (const R2*)(hin + (long)F[0].nb * vs);
@@ -406,7 +414,7 @@ __global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? 5 : 3)
   if (wid == 0) {
     double rr[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     if (lane < nloc) {
-      const int c = d.step_rec[c0 + lane].x;
+      const int c = RS[lane].x;
       const double* Sc = S + lane * US_NM;
       double* w = d.w + 4L * c;
       double* p = d.prim + 4L * c;
@@ -456,7 +464,7 @@ __global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? 5 : 3)
   // (3) relaxation of h, b
   const R Km5 = R(d.Kb - 5.0), Km3 = R(d.Kb - 3.0);
   for (int i = wid; i < nloc; i += US_W) {
-    const int c = d.step_rec[c0 + i].x;
+    const int c = RS[i].x;
     const R* Pc = P + i * US_NP;
     const R rn = Pc[0], U = Pc[1], V = Pc[2], lam = Pc[3], cB = Pc[4];
     const R kk = Pc[5], i1k = Pc[6], ia = Pc[7];
@@ -684,13 +692,13 @@ static std::vector<int> us_levels(int ncell, const int32_t* cell_nb, const int32
 }
 
 // Cells per CTA of the step kernel and its shared memory: the per-velocity
-// flux sums of cb cells (2 nvel values each) plus the per-cell sums and
-// parameters.  cb = 0 picks the largest count up to 32 within 32 KB of flux
+// flux sums of cb cells (2 nvel values each) plus the per-cell sums,
+// parameters and staged records (cell, neighbours, face geometry).  cb = 0 picks the largest count up to 32 within 32 KB of flux
 // sums (at least one cell).
 static int us_set_cells_per_cta(kb_us* U, int cb) {
   const kb::UsDev& d = U->d;
   const size_t esz = U->prec == KB_PREC_FP64 ? 8 : 4;
-  const size_t per = 2 * (size_t)d.vstride * esz;
+  const size_t per = 2 * (size_t)d.vstride * esz + sizeof(int4) + 12 * esz;
   if (cb == 0) cb = (int)std::max<size_t>(1, std::min<size_t>(kb::US_CB, (32u << 10) / per));
   if (cb < 1 || cb > kb::US_CB) return usfail(KB_ERR_ARG, "cells per CTA must be 1 .. 32");
   const size_t smem = (sizeof(double) * (kb::US_NM + kb::US_NP) + per) * cb;
