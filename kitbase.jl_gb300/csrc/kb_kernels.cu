@@ -790,6 +790,53 @@ __global__ void k_conv(DT* __restrict__ dst, const ST* __restrict__ src, long nc
     for (int v = threadIdx.x; v < nvel; v += blockDim.x) dst[c * dvs + v] = (DT)src[c * svs + v];
   }
 }
+// The same conversion when both layouts are one dense array (nvel equal to
+// the device row stride): element pairs, CONV_U of them per thread with all
+// loads issued before the first store.  Across the host link (page-locked
+// host arrays read or written in place) each load waits microseconds, so
+// the bandwidth is the number of bytes in flight: 16-byte FP64 pairs, eight
+// per thread.
+constexpr int CONV_T = 256, CONV_U = 8;
+template <typename T> struct ConvPair;
+template <> struct ConvPair<float> {
+  using T = float2;
+  __device__ static float2 make(double a, double b) { return make_float2((float)a, (float)b); }
+};
+template <> struct ConvPair<double> {
+  using T = double2;
+  __device__ static double2 make(double a, double b) { return make_double2(a, b); }
+};
+template <typename DT, typename ST>
+__global__ void __launch_bounds__(CONV_T) k_conv_flat(DT* __restrict__ dst, const ST* __restrict__ src,
+                                                      long npair) {
+  using S2 = typename ConvPair<ST>::T;
+  using D2 = typename ConvPair<DT>::T;
+  const long p0 = (long)blockIdx.x * (CONV_T * CONV_U) + threadIdx.x;
+  S2 v[CONV_U];
+#pragma unroll
+  for (int u = 0; u < CONV_U; ++u) {
+    const long p = p0 + (long)u * CONV_T;
+    if (p < npair) v[u] = ((const S2*)src)[p];
+  }
+#pragma unroll
+  for (int u = 0; u < CONV_U; ++u) {
+    const long p = p0 + (long)u * CONV_T;
+    if (p < npair) ((D2*)dst)[p] = ConvPair<DT>::make((double)v[u].x, (double)v[u].y);
+  }
+}
+// Dense, even-length arrays whose pair loads and stores are aligned take the
+// pair kernel.
+static bool conv_flat_ok(const void* dst, size_t desz, const void* src, size_t sesz, int nvel, int vstride) {
+  return nvel == vstride && nvel % 2 == 0 && (uintptr_t)dst % (2 * desz) == 0 &&
+         (uintptr_t)src % (2 * sesz) == 0;
+}
+template <typename DT, typename ST>
+static void conv_flat(DT* dst, const ST* src, long n, cudaStream_t st) {
+  const long npair = n / 2;
+  const unsigned nb = (unsigned)((npair + CONV_T * CONV_U - 1) / (CONV_T * CONV_U));
+  k_conv_flat<DT, ST><<<nb, CONV_T, 0, st>>>(dst, src, npair);
+}
+
 __global__ void k_pack_w(double* dst4, const double* src, long ncell, int nw) {
   long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncell) return;
@@ -1041,6 +1088,11 @@ int launch_slopes_dump(DevState& s, double* sh, double* sb, cudaStream_t st) {
 int launch_convert_in(void* dst, int prec, const double* src, long ncell, int nvel, int vstride,
                       cudaStream_t st) {
   if (ncell * nvel == 0) return 0;
+  if (conv_flat_ok(dst, prec == 0 ? 8 : 4, src, 8, nvel, vstride)) {
+    if (prec == 0) conv_flat((double*)dst, src, ncell * nvel, st);
+    else conv_flat((float*)dst, src, ncell * nvel, st);
+    return 1;
+  }
   const int cpb = std::max(1, 2048 / nvel);
   const unsigned nb = (unsigned)((ncell + cpb - 1) / cpb);
   if (prec == 0) k_conv<double, double><<<nb, 256, 0, st>>>((double*)dst, src, ncell, nvel, vstride, nvel, cpb);
@@ -1051,6 +1103,11 @@ int launch_convert_in(void* dst, int prec, const double* src, long ncell, int nv
 int launch_convert_out(double* dst, int prec, const void* src, long ncell, int nvel, int vstride,
                        cudaStream_t st) {
   if (ncell * nvel == 0) return 0;
+  if (conv_flat_ok(dst, 8, src, prec == 0 ? 8 : 4, nvel, vstride)) {
+    if (prec == 0) conv_flat(dst, (const double*)src, ncell * nvel, st);
+    else conv_flat(dst, (const float*)src, ncell * nvel, st);
+    return 1;
+  }
   const int cpb = std::max(1, 2048 / nvel);
   const unsigned nb = (unsigned)((ncell + cpb - 1) / cpb);
   if (prec == 0)
