@@ -55,7 +55,7 @@ struct UsDev {
   const float4* step_geo32;  // [nstep][3] per face: n1, n2, len, sg |n|^2 (FP32 form)
   const UsG64* step_geo64;   // [nstep][3] the same in FP64
   const int* avg_list;       // type-3 cells by dependency level [navg]
-  const double* cell_area;   // [ncell]
+  const double* cell_iarea;  // [ncell] 1 / area (one IEEE division per cell, on the host)
   const double* cell_mindx;  // [ncell] smallest centre-to-edge distance
   const double* u;           // velocity grid, FP64
   const double* v;
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? (SHAK ? 6 : 7) : 3)
       double* w = d.w + 4L * c;
       double* p = d.prim + 4L * c;
       const double rho_o = p[0], U_o = p[1], V_o = p[2], lam_o = p[3];
-      const double ia = 1.0 / d.cell_area[c];
+      const double ia = d.cell_iarea[c];
       const double A[4] = {Sc[0], Sc[1], Sc[2], 0.5 * (Sc[3] + Sc[4])};
       double wo[4], pn[4];
       for (int k = 0; k < 4; ++k) {
@@ -433,25 +433,53 @@ __global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? (SHAK ? 6 : 7) : 3)
         rr[4 + k] = fabs(w[k]);
       }
       if (!(pn[0] > 0.0) || !(pn[3] > 0.0) || !isfinite(pn[0]) || !isfinite(pn[3])) atomicOr(d.status, 1);
-      const double k = dt / vhs_time<FAST>(pn[0], pn[3], d.mu_ref, d.omega);
       R* Pc = P + lane * US_NP;
-      Pc[0] = R(pn[0] * (pn[3] / PI));  // Maxwellian amplitude
-      Pc[1] = R(pn[1]);
-      Pc[2] = R(pn[2]);
-      Pc[3] = R(pn[3]);
-      Pc[4] = R(d.Kb / (2.0 * pn[3]));  // B / H
-      Pc[5] = R(k);
-      Pc[6] = R(1.0 / (1.0 + k));
-      Pc[7] = R(ia);
-      if (shak) {  // shakhov 2F2V of the old state (src/Theory/theory_equilibrium.jl:227-238)
-        const double sfac = 0.8 * (1.0 - d.Pr) * (lam_o * lam_o) / rho_o;
-        Pc[8] = R(sfac * 0.5 * Sc[5]);
-        Pc[9] = R(sfac * 0.5 * Sc[6]);
-        Pc[10] = R(rho_o * (lam_o / PI));
-        Pc[11] = R(d.Kb / (2.0 * lam_o));
-        Pc[12] = R(lam_o);
-        Pc[13] = R(U_o);
-        Pc[14] = R(V_o);
+      if constexpr (FAST) {
+        // The relaxation's FP32 coefficients are formed in FP32: FP64
+        // division runs on GB300's slow FP64 pipe while the CTA's other
+        // warps wait at the barrier.
+        const float rho = (float)pn[0], lam = (float)pn[3], Kb = (float)d.Kb;
+        const float tau = (float)(2.0 * d.mu_ref) * powf(lam, (float)(1.0 - d.omega)) / rho;
+        const float k = (float)dt / tau;
+        Pc[0] = rho * (lam * (float)(1.0 / PI));  // Maxwellian amplitude
+        Pc[1] = R(pn[1]);
+        Pc[2] = R(pn[2]);
+        Pc[3] = lam;
+        Pc[4] = Kb / (2.f * lam);  // B / H
+        Pc[5] = k;
+        Pc[6] = 1.f / (1.f + k);
+        Pc[7] = R(ia);
+        if (shak) {  // shakhov 2F2V of the old state (src/Theory/theory_equilibrium.jl:227-238)
+          const float ro = (float)rho_o, lo = (float)lam_o;
+          const float sfac = (float)(0.8 * (1.0 - d.Pr)) * (lo * lo) / ro;
+          Pc[8] = sfac * 0.5f * (float)Sc[5];
+          Pc[9] = sfac * 0.5f * (float)Sc[6];
+          Pc[10] = ro * (lo * (float)(1.0 / PI));
+          Pc[11] = Kb / (2.f * lo);
+          Pc[12] = lo;
+          Pc[13] = R(U_o);
+          Pc[14] = R(V_o);
+        }
+      } else {
+        const double k = dt / vhs_time<FAST>(pn[0], pn[3], d.mu_ref, d.omega);
+        Pc[0] = R(pn[0] * (pn[3] / PI));  // Maxwellian amplitude
+        Pc[1] = R(pn[1]);
+        Pc[2] = R(pn[2]);
+        Pc[3] = R(pn[3]);
+        Pc[4] = R(d.Kb / (2.0 * pn[3]));  // B / H
+        Pc[5] = R(k);
+        Pc[6] = R(1.0 / (1.0 + k));
+        Pc[7] = R(ia);
+        if (shak) {  // shakhov 2F2V of the old state (src/Theory/theory_equilibrium.jl:227-238)
+          const double sfac = 0.8 * (1.0 - d.Pr) * (lam_o * lam_o) / rho_o;
+          Pc[8] = R(sfac * 0.5 * Sc[5]);
+          Pc[9] = R(sfac * 0.5 * Sc[6]);
+          Pc[10] = R(rho_o * (lam_o / PI));
+          Pc[11] = R(d.Kb / (2.0 * lam_o));
+          Pc[12] = R(lam_o);
+          Pc[13] = R(U_o);
+          Pc[14] = R(V_o);
+        }
       }
     }
     // residual partials of update! (src/Solver/solver_update.jl:465-467)
@@ -894,7 +922,11 @@ extern "C" int kb_us_create(const kb_config_t* cfg, int32_t ncell, int32_t nface
     up(sg64, g64.data(), sizeof(kb::UsG64) * g64.size());
   }
   if (!avg.empty()) up(al, avg.data(), sizeof(int) * avg.size());
-  up(ca, cell_area, sizeof(double) * ncell);
+  {
+    std::vector<double> ia(ncell);
+    for (long i = 0; i < ncell; ++i) ia[i] = 1.0 / cell_area[i];
+    up(ca, ia.data(), sizeof(double) * ncell);
+  }
   up(cm, cell_mindx, sizeof(double) * ncell);
   up(du, f64.data(), sizeof(double) * VS);
   up(dv, f64.data() + VS, sizeof(double) * VS);
@@ -913,7 +945,7 @@ extern "C" int kb_us_create(const kb_config_t* cfg, int32_t ncell, int32_t nface
   d.step_geo64 = sg64;
   d.avg_list = al;
   d.status = st;
-  d.cell_area = ca;
+  d.cell_iarea = ca;
   d.cell_mindx = cm;
   d.u = du;
   d.v = dv;
