@@ -234,7 +234,9 @@ template <> struct UsGeoRow<double> { using T = UsG64; };
 // their cells.  The FP32 form takes its face geometry from an FP32 table and
 // evaluates the cell's transcendentals in FP32 (GB300 runs FP64 at a small
 // fraction of the FP32 rate, so per-cell FP64 work is kept to the lane-per-
-// cell phase).
+// cell phase).  Launch bounds: the FP32 form fits 7 CTAs per SM (BGK, 72
+// registers) or 6 (Shakhov, whose heat-flux sums need more registers; 7 would
+// spill); the FP64 form 3.
 template <typename R, bool SHAK>
 __global__ void __launch_bounds__(US_T, sizeof(R) == 4 ? (SHAK ? 6 : 7) : 3)
     k_us_step(UsDev d, double dt, int cb, const R* __restrict__ hin,
