@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from kitgpu import serve as S
+from kitgpu import _native as N
 from kitgpu._native import KitGPUError
 
 
@@ -87,7 +88,7 @@ def make_fakes(fleet, precision):
             cells = KS.ps.nx + 2 * KS.ps.ng
             if (len(self.slots) >= self.cap
                     or sum(s[2] for s in self.slots.values()) + cells > self.max_cells):
-                raise KitGPUError("pool full")
+                raise KitGPUError(N.KB_ERR_NOMEM, "pool full")
             slot = min(set(range(self.cap)) - set(self.slots))
             self.slots[slot] = [0, decay_of(KS.ps.nx), cells]
             fleet.routes[(KS.ps.nx, 1, KS.vs.nu)] = "pool"
@@ -123,7 +124,7 @@ def make_fakes(fleet, precision):
 
         def add(self, handle, dt):
             if handle.cfg.nx > 40:  # the ABI refuses grids its cell blocks do not cover
-                raise KitGPUError("grid too large for the group")
+                raise KitGPUError(N.KB_ERR_CONFIG, "grid too large for the group")
             self.members.append(handle)
             fleet.routes[handle.key] = "group"
 
@@ -243,3 +244,19 @@ def test_a_request_larger_than_the_budget_runs_alone(fake_device):
     m = srv.run(reqs)
     assert m["requests"] == len(reqs)
     assert fleet.peak_residents == 1  # admitted only when nothing else is resident
+
+
+def test_group_refusal_falls_back_to_own_stream(fake_device):
+    """A 2D request under the group's size threshold that the group kernels
+    do not cover (the ABI refuses it) runs on its own stream instead."""
+    fleet = fake_device("fp32")
+    reqs = [S.Request(0, 0.0, S.cavity_request(48, 8, 1e-2), 40, 1e-6),   # refused: own stream
+            S.Request(1, 0.0, S.cavity_request(12, 8, 1e-2), 40, 1e-6),   # grouped
+            S.Request(2, 0.0, S.sod_request(64, 32), 40, 1e-6)]           # pooled
+    srv = S.Server(precision="fp32", max_slots=4, chunk=8, hbm_budget=1 << 30)
+    m = srv.run(reqs)
+    assert m["requests"] == 3
+    assert fleet.routes[(48, 48, 8)] == "stream"
+    assert fleet.routes[(12, 12, 8)] == "group"
+    assert fleet.routes[(64, 1, 32)] == "pool"
+    check_retired(srv, reqs, 8)
