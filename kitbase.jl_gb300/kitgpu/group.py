@@ -9,6 +9,7 @@ Members: 2D FP32-split KCU solves (BGK or Shakhov, one model per group)
 without ghost-filled boundaries -- the served lid-driven cavities.
 """
 import ctypes
+import time
 
 import numpy as np
 
@@ -68,11 +69,17 @@ class Group:
                                         ctypes.byref(ready)))
         return bool(ready.value), res[:n], st[:n]
 
-    def wait(self):
+    def wait(self, timeout=None):
+        """Poll until the last chunk is done; TimeoutError after `timeout`
+        seconds (None: no limit)."""
+        t_end = None if timeout is None else time.monotonic() + timeout
         while True:
             ready, res, st = self.query()
             if ready:
                 return res, st
+            if t_end is not None and time.monotonic() > t_end:
+                raise TimeoutError("group chunk not done after %.3g s" % timeout)
+            time.sleep(0)
 
     def launches(self):
         n, l = ctypes.c_int32(), ctypes.c_int64()
